@@ -1,0 +1,205 @@
+/*
+ * kevd.h -- C ABI of the GB300 kernel low-rank pipeline.
+ *
+ * The reference (cval26/kernel_evd) exposes its three stages as standalone
+ * programs whose boundary is a process plus files:
+ *
+ *   ./cuband    ks_bandwidth.cu:339-667   bandwidth calibration  -> bw0.out
+ *   ./cuarpclm  ks_arpclm.cu:566-1152     block RPCholesky       -> linv, spiv
+ *   ./cukevd    ks_kevd.cu:419-2403       bistochastic EVD       -> lam, U
+ *
+ * Each entry point below replaces the compute of one stage (or one piece of
+ * it) and is what a caller of that stage binds: the drivers in
+ * kernel_evd_gb300/csrc/drivers reproduce the programs' invocation and file
+ * layout on top of it, and the Python package binds it through ctypes.
+ *
+ * Conventions
+ *   - Every function returns an int status (enum kevd_status); no exceptions
+ *     or exits cross the boundary.  kevd_last_error() describes the failure.
+ *   - Pointers documented "device" are caller-owned device buffers; "host"
+ *     are caller-owned host buffers.  Sample matrices X are row-major
+ *     N x d float32 (one sample per row, d contiguous).
+ *   - stream is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     Calls enqueue work on it and return after the host-visible outputs are
+ *     written (they synchronise the stream when they return host data).
+ *   - A context is bound to one device and is not internally locked: use one
+ *     context per host thread.
+ *   - Kernel: K(i,j) = exp(-scale * ||x_i - x_j||^2).  The Hankel view of the
+ *     reference uses scale = 1/(Nq*bw) (ks_arpclm.cu:275); dense states use
+ *     scale = 1/eps.
+ */
+#ifndef KEVD_H
+#define KEVD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kevd_ctx kevd_ctx;
+
+enum kevd_status {
+    KEVD_OK = 0,
+    KEVD_ERR_ARG = 1,           /* invalid argument or unsupported size       */
+    KEVD_ERR_CUDA = 2,          /* CUDA runtime / cuBLAS / cuSOLVER failure   */
+    KEVD_ERR_NONPOS_DTIL = 3,   /* dtil <= 0: ks_kevd.cu:1170-1181 (abort 2)  */
+    KEVD_ERR_POTRF = 4,         /* chol(A+sI) failed: ks_kevd.cu:1510-1520 (3)*/
+    KEVD_ERR_NONPOS_QTIL = 5,   /* qtil <= 0: ks_kevd.cu:1692-1703 (abort 4)  */
+    KEVD_ERR_SYEVD = 6,         /* eigensolver failed: ks_kevd.cu:1904-1913 (5)*/
+    KEVD_ERR_NOMEM = 7,         /* device allocation failed                   */
+    KEVD_ERR_TIMEOUT = 8        /* a bounded device wait gave up              */
+};
+
+enum kevd_precision {
+    KEVD_FP64 = 0,   /* plain form: factor and all arithmetic in FP64          */
+    KEVD_MIXED = 1   /* factor F in FP32, FP64 in the pivot block, residual
+                        diagonal, scaling vectors and the k x k eigensolve   */
+};
+
+/* ---- context ---------------------------------------------------------- */
+int kevd_ctx_create(int device, kevd_ctx** out);
+void kevd_ctx_destroy(kevd_ctx* ctx);
+const char* kevd_last_error(const kevd_ctx* ctx);
+const char* kevd_status_name(int status);
+int kevd_abi_version(void);
+
+/* ---- sample views ------------------------------------------------------ */
+
+/* Materialise the delay-embedded samples of the reference programs as rows.
+ * u: device, M*Ndata floats, time fastest.  X: device, (Ndata-Nq+1)*M x Nq.
+ * Row i = gridpoint i/N, time i%N (ks_arpclm.cu:263-268,
+ * ks_bandwidth.cu:168-169). */
+int kevd_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M,
+                     int64_t Nq, float* X, void* stream);
+
+/* Kernel block out[r*ld + c] = K(row_r, cols[c]) in FP64 (precision
+ * KEVD_FP64, out is double*) or FP32 (KEVD_MIXED, out is float*).
+ * rows: device index array, or NULL for the contiguous rows row0..row0+nrows-1.
+ * cols: device index array.  Replaces compute_kblock<T>
+ * (ks_arpclm.cu:242-280, ks_kevd.cu:302-340). */
+int kevd_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                      double scale, const int64_t* rows, int64_t row0,
+                      int64_t nrows, const int64_t* cols, int64_t ncols,
+                      int32_t precision, void* out, int64_t ld, void* stream);
+
+/* ---- stage 1: bandwidth calibration (ks_bandwidth.cu) ------------------ */
+
+/* sums[j] = sum over i > l of exp(-scales[j] * ||x_i - x_l||^2), FP64, over
+ * the strict lower triangle.  All n_scales values are accumulated in one pass
+ * over the pair tiles.  Replaces dmat_comp + 36 x kernelsum_comp
+ * (ks_bandwidth.cu:181-325, :537-577); the reference's per-summand 1/NM is
+ * applied by kevd_calibrate_select.  scales, sums: host, n_scales <= 256. */
+int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                   const double* scales, int32_t n_scales, double* sums,
+                   void* stream);
+
+/* Host post-processing of ks_bandwidth.cu:612-642 in FP64:
+ * logS[i] = log(2 sums[i]/NM + 1); slope[i-1] = centred difference at bw[i]
+ * (n-2 values); idmax = first arg-max; eopt = bw[idmax+1];
+ * mdim = 2 slope[idmax].  All pointers host. */
+int kevd_calibrate_select(const double* bw, const double* sums, int32_t n,
+                          int64_t NM, double* logS, double* slope,
+                          int32_t* idmax, double* eopt, double* mdim);
+
+/* Squared-distance median over pairs i > l.  n_pairs == 0: exact, over all
+ * N(N-1)/2 pairs (lower median).  n_pairs > 0: over the seeded sample of
+ * pair indices (pi[s], pl[s]) given on the device. */
+int kevd_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                     const int64_t* pi, const int64_t* pl, int64_t n_pairs,
+                     double* median, void* stream);
+
+/* ---- stage 2: block RPCholesky (ks_arpclm.cu) -------------------------- */
+
+typedef struct {
+    int64_t k_max;          /* factor capacity (target rank)                 */
+    int32_t block;          /* proposals per round b, 1..128                  */
+    int32_t max_rounds;     /* round limit                                    */
+    double tol;             /* rejection tolerance (reference: 1e-10)         */
+    double err_target;      /* stop once trace error <= this (0: never)       */
+    uint64_t seed;          /* Philox key when uniforms == NULL               */
+    const double* uniforms; /* host, optional: max_rounds x 2 x block draws in
+                               (0,1]; [r][0][:] proposals, [r][1][:] accepts  */
+    int32_t precision;      /* enum kevd_precision                            */
+} kevd_rpchol_params;
+
+typedef struct {
+    int64_t rank;           /* realised rank r                                */
+    int32_t rounds;         /* rounds executed                                */
+    double trace_error;     /* tr(K - F F^T)/tr(K) after the last round       */
+} kevd_rpchol_result;
+
+/* Factor K ~= F F^T with F = K(:,S) L^{-T}.  F: device, N x ldF, double
+ * (KEVD_FP64) or float (KEVD_MIXED), ldF >= k_max; columns [0, rank) are
+ * written.  piv: host, k_max int64 (pivots in acceptance order, the
+ * reference's /spiv).  err, accepted: host, max_rounds entries (per-round
+ * trace error and accepted count, the reference's round table
+ * ks_arpclm.cu:1129-1136).  Replaces the round loop ks_arpclm.cu:793-1046. */
+int kevd_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                double scale, const kevd_rpchol_params* params, void* F,
+                int64_t ldF, int64_t* piv, double* err, int32_t* accepted,
+                kevd_rpchol_result* result, void* stream);
+
+/* The reference's /linv output: L^{-1} (r x r, column-major, lower, zeros
+ * stored) with L = F(S,:) (ks_arpclm.cu:1055-1095).  F: device; piv: host;
+ * Linv: host. */
+int kevd_linv_from_factor(kevd_ctx* ctx, const void* F, int32_t precision,
+                          int64_t ldF, const int64_t* piv, int64_t r,
+                          double* Linv, void* stream);
+
+/* ---- stage 3: bistochastic normalisation + EVD (ks_kevd.cu) ------------ */
+
+typedef struct {
+    double trace_A;         /* tr(A), A = F^T Dtil^{-2} F                     */
+    double shift;           /* s = DBL_EPSILON tr(A) (ks_kevd.cu:1481-1499)    */
+} kevd_evd_info;
+
+/* Optional host copies of the intermediates (the reference's dump points,
+ * ks_kevd.cu:483-484); any pointer may be NULL. */
+typedef struct {
+    double* c1;    /* k      F^T 1                                           */
+    double* dtil;  /* N      F c1                                            */
+    double* cq;    /* k      F^T dtil^{-1}                                   */
+    double* qtil;  /* N      F cq                                            */
+    double* A;     /* k x k  F^T Dtil^{-2} F   (column-major, full)          */
+    double* B;     /* k x k  F^T Qtil^{-1} F                                 */
+    double* W;     /* k x k  R B R^T                                         */
+    double* Z;     /* k x k_out  R^{-1} V[:, top k_out] (column-major)       */
+} kevd_evd_dump;
+
+/* Bistochastic EVD of Khat = F F^T.  F: device N x ldF (double or float by
+ * precision).  lam: host, k eigenvalues ascending.  U: device, N x k_out
+ * float row-major, columns ascending (the last is the leading eigenvector),
+ * the reference's /lam and /U (ks_kevd.cu:1932-1940, :2301-2308). */
+int kevd_bistochastic_evd(kevd_ctx* ctx, const void* F, int32_t precision,
+                          int64_t N, int64_t k, int64_t ldF, int32_t k_out,
+                          double* lam, float* U, kevd_evd_info* info,
+                          kevd_evd_dump* dump, void* stream);
+
+/* F = K(:,S) L^{-T} from the reference's stage-2 outputs (/linv, /spiv), so
+ * that kevd_bistochastic_evd consumes them as ./cukevd does
+ * (ks_kevd.cu:760-2308).  piv, Linv: host (Linv r x r column-major).
+ * F: device N x ldF, double or float by precision. */
+int kevd_factor_from_linv(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                          double scale, const int64_t* piv, int64_t r,
+                          const double* Linv, int32_t precision, void* F,
+                          int64_t ldF, void* stream);
+
+/* Out-of-sample (Nystrom) eigenfunctions of new states Y (device, n x d):
+ * Uy[j,:] = (K(y_j,S) Z') / (K(y_j,S) p1'), the pass-4 formula
+ * (ks_kevd.cu:2246-2269) applied to new rows; the model (landmarks S, Z', p1')
+ * is prepared by kevd_nystrom_prepare from a factor and its EVD. */
+typedef struct kevd_model kevd_model;
+int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                         double scale, const void* F, int32_t precision,
+                         int64_t ldF, const int64_t* piv, int64_t r,
+                         int32_t k_out, kevd_model** model, void* stream);
+int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y,
+                      int64_t n, float* Uy, void* stream);
+void kevd_model_destroy(kevd_model* model);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KEVD_H */

@@ -1,0 +1,314 @@
+"""Python mirror of the three stage programs over the kevd C ABI.
+
+Stage functions keep the reference programs' vocabulary and error behaviour:
+
+* ``calibrate`` / ``select_bandwidth`` -- ``./cuband`` (ks_bandwidth.cu), the
+  pair-sum sweep and the slope/arg-max selection written to ``bw0.out``;
+* ``rpcholesky`` -- ``./cuarpclm`` (ks_arpclm.cu), pivots in acceptance order
+  (``/spiv``), the per-round table and ``linv`` (``/linv``);
+* ``bistochastic_evd`` -- ``./cukevd`` (ks_kevd.cu), eigenvalues ascending
+  (``/lam``) and the N x k_out eigenvector block ``/U``; the reference's abort
+  codes become ``KevdError`` with the matching status.
+
+Device memory is held in torch tensors (plumbing only); every compute call is
+a CUDA kernel of libkevd.so.  Nothing here falls back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import (KEVD_FP64, KEVD_MIXED, EvdDump, EvdInfo, KevdError, RpcholParams, RpcholResult,
+                   check)
+
+PRECISIONS = {"fp64": KEVD_FP64, "mixed": KEVD_MIXED}
+
+
+def _prec(p) -> int:
+    if isinstance(p, str):
+        return PRECISIONS[p]
+    return int(p)
+
+
+def _ptr(t: torch.Tensor | None):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _np_ptr(a: np.ndarray | None):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _need_cuda(t: torch.Tensor, dtype, name: str):
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+        raise ValueError(f"{name} must be a contiguous CUDA tensor of {dtype}")
+
+
+class Context:
+    """One kevd context (cuBLAS / cuSOLVER handles and device workspace)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        self.device = device
+        h = C.c_void_p()
+        st = self.lib.kevd_ctx_create(device, C.byref(h))
+        if st != 0:
+            raise KevdError(st, "kevd_ctx_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kevd_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        check(st, self.h)
+
+
+# ---- views -----------------------------------------------------------------
+def hankel_rows(ctx: Context, u: torch.Tensor, Ndata: int, M: int, Nq: int) -> torch.Tensor:
+    _need_cuda(u, torch.float32, "u")
+    N = Ndata - Nq + 1
+    X = torch.empty((N * M, Nq), dtype=torch.float32, device=u.device)
+    ctx._check(ctx.lib.kevd_hankel_rows(ctx.h, _ptr(u), Ndata, M, Nq, _ptr(X), _stream()))
+    return X
+
+
+def kernel_block(ctx: Context, X: torch.Tensor, scale: float, cols: torch.Tensor, rows=None,
+                 row0: int = 0, nrows: int | None = None, precision="fp64") -> torch.Tensor:
+    _need_cuda(X, torch.float32, "X")
+    N, d = X.shape
+    p = _prec(precision)
+    if rows is not None:
+        nrows = rows.numel()
+    elif nrows is None:
+        nrows = N - row0
+    dt = torch.float64 if p == KEVD_FP64 else torch.float32
+    out = torch.empty((nrows, cols.numel()), dtype=dt, device=X.device)
+    ctx._check(ctx.lib.kevd_kernel_block(ctx.h, _ptr(X), N, d, float(scale), _ptr(rows), row0, nrows,
+                                         _ptr(cols), cols.numel(), p, _ptr(out), cols.numel(), _stream()))
+    return out
+
+
+# ---- stage 1 ---------------------------------------------------------------
+def calibrate(ctx: Context, X: torch.Tensor, scales) -> np.ndarray:
+    """sums[j] = sum_{i>l} exp(-scales[j] ||x_i - x_l||^2) (FP64, host)."""
+    _need_cuda(X, torch.float32, "X")
+    scales = np.ascontiguousarray(scales, dtype=np.float64)
+    sums = np.zeros(scales.size, dtype=np.float64)
+    N, d = X.shape
+    ctx._check(ctx.lib.kevd_calibrate(ctx.h, _ptr(X), N, d, _np_ptr(scales), scales.size,
+                                      _np_ptr(sums), _stream()))
+    return sums
+
+
+def select_bandwidth(bw, sums, NM: int) -> dict:
+    """ks_bandwidth.cu:612-642: logS, centred slope, first arg-max, eopt, mdim."""
+    lib = _lib.load()
+    bw = np.ascontiguousarray(bw, dtype=np.float64)
+    sums = np.ascontiguousarray(sums, dtype=np.float64)
+    n = bw.size
+    logS = np.zeros(n)
+    slope = np.zeros(max(n - 2, 1))
+    idmax = C.c_int32()
+    eopt = C.c_double()
+    mdim = C.c_double()
+    st = lib.kevd_calibrate_select(_np_ptr(bw), _np_ptr(sums), n, NM, _np_ptr(logS), _np_ptr(slope),
+                                   C.byref(idmax), C.byref(eopt), C.byref(mdim))
+    check(st)
+    return dict(logS=logS, slope=slope[: n - 2], idmax=idmax.value, eopt=eopt.value, mdim=mdim.value)
+
+
+def bw0_text(bw, sel: dict) -> str:
+    """bw0.out contents (ks_bandwidth.cu:645-655)."""
+    logS, slope = sel["logS"], sel["slope"]
+    lines = [f"{bw[i]:.5e} {logS[i]:.5e} {slope[i - 1]:.5e}" for i in range(1, len(bw) - 1)]
+    return "\n".join(lines) + f"\n\n{sel['eopt']:.5e}\n{sel['mdim']:.5e}\n"
+
+
+def pair_median(ctx: Context, X: torch.Tensor, pairs=None) -> float:
+    """Lower median of ||x_i - x_l||^2 over all pairs i > l, or over given pairs."""
+    _need_cuda(X, torch.float32, "X")
+    N, d = X.shape
+    out = C.c_double()
+    if pairs is None:
+        st = ctx.lib.kevd_pair_median(ctx.h, _ptr(X), N, d, None, None, 0, C.byref(out), _stream())
+    else:
+        pi, pl = pairs
+        st = ctx.lib.kevd_pair_median(ctx.h, _ptr(X), N, d, _ptr(pi), _ptr(pl), pi.numel(), C.byref(out),
+                                      _stream())
+    ctx._check(st)
+    return out.value
+
+
+def log_sweep(median: float, n: int, lo: float = -10.0, hi: float = 10.0) -> np.ndarray:
+    return float(median) * 2.0 ** np.linspace(lo, hi, n)
+
+
+# ---- stage 2 ---------------------------------------------------------------
+@dataclass
+class Factorization:
+    F: torch.Tensor          # N x ldF (columns [0, rank) valid)
+    piv: np.ndarray          # rank pivots, acceptance order
+    err: np.ndarray          # per-round trace error
+    accepted: np.ndarray     # per-round accepted count
+    rank: int
+    rounds: int
+    trace_error: float
+    precision: int
+    scale: float = 0.0
+
+    @property
+    def factor(self) -> torch.Tensor:
+        return self.F[:, : self.rank]
+
+
+def rpcholesky(ctx: Context, X: torch.Tensor, scale: float, k_max: int, block: int = 64,
+               max_rounds: int | None = None, tol: float = 1e-10, err_target: float = 0.0,
+               seed: int = 1234, uniforms: np.ndarray | None = None, precision="mixed",
+               F: torch.Tensor | None = None) -> Factorization:
+    _need_cuda(X, torch.float32, "X")
+    N, d = X.shape
+    p = _prec(precision)
+    if max_rounds is None:
+        max_rounds = max(1, 4 * ((k_max + block - 1) // block) + 8)
+    dt = torch.float64 if p == KEVD_FP64 else torch.float32
+    if F is None:
+        F = torch.empty((N, k_max), dtype=dt, device=X.device)
+    prm = RpcholParams()
+    prm.k_max, prm.block, prm.max_rounds = k_max, block, max_rounds
+    prm.tol, prm.err_target, prm.seed, prm.precision = tol, err_target, seed & (2**64 - 1), p
+    u = None
+    if uniforms is not None:
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        if u.size < max_rounds * 2 * block:
+            raise ValueError("uniforms must hold max_rounds x 2 x block draws")
+        prm.uniforms = u.ctypes.data_as(C.POINTER(C.c_double))
+    piv = np.zeros(k_max, dtype=np.int64)
+    err = np.zeros(max_rounds, dtype=np.float64)
+    acc = np.zeros(max_rounds, dtype=np.int32)
+    res = RpcholResult()
+    ctx._check(ctx.lib.kevd_rpchol(ctx.h, _ptr(X), N, d, float(scale), C.byref(prm), _ptr(F), F.shape[1],
+                                   _np_ptr(piv), _np_ptr(err), _np_ptr(acc), C.byref(res), _stream()))
+    return Factorization(F=F, piv=piv[: res.rank].copy(), err=err[: res.rounds].copy(),
+                         accepted=acc[: res.rounds].copy(), rank=res.rank, rounds=res.rounds,
+                         trace_error=res.trace_error, precision=p, scale=float(scale))
+
+
+def linv(ctx: Context, fac: Factorization) -> np.ndarray:
+    """The reference's /linv: L^{-1} (r x r, lower) with L = F(S, :)."""
+    r = fac.rank
+    out = np.zeros((r, r), dtype=np.float64, order="F")
+    piv = np.ascontiguousarray(fac.piv, dtype=np.int64)
+    ctx._check(ctx.lib.kevd_linv_from_factor(ctx.h, _ptr(fac.F), fac.precision, fac.F.shape[1],
+                                             _np_ptr(piv), r, out.ctypes.data, _stream()))
+    return out
+
+
+def factor_from_linv(ctx: Context, X: torch.Tensor, scale: float, piv, Linv: np.ndarray,
+                     precision="fp64") -> torch.Tensor:
+    """F = K(:, S) L^{-T} from the reference's stage-2 outputs."""
+    _need_cuda(X, torch.float32, "X")
+    N, d = X.shape
+    p = _prec(precision)
+    piv = np.ascontiguousarray(piv, dtype=np.int64)
+    r = piv.size
+    Li = np.asfortranarray(Linv, dtype=np.float64)
+    dt = torch.float64 if p == KEVD_FP64 else torch.float32
+    F = torch.empty((N, r), dtype=dt, device=X.device)
+    ctx._check(ctx.lib.kevd_factor_from_linv(ctx.h, _ptr(X), N, d, float(scale), _np_ptr(piv), r,
+                                             Li.ctypes.data, p, _ptr(F), r, _stream()))
+    return F
+
+
+# ---- stage 3 ---------------------------------------------------------------
+@dataclass
+class Eigendecomposition:
+    lam: np.ndarray                 # k eigenvalues, ascending
+    U: torch.Tensor                 # N x k_out float32, columns ascending
+    trace_A: float
+    shift: float
+    dump: dict = field(default_factory=dict)
+
+
+def bistochastic_evd(ctx: Context, F: torch.Tensor, k: int | None = None, k_out: int = 32,
+                     precision=None, dump: bool = False, U: torch.Tensor | None = None) -> Eigendecomposition:
+    if not (F.is_cuda and F.dtype in (torch.float32, torch.float64) and F.stride(1) == 1):
+        raise ValueError("F must be a CUDA float32/float64 tensor with unit column stride")
+    p = KEVD_FP64 if F.dtype == torch.float64 else KEVD_MIXED
+    if precision is not None and _prec(precision) != p:
+        raise ValueError("precision does not match F's dtype")
+    N = F.shape[0]
+    ldF = F.stride(0)
+    if k is None:
+        k = F.shape[1]
+    lam = np.zeros(k, dtype=np.float64)
+    if U is None:
+        U = torch.empty((N, k_out), dtype=torch.float32, device=F.device)
+    info = EvdInfo()
+    dmp = None
+    host = {}
+    if dump:
+        host = dict(c1=np.zeros(k), dtil=np.zeros(N), cq=np.zeros(k), qtil=np.zeros(N),
+                    A=np.zeros((k, k), order="F"), B=np.zeros((k, k), order="F"),
+                    W=np.zeros((k, k), order="F"), Z=np.zeros((k, k_out), order="F"))
+        dmp = EvdDump(**{n: a.ctypes.data_as(C.POINTER(C.c_double)) for n, a in host.items()})
+    ctx._check(ctx.lib.kevd_bistochastic_evd(ctx.h, _ptr(F), p, N, k, ldF, k_out, _np_ptr(lam), _ptr(U),
+                                             C.byref(info), C.byref(dmp) if dmp is not None else None,
+                                             _stream()))
+    return Eigendecomposition(lam=lam, U=U, trace_A=info.trace_A, shift=info.shift, dump=host)
+
+
+class NystromModel:
+    """Resident landmarks + eigenfunction coefficients for out-of-sample states."""
+
+    def __init__(self, ctx: Context, X: torch.Tensor, fac: Factorization, k_out: int = 32):
+        _need_cuda(X, torch.float32, "X")
+        self.ctx = ctx
+        N, d = X.shape
+        self.d = d
+        self.k_out = k_out
+        h = C.c_void_p()
+        piv = np.ascontiguousarray(fac.piv, dtype=np.int64)
+        ctx._check(ctx.lib.kevd_nystrom_prepare(ctx.h, _ptr(X), N, d, fac.scale, _ptr(fac.F), fac.precision,
+                                                fac.F.shape[1], _np_ptr(piv), fac.rank, k_out, C.byref(h),
+                                                _stream()))
+        self.h = h
+
+    def __call__(self, Y: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        _need_cuda(Y, torch.float32, "Y")
+        n = Y.shape[0]
+        if out is None:
+            out = torch.empty((n, self.k_out), dtype=torch.float32, device=Y.device)
+        self.ctx._check(self.ctx.lib.kevd_nystrom_eval(self.ctx.h, self.h, _ptr(Y), n, _ptr(out), _stream()))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.kevd_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,309 @@
+// Stage 1: fused bandwidth-calibration pair sums and the pair-distance median.
+//
+// The reference writes every strict-lower-triangle distance to HBM
+// (dmat_comp, ks_bandwidth.cu:181-232) and re-reads the whole buffer once per
+// bandwidth (kernelsum_comp x 36, :276-325, :566-572).  Here each 128 x 128
+// pair tile is evaluated once into registers and every scale of the sweep is
+// accumulated from those registers in the same pass: no distance buffer, one
+// read of X (L2-resident), and the work is bound by the exp2 (MUFU) rate.
+//
+// Tiles cover the lower triangle ti >= tj of the 128-row tile grid; pairs with
+// i <= l, or outside [0, N), are masked to D = +inf (exp2(-inf) = 0).  Each
+// CTA is persistent over a static stride of tiles and keeps one FP64
+// accumulator per scale; warp partials are FP32 (<= 2048 terms of <= 1).  The
+// per-CTA FP64 partials go to a scratch array and a second kernel reduces them
+// in a fixed order, so the result is deterministic.
+#include "kevd_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace kevd {
+
+constexpr int kCalTile = 128;
+constexpr int kCalMaxScales = 256;
+constexpr int kCalMaxD = 128;
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Tile index t of the lower-triangular tile grid -> (ti, tj), ti >= tj.
+__device__ __forceinline__ void tri_tile(int64_t t, int64_t& ti, int64_t& tj) {
+    int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    ti = i;
+    tj = t - i * (i + 1) / 2;
+}
+
+// Loads rows [r0, r0+128) of X into a [128][d+1] shared tile (zeros past N).
+__device__ __forceinline__ void load_rows(const float* __restrict__ X, int64_t N, int d,
+                                          int64_t r0, float* dst) {
+    const int dp = d + 1;
+    for (int e = threadIdx.x; e < kCalTile * d; e += blockDim.x) {
+        const int rr = e / d, kk = e - rr * d;
+        const int64_t r = r0 + rr;
+        dst[rr * dp + kk] = (r < N) ? X[r * d + kk] : 0.f;
+    }
+}
+
+// 8 x 8 squared distances of thread (ty, tx): rows ty + 16a, cols tx + 16b.
+__device__ __forceinline__ void tile_dist(const float* xi, const float* xj, int d, int ty, int tx,
+                                          float (&D)[8][8]) {
+    const int dp = d + 1;
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) D[a][b] = 0.f;
+    for (int k = 0; k < d; ++k) {
+        float vi[8], vj[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * dp + k];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * dp + k];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const float t = vi[a] - vj[b];
+                D[a][b] = fmaf(t, t, D[a][b]);
+            }
+    }
+}
+
+__global__ void __launch_bounds__(256, 2)
+calibrate_tiles_kernel(const float* __restrict__ X, int64_t N, int d,
+                       const float* __restrict__ c2, int n_scales, int64_t n_tiles,
+                       double* __restrict__ partial) {
+    extern __shared__ float sm[];
+    const int dp = d + 1;
+    float* xi = sm;
+    float* xj = sm + kCalTile * dp;
+    float* cs = xj + kCalTile * dp;                      // n_scales
+    float* red = cs + kCalMaxScales;                     // 8 warps x n_scales
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < n_scales; j += blockDim.x) cs[j] = c2[j];
+    double acc = 0.0;  // thread j < n_scales owns scale j
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        int64_t ti, tj;
+        tri_tile(t, ti, tj);
+        __syncthreads();
+        load_rows(X, N, d, ti * kCalTile, xi);
+        load_rows(X, N, d, tj * kCalTile, xj);
+        __syncthreads();
+        float D[8][8];
+        tile_dist(xi, xj, d, ty, tx, D);
+        const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const int64_t gi = gi0 + 16 * a, gj = gj0 + 16 * b;
+                if (!(gi < N && gi > gj)) D[a][b] = __int_as_float(0x7f800000);  // +inf
+            }
+        for (int j = 0; j < n_scales; ++j) {
+            const float c = -cs[j];
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) s += ex2_approx(D[a][b] * c);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) red[warp * kCalMaxScales + j] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < n_scales) {
+            double w = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) w += (double)red[q * kCalMaxScales + threadIdx.x];
+            acc += w;
+        }
+    }
+    if (threadIdx.x < n_scales) partial[(int64_t)blockIdx.x * n_scales + threadIdx.x] = acc;
+}
+
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int n_parts,
+                                       int n_scales, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_scales) return;
+    double s = 0.0;
+    for (int p = 0; p < n_parts; ++p) s += partial[(int64_t)p * n_scales + j];
+    out[j] = s;
+}
+
+static size_t calib_smem(int d) {
+    return (2 * kCalTile * (size_t)(d + 1) + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
+}
+
+int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
+                  int n_scales, double* sums, cudaStream_t s) {
+    if (!X || !scales || !sums || N < 1 || d < 1 || d > kCalMaxD || n_scales < 1 ||
+        n_scales > kCalMaxScales)
+        return set_error(ctx, KEVD_ERR_ARG,
+                         "calibrate: need N >= 1, 1 <= d <= %d, 1 <= n_scales <= %d", kCalMaxD,
+                         kCalMaxScales);
+    const int64_t nt = (N + kCalTile - 1) / kCalTile;
+    const int64_t n_tiles = nt * (nt + 1) / 2;
+    const int grid = (int)std::min<int64_t>(n_tiles, (int64_t)ctx->num_sms * 2);
+    int st = KEVD_OK;
+    float* c2 = arena_get<float>(ctx, "cal.c2", kCalMaxScales, &st);
+    double* partial = arena_get<double>(ctx, "cal.partial", (size_t)grid * n_scales, &st);
+    double* out = arena_get<double>(ctx, "cal.out", kCalMaxScales, &st);
+    if (st != KEVD_OK) return st;
+    std::vector<float> hc(n_scales);
+    for (int j = 0; j < n_scales; ++j) {
+        if (!(scales[j] > 0.0))
+            return set_error(ctx, KEVD_ERR_ARG, "calibrate: scales must be positive");
+        hc[j] = (float)(scales[j] * 1.4426950408889634);  // exp(-x s) = exp2(-x s log2 e)
+    }
+    KEVD_CUDA(ctx, cudaMemcpyAsync(c2, hc.data(), n_scales * sizeof(float),
+                                   cudaMemcpyHostToDevice, s));
+    const size_t smem = calib_smem(d);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_tiles_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, c2, n_scales, n_tiles, partial);
+    KEVD_LAUNCH(ctx);
+    reduce_partials_kernel<<<1, kCalMaxScales, 0, s>>>(partial, grid, n_scales, out);
+    KEVD_LAUNCH(ctx);
+    KEVD_CUDA(ctx, cudaMemcpyAsync(sums, out, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    return KEVD_OK;
+}
+
+// ---- pair-distance median by radix selection over FP32 bit patterns -------
+//
+// Non-negative floats order like their uint32 bit patterns.  Three passes
+// histogram bits [31:20], [19:8], [7:0] of the distances whose higher bits
+// match the prefix found so far; the host walks each histogram to the bin
+// holding the wanted rank.  Distances are recomputed in every pass (cheap
+// next to the 4096-bin shared-memory histogram).
+
+constexpr int kHistBins = 4096;
+
+__device__ __forceinline__ void hist_add(unsigned* h, float D, int shift, unsigned mask,
+                                         unsigned prefix, int hi_shift) {
+    const unsigned u = __float_as_uint(D);
+    const bool match = (hi_shift >= 32) ? true : ((u >> hi_shift) == prefix);
+    if (match) atomicAdd(&h[(u >> shift) & mask], 1u);
+}
+
+__global__ void __launch_bounds__(256, 2)
+median_tiles_kernel(const float* __restrict__ X, int64_t N, int d, int64_t n_tiles, int shift,
+                    unsigned mask, unsigned prefix, int hi_shift, unsigned* __restrict__ hist) {
+    extern __shared__ float sm[];
+    const int dp = d + 1;
+    float* xi = sm;
+    float* xj = sm + kCalTile * dp;
+    unsigned* h = reinterpret_cast<unsigned*>(xj + kCalTile * dp);
+    for (int e = threadIdx.x; e < kHistBins; e += blockDim.x) h[e] = 0u;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        int64_t ti, tj;
+        tri_tile(t, ti, tj);
+        __syncthreads();
+        load_rows(X, N, d, ti * kCalTile, xi);
+        load_rows(X, N, d, tj * kCalTile, xj);
+        __syncthreads();
+        float D[8][8];
+        tile_dist(xi, xj, d, ty, tx, D);
+        const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const int64_t gi = gi0 + 16 * a, gj = gj0 + 16 * b;
+                if (gi < N && gi > gj) hist_add(h, D[a][b], shift, mask, prefix, hi_shift);
+            }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kHistBins; e += blockDim.x)
+        if (h[e]) atomicAdd(&hist[e], h[e]);
+}
+
+__global__ void median_pairs_kernel(const float* __restrict__ X, int d,
+                                    const int64_t* __restrict__ pi, const int64_t* __restrict__ pl,
+                                    int64_t n_pairs, int shift, unsigned mask, unsigned prefix,
+                                    int hi_shift, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[kHistBins];
+    for (int e = threadIdx.x; e < kHistBins; e += blockDim.x) h[e] = 0u;
+    __syncthreads();
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_pairs;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const float* a = X + pi[p] * d;
+        const float* b = X + pl[p] * d;
+        float D = 0.f;
+        for (int k = 0; k < d; ++k) {
+            const float t = a[k] - b[k];
+            D = fmaf(t, t, D);
+        }
+        hist_add(h, D, shift, mask, prefix, hi_shift);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kHistBins; e += blockDim.x)
+        if (h[e]) atomicAdd(&hist[e], h[e]);
+}
+
+int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64_t* pi,
+                    const int64_t* pl, int64_t n_pairs, double* median, cudaStream_t s) {
+    if (!X || !median || N < 2 || d < 1 || d > kCalMaxD || n_pairs < 0 ||
+        (n_pairs > 0 && (!pi || !pl)))
+        return set_error(ctx, KEVD_ERR_ARG, "pair_median: bad arguments");
+    const bool exact = (n_pairs == 0);
+    const int64_t nt = (N + kCalTile - 1) / kCalTile;
+    const int64_t n_tiles = nt * (nt + 1) / 2;
+    const uint64_t total = exact ? (uint64_t)N * (uint64_t)(N - 1) / 2 : (uint64_t)n_pairs;
+    uint64_t rank = (total - 1) / 2;  // lower median
+    int st = KEVD_OK;
+    unsigned* hist = arena_get<unsigned>(ctx, "med.hist", kHistBins, &st);
+    if (st != KEVD_OK) return st;
+    const size_t smem = 2 * kCalTile * (size_t)(d + 1) * sizeof(float) + kHistBins * sizeof(unsigned);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(median_tiles_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int shifts[3] = {20, 8, 0};
+    const unsigned masks[3] = {0xfffu, 0xfffu, 0xffu};
+    unsigned prefix = 0;
+    int hi_shift = 32;
+    std::vector<unsigned> hh(kHistBins);
+    for (int pass = 0; pass < 3; ++pass) {
+        KEVD_CUDA(ctx, cudaMemsetAsync(hist, 0, kHistBins * sizeof(unsigned), s));
+        if (exact) {
+            const int grid = (int)std::min<int64_t>(n_tiles, (int64_t)ctx->num_sms * 2);
+            median_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, n_tiles, shifts[pass],
+                                                        masks[pass], prefix, hi_shift, hist);
+        } else {
+            const int grid = (int)std::min<int64_t>((n_pairs + 255) / 256, (int64_t)ctx->num_sms * 4);
+            median_pairs_kernel<<<grid, 256, 0, s>>>(X, d, pi, pl, n_pairs, shifts[pass],
+                                                     masks[pass], prefix, hi_shift, hist);
+        }
+        KEVD_LAUNCH(ctx);
+        KEVD_CUDA(ctx, cudaMemcpyAsync(hh.data(), hist, kHistBins * sizeof(unsigned),
+                                       cudaMemcpyDeviceToHost, s));
+        KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+        uint64_t cum = 0;
+        int bin = -1;
+        for (int b = 0; b <= (int)masks[pass]; ++b) {
+            if (cum + hh[b] > rank) {
+                bin = b;
+                break;
+            }
+            cum += hh[b];
+        }
+        if (bin < 0) return set_error(ctx, KEVD_ERR_CUDA, "pair_median: histogram lost counts");
+        rank -= cum;
+        prefix = (hi_shift >= 32 ? 0u : (prefix << (hi_shift - shifts[pass]))) | (unsigned)bin;
+        hi_shift = shifts[pass];
+    }
+    float m;
+    unsigned bits = prefix;
+    std::memcpy(&m, &bits, sizeof(float));
+    *median = (double)m;
+    return KEVD_OK;
+}
+
+}  // namespace kevd

@@ -1,0 +1,432 @@
+// Stage 3: bistochastic normalisation + EVD of a stored factor F (N x k).
+//
+// Closed form of ks_kevd.cu (README_kevd.md:20-69) with Khat = F F^T:
+//
+//   c1   = F^T 1                 colsum pass
+//   dtil = F c1                  rowdot pass (+ positivity check, abort code 2)
+//   cq   = F^T dtil^{-1}         colsum pass
+//   qtil = F cq                  rowdot pass (+ positivity check, abort code 4)
+//   A    = F^T Dtil^{-2} F       weighted Gram
+//   B    = F^T Qtil^{-1} F       weighted Gram
+//   s    = DBL_EPSILON tr(A);  A + sI = L L^T (R = L^T)      (abort code 3)
+//   W    = R B R^T; (lam, V) = syevd(W), ascending           (abort code 5)
+//   Z    = R^{-1} V[:, k-k_out:];  U = Dtil^{-1} F Z (float, row-major)
+//
+// The streaming passes and Grams are this file's kernels; the k x k FP64
+// factorisation, products and eigensolve use cuSOLVER / cuBLAS (the reference
+// uses cuSOLVERMp / cuBLASMp for the same dense steps).  Cross-row sums are
+// FP64; FP32 factors accumulate FP32 partials over 1024-row chunks that are
+// then added in FP64.
+#include "kevd_internal.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <vector>
+
+namespace kevd {
+
+// ---- column sums c = F^T w (w == nullptr: ones) ----------------------------
+template <typename T>
+__global__ void __launch_bounds__(256)
+ev_colsum_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k,
+                 const double* __restrict__ w, int64_t rows_per, double* __restrict__ partial) {
+    const int64_t c = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
+    if (c >= k) return;
+    double acc = 0.0;
+    for (int64_t i = r0; i < r1; ++i) {
+        const double f = (double)F[i * ldF + c];
+        acc += w ? f * w[i] : f;
+    }
+    partial[(int64_t)blockIdx.y * k + c] = acc;
+}
+
+__global__ void ev_sum_partials_kernel(const double* __restrict__ partial, int n_parts, int64_t k,
+                                       double* __restrict__ out) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    double s = 0.0;
+    for (int p = 0; p < n_parts; ++p) s += partial[(int64_t)p * k + c];
+    out[c] = s;
+}
+
+// ---- row dots y = F v, with y > 0 check and 1/y ----------------------------
+template <typename T>
+__global__ void __launch_bounds__(256)
+ev_rowdot_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k,
+                 const double* __restrict__ v, double* __restrict__ y, double* __restrict__ yinv,
+                 int* __restrict__ bad) {
+    extern __shared__ double vs[];
+    for (int64_t c = threadIdx.x; c < k; c += blockDim.x) vs[c] = v[c];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < N; i += warps) {
+        const T* row = F + i * ldF;
+        double acc = 0.0;
+        for (int64_t c = lane; c < k; c += 32) acc += (double)row[c] * vs[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            y[i] = acc;
+            yinv[i] = 1.0 / acc;
+            if (!(acc > 0.0)) atomicOr(bad, 1);
+        }
+    }
+}
+
+// ---- weighted Gram  G = sum_i w_i F_i^T F_i, lower 64 x 64 tiles -----------
+// grid.x = lower tile index, grid.y = row split.  Thread (ty, tx) of 16 x 16
+// owns rows ty + 16a and columns tx + 16b of the tile.
+constexpr int kGT = 64;   // tile edge
+constexpr int kGK = 32;   // rows per stage
+constexpr int kGFlush = 1024;  // rows per FP32 partial (FP32 factors)
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+ev_gram_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k,
+               const double* __restrict__ w, int64_t rows_per, double* __restrict__ partial) {
+    __shared__ T As[kGK][kGT + 1];
+    __shared__ T Bs[kGK][kGT + 1];
+    // lower tile (ta >= tb) from the linear index
+    const int64_t t = blockIdx.x;
+    int64_t ta = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (ta * (ta + 1) / 2 > t) --ta;
+    while ((ta + 1) * (ta + 2) / 2 <= t) ++ta;
+    const int64_t tb = t - ta * (ta + 1) / 2;
+    const int64_t a0 = ta * kGT, b0 = tb * kGT;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
+    double acc64[4][4];
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { acc64[i][j] = 0.0; acc[i][j] = 0; }
+    int64_t since_flush = 0;
+    for (int64_t i0 = r0; i0 < r1; i0 += kGK) {
+        for (int e = threadIdx.x; e < kGK * kGT; e += 256) {
+            const int rr = e / kGT, cc = e - rr * kGT;
+            const int64_t i = i0 + rr;
+            T fa = 0, fb = 0;
+            if (i < r1) {
+                const T wi = (T)w[i];
+                if (a0 + cc < k) fa = F[i * ldF + a0 + cc] * wi;
+                if (b0 + cc < k) fb = F[i * ldF + b0 + cc];
+            }
+            As[rr][cc] = fa;
+            Bs[rr][cc] = fb;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int rr = 0; rr < kGK; ++rr) {
+            T va[4], vb[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) va[a] = As[rr][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) vb[b] = Bs[rr][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += va[a] * vb[b];
+        }
+        __syncthreads();
+        since_flush += kGK;
+        if (sizeof(T) == 4 && since_flush >= kGFlush) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) { acc64[a][b] += (double)acc[a][b]; acc[a][b] = 0; }
+            since_flush = 0;
+        }
+    }
+    double* out = partial + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * kGT * kGT;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            out[(ty + 16 * a) * kGT + tx + 16 * b] = acc64[a][b] + (double)acc[a][b];
+}
+
+// Sum the row-split partials of every lower tile into a full symmetric
+// column-major k x k matrix.
+__global__ void ev_gram_reduce_kernel(const double* __restrict__ partial, int n_tiles, int n_split,
+                                      int64_t k, double* __restrict__ G) {
+    const int64_t t = blockIdx.x;
+    int64_t ta = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (ta * (ta + 1) / 2 > t) --ta;
+    while ((ta + 1) * (ta + 2) / 2 <= t) ++ta;
+    const int64_t tb = t - ta * (ta + 1) / 2;
+    for (int e = threadIdx.x; e < kGT * kGT; e += blockDim.x) {
+        const int ia = e / kGT, ib = e - ia * kGT;
+        const int64_t ga = ta * kGT + ia, gb = tb * kGT + ib;
+        if (ga >= k || gb >= k) continue;
+        double s = 0.0;
+        for (int p = 0; p < n_split; ++p) s += partial[((int64_t)p * n_tiles + t) * kGT * kGT + e];
+        G[gb * k + ga] = s;   // (ga, gb)
+        G[ga * k + gb] = s;   // (gb, ga)
+    }
+}
+
+// ---- small helpers ---------------------------------------------------------
+__global__ void ev_square_kernel(const double* __restrict__ x, double* __restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = x[i] * x[i];
+}
+
+__global__ void ev_trace_shift_kernel(double* __restrict__ A, int64_t k, double* __restrict__ out) {
+    // one CTA: out[0] = tr(A), out[1] = shift; A += shift I
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < k; i += blockDim.x) s += A[i * k + i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double tr = red[0];
+    const double sh = DBL_EPSILON * tr;
+    for (int64_t i = threadIdx.x; i < k; i += blockDim.x) A[i * k + i] += sh;
+    if (threadIdx.x == 0) {
+        out[0] = tr;
+        out[1] = sh;
+    }
+}
+
+__global__ void ev_symmetrize_kernel(double* __restrict__ W, int64_t k) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k * k;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e / k, r = e - c * k;
+        if (r > c) {
+            const double v = 0.5 * (W[c * k + r] + W[r * k + c]);
+            W[c * k + r] = v;
+            W[r * k + c] = v;
+        }
+    }
+}
+
+// ---- U = Dtil^{-1} F Z (row-major float, N x k_out) -------------------------
+// CTA: 64 rows x k_out (<= 64) columns; Z chunks of 32 rows staged as T.
+template <typename T>
+__global__ void __launch_bounds__(256)
+ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ Z,
+            int k_out, const double* __restrict__ dinv, float* __restrict__ U) {
+    __shared__ T Fs[64][33];
+    __shared__ T Zs[32][65];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t row0 = (int64_t)blockIdx.x * 64;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0;
+    for (int64_t c0 = 0; c0 < k; c0 += 32) {
+        for (int e = threadIdx.x; e < 64 * 32; e += 256) {
+            const int rr = e / 32, cc = e - rr * 32;
+            const int64_t i = row0 + rr, c = c0 + cc;
+            Fs[rr][cc] = (i < N && c < k) ? F[i * ldF + c] : (T)0;
+        }
+        for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+            const int cc = e / 64, j = e - cc * 64;
+            const int64_t c = c0 + cc;
+            Zs[cc][j] = (c < k && j < k_out) ? (T)Z[(int64_t)j * k + c] : (T)0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int cc = 0; cc < 32; ++cc) {
+            T vf[4], vz[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) vf[a] = Fs[ty + 16 * a][cc];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) vz[b] = Zs[cc][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] += vf[a] * vz[b];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int64_t i = row0 + ty + 16 * a;
+        if (i >= N) continue;
+        const double di = dinv[i];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int j = tx + 16 * b;
+            if (j < k_out) U[i * k_out + j] = (float)((double)acc[a][b] * di);
+        }
+    }
+}
+
+template <typename T>
+static int colsum(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, const double* w,
+                  double* out, cudaStream_t s) {
+    const int ny = (int)std::min<int64_t>((N + 1023) / 1024, (int64_t)ctx->num_sms * 4);
+    const int64_t rows_per = (N + ny - 1) / ny;
+    int st = KEVD_OK;
+    double* partial = arena_get<double>(ctx, "ev.cpart", (size_t)ny * k, &st);
+    if (st != KEVD_OK) return st;
+    ev_colsum_kernel<T><<<dim3(ceil_div(k, 256), ny), 256, 0, s>>>(F, ldF, N, k, w, rows_per, partial);
+    KEVD_LAUNCH(ctx);
+    ev_sum_partials_kernel<<<ceil_div(k, 256), 256, 0, s>>>(partial, ny, k, out);
+    KEVD_LAUNCH(ctx);
+    return KEVD_OK;
+}
+
+template <typename T>
+static int rowdot(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, const double* v,
+                  double* y, double* yinv, int* bad, cudaStream_t s) {
+    const size_t smem = (size_t)k * sizeof(double);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(ev_rowdot_kernel<T>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = (int)std::min<int64_t>((N + 7) / 8, (int64_t)ctx->num_sms * 8);
+    ev_rowdot_kernel<T><<<grid, 256, smem, s>>>(F, ldF, N, k, v, y, yinv, bad);
+    KEVD_LAUNCH(ctx);
+    return KEVD_OK;
+}
+
+template <typename T>
+static int gram(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, const double* w,
+                double* G, cudaStream_t s) {
+    const int nt = ceil_div(k, kGT);
+    const int n_tiles = nt * (nt + 1) / 2;
+    int n_split = (int)std::max<int64_t>(1, ((int64_t)ctx->num_sms * 8 + n_tiles - 1) / n_tiles);
+    n_split = (int)std::min<int64_t>(n_split, std::max<int64_t>(1, N / 256));
+    const int64_t rows_per = ((N + n_split - 1) / n_split + kGK - 1) / kGK * kGK;
+    int st = KEVD_OK;
+    double* partial = arena_get<double>(ctx, "ev.gpart", (size_t)n_split * n_tiles * kGT * kGT, &st);
+    if (st != KEVD_OK) return st;
+    ev_gram_kernel<T><<<dim3(n_tiles, n_split), 256, 0, s>>>(F, ldF, N, k, w, rows_per, partial);
+    KEVD_LAUNCH(ctx);
+    ev_gram_reduce_kernel<<<n_tiles, 256, 0, s>>>(partial, n_tiles, n_split, k, G);
+    KEVD_LAUNCH(ctx);
+    return KEVD_OK;
+}
+
+static int d2h(kevd_ctx* ctx, double* host, const double* dev, size_t n, cudaStream_t s) {
+    if (!host) return KEVD_OK;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    return KEVD_OK;
+}
+
+template <typename T>
+static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF, int k_out,
+                    double* lam_h, float* U, kevd_evd_info* info, kevd_evd_dump* dump,
+                    cudaStream_t s) {
+    int st = KEVD_OK;
+    double* c1 = arena_get<double>(ctx, "ev.c1", k, &st);
+    double* cq = arena_get<double>(ctx, "ev.cq", k, &st);
+    double* dtil = arena_get<double>(ctx, "ev.dtil", N, &st);
+    double* dinv = arena_get<double>(ctx, "ev.dinv", N, &st);
+    double* qtil = arena_get<double>(ctx, "ev.qtil", N, &st);
+    double* qinv = arena_get<double>(ctx, "ev.qinv", N, &st);
+    double* w2 = arena_get<double>(ctx, "ev.w2", N, &st);
+    double* A = arena_get<double>(ctx, "ev.A", (size_t)k * k, &st);
+    double* B = arena_get<double>(ctx, "ev.B", (size_t)k * k, &st);
+    double* W = arena_get<double>(ctx, "ev.W", (size_t)k * k, &st);
+    double* lam = arena_get<double>(ctx, "ev.lam", k, &st);
+    double* Z = arena_get<double>(ctx, "ev.Z", (size_t)k * k_out, &st);
+    double* trsh = arena_get<double>(ctx, "ev.trsh", 2, &st);
+    int* flags = arena_get<int>(ctx, "ev.flags", 4, &st);
+    if (st != KEVD_OK) return st;
+    int* hflags = static_cast<int*>(ctx->pinned);
+    KEVD_CUDA(ctx, cudaMemsetAsync(flags, 0, 4 * sizeof(int), s));
+
+    // pass 1: c1 = F^T 1;  pass 2: dtil = F c1, cq = F^T dtil^{-1}
+    KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, nullptr, c1, s));
+    KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, c1, dtil, dinv, flags + 0, s));
+    KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, dinv, cq, s));
+    // pass 3: qtil = F cq
+    KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, cq, qtil, qinv, flags + 1, s));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hflags[0]) return set_error(ctx, KEVD_ERR_NONPOS_DTIL, "bistochastic_evd: nonpositive dtil");
+    if (hflags[1]) return set_error(ctx, KEVD_ERR_NONPOS_QTIL, "bistochastic_evd: nonpositive qtil");
+
+    // Grams
+    ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
+    KEVD_LAUNCH(ctx);
+    KEVD_TRY(gram<T>(ctx, F, ldF, N, k, w2, A, s));
+    KEVD_TRY(gram<T>(ctx, F, ldF, N, k, qinv, B, s));
+    if (dump) {
+        KEVD_TRY(d2h(ctx, dump->c1, c1, k, s));
+        KEVD_TRY(d2h(ctx, dump->dtil, dtil, N, s));
+        KEVD_TRY(d2h(ctx, dump->cq, cq, k, s));
+        KEVD_TRY(d2h(ctx, dump->qtil, qtil, N, s));
+        KEVD_TRY(d2h(ctx, dump->A, A, (size_t)k * k, s));
+        KEVD_TRY(d2h(ctx, dump->B, B, (size_t)k * k, s));
+    }
+
+    // dense 1: shift, Cholesky A + sI = L L^T
+    ev_trace_shift_kernel<<<1, 1024, 0, s>>>(A, k, trsh);
+    KEVD_LAUNCH(ctx);
+    KEVD_SOLVER(ctx, cusolverDnSetStream(ctx->solver, s));
+    KEVD_BLAS(ctx, cublasSetStream(ctx->blas, s));
+    int lwork = 0, lwork2 = 0;
+    KEVD_SOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A,
+                                                 (int)k, &lwork));
+    KEVD_SOLVER(ctx, cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                                 CUBLAS_FILL_MODE_LOWER, (int)k, W, (int)k, lam,
+                                                 &lwork2));
+    double* work = arena_get<double>(ctx, "ev.work", (size_t)std::max(lwork, lwork2) + 1, &st);
+    if (st != KEVD_OK) return st;
+    KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A, (int)k, work,
+                                      lwork, flags + 2));
+    // dense 2: W = L^T B L
+    const double one = 1.0;
+    KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                               CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, B, (int)k, W,
+                               (int)k));
+    KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                               CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, W, (int)k, W,
+                               (int)k));
+    ev_symmetrize_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(W, k);
+    KEVD_LAUNCH(ctx);
+    if (dump) KEVD_TRY(d2h(ctx, dump->W, W, (size_t)k * k, s));
+    KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                      (int)k, W, (int)k, lam, work, lwork2, flags + 3));
+    // Z = L^{-T} V[:, k-k_out:]
+    KEVD_CUDA(ctx, cudaMemcpyAsync(Z, W + (k - k_out) * k, (size_t)k * k_out * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+    KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                               CUBLAS_DIAG_NON_UNIT, (int)k, k_out, &one, A, (int)k, Z, (int)k));
+    // pass 4: U = Dtil^{-1} F Z
+    ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
+    KEVD_LAUNCH(ctx);
+    if (dump) KEVD_TRY(d2h(ctx, dump->Z, Z, (size_t)k * k_out, s));
+    double htr[2];
+    KEVD_CUDA(ctx, cudaMemcpyAsync(htr, trsh, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(hflags, flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (lam_h) KEVD_CUDA(ctx, cudaMemcpyAsync(lam_h, lam, k * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (info) {
+        info->trace_A = htr[0];
+        info->shift = htr[1];
+    }
+    if (hflags[2] != 0)
+        return set_error(ctx, KEVD_ERR_POTRF, "bistochastic_evd: potrf failed, info %d", hflags[2]);
+    if (hflags[3] != 0)
+        return set_error(ctx, KEVD_ERR_SYEVD, "bistochastic_evd: syevd failed, info %d", hflags[3]);
+    return KEVD_OK;
+}
+
+int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k,
+                         int64_t ldF, int k_out, double* lam, float* U, kevd_evd_info* info,
+                         kevd_evd_dump* dump, cudaStream_t s) {
+    if (!F || !U || N < 1 || k < 1 || ldF < k || k_out < 1 || k_out > 64 || k_out > k || k > 8192)
+        return set_error(ctx, KEVD_ERR_ARG,
+                         "bistochastic_evd: need F, U, N >= 1, 1 <= k <= 8192, ldF >= k, "
+                         "1 <= k_out <= min(k, 64)");
+    if (precision == KEVD_FP64)
+        return evd_impl<double>(ctx, (const double*)F, N, k, ldF, k_out, lam, U, info, dump, s);
+    if (precision == KEVD_MIXED)
+        return evd_impl<float>(ctx, (const float*)F, N, k, ldF, k_out, lam, U, info, dump, s);
+    return set_error(ctx, KEVD_ERR_ARG, "bistochastic_evd: unknown precision %d", precision);
+}
+
+}  // namespace kevd

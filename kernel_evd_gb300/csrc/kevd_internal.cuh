@@ -1,0 +1,125 @@
+// Internal declarations shared by the kevd CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+
+#include "../../include/kevd.h"
+
+namespace kevd {
+
+constexpr int kNumSMs = 152;
+
+// Status with a message stored in the context.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+// One named, growable device buffer per purpose.  Buffers are reused across
+// calls and only grow; they are released with the context.
+class Arena {
+  public:
+    ~Arena() { release(); }
+    void* get(const std::string& name, size_t bytes, int* status);
+    void release();
+
+  private:
+    struct Buf {
+        void* p = nullptr;
+        size_t n = 0;
+    };
+    std::map<std::string, Buf> bufs_;
+};
+
+}  // namespace kevd
+
+struct kevd_ctx {
+    int device = 0;
+    int num_sms = kevd::kNumSMs;
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+    kevd::Arena arena;
+    void* pinned = nullptr;  // small pinned host staging area
+    size_t pinned_bytes = 0;
+    std::string last_error;
+};
+
+namespace kevd {
+
+int set_error(kevd_ctx* ctx, int code, const char* fmt, ...);
+
+#define KEVD_CUDA(ctx, call)                                                          \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return ::kevd::set_error((ctx), KEVD_ERR_CUDA, "%s:%d %s: %s", __FILE__,  \
+                                     __LINE__, #call, cudaGetErrorString(e_));        \
+    } while (0)
+
+#define KEVD_LAUNCH(ctx)                                                              \
+    do {                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                          \
+        if (e_ != cudaSuccess)                                                        \
+            return ::kevd::set_error((ctx), KEVD_ERR_CUDA, "%s:%d launch: %s",        \
+                                     __FILE__, __LINE__, cudaGetErrorString(e_));     \
+    } while (0)
+
+#define KEVD_BLAS(ctx, call)                                                          \
+    do {                                                                              \
+        cublasStatus_t s_ = (call);                                                   \
+        if (s_ != CUBLAS_STATUS_SUCCESS)                                              \
+            return ::kevd::set_error((ctx), KEVD_ERR_CUDA, "%s:%d %s: cublas status %d", \
+                                     __FILE__, __LINE__, #call, (int)s_);             \
+    } while (0)
+
+#define KEVD_SOLVER(ctx, call)                                                        \
+    do {                                                                              \
+        cusolverStatus_t s_ = (call);                                                 \
+        if (s_ != CUSOLVER_STATUS_SUCCESS)                                            \
+            return ::kevd::set_error((ctx), KEVD_ERR_CUDA, "%s:%d %s: cusolver status %d", \
+                                     __FILE__, __LINE__, #call, (int)s_);             \
+    } while (0)
+
+#define KEVD_TRY(expr)                 \
+    do {                               \
+        int st_ = (expr);              \
+        if (st_ != KEVD_OK) return st_; \
+    } while (0)
+
+template <typename T>
+T* arena_get(kevd_ctx* ctx, const char* name, size_t count, int* st) {
+    return static_cast<T*>(ctx->arena.get(name, count * sizeof(T), st));
+}
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// ---- stage entry points implemented in the .cu files (C++ linkage) --------
+int launch_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M, int64_t Nq,
+                       float* X, cudaStream_t s);
+int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
+                        const int64_t* rows, int64_t row0, int64_t nrows, const int64_t* cols,
+                        int64_t ncols, int precision, void* out, int64_t ld, cudaStream_t s,
+                        const float* Xc = nullptr);
+int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
+                  int n_scales, double* sums, cudaStream_t s);
+int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64_t* pi,
+                    const int64_t* pl, int64_t n_pairs, double* median, cudaStream_t s);
+int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
+               const kevd_rpchol_params* p, void* F, int64_t ldF, int64_t* piv, double* err,
+               int32_t* accepted, kevd_rpchol_result* res, cudaStream_t s);
+int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k,
+                         int64_t ldF, int k_out, double* lam, float* U, kevd_evd_info* info,
+                         kevd_evd_dump* dump, cudaStream_t s);
+int run_gather_rows(kevd_ctx* ctx, const void* F, int precision, int64_t ldF, const int64_t* idx,
+                    int64_t n, int64_t ncols, double* out, cudaStream_t s);
+
+}  // namespace kevd

@@ -1,0 +1,617 @@
+// Stage 2: block randomly pivoted Cholesky with a stored factor.
+//
+// Semantics follow ks_arpclm.cu's round (propose, residual block, accept /
+// reject + factor, residual-diagonal update, trace error), with the factor F
+// kept in HBM instead of regenerating K(R, S) every round:
+//
+//   round:  sample   b proposals ~ d                    (1 CTA)
+//           hgram    F(S',:) F(S',:)^T split over column chunks, and K(S',S')
+//           factor   H = K(S',S') - F F^T, accept/reject, Cholesky, L_i^{-1}
+//           update   G = (K(R,S_i) - F(R,:) F(S_i,:)^T) L_i^{-T} for every row
+//                    block R; F(R, r:r+nacc) = G; d(R) -= rowsq(G), clamped;
+//                    per-block sums of d for the next sampler
+//
+// All round state stays on the device: kernels read the rank and accepted
+// count from a RoundState, and after the stop condition every kernel returns
+// immediately, so the host enqueues rounds without a per-round sync (the
+// reference synchronises and copies nacc to the host every round,
+// ks_arpclm.cu:877-886).
+//
+// T = double is the plain FP64 form; T = float the mixed form (F, the F F^T
+// products and G in FP32; H, its Cholesky and inverse, the residual diagonal
+// and all sums in FP64).
+#include "kevd_internal.cuh"
+#include "kevd_rng.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace kevd {
+
+constexpr int kRowBlock = 128;   // rows per update CTA (= rows per d partial sum)
+constexpr int kMaxBlock = 64;    // proposals per round supported by the SIMT update
+constexpr int kColChunk = 32;    // F columns per hgram CTA
+constexpr int kSampleThreads = 1024;
+
+struct RoundState {
+    int64_t rank;    // columns of F written
+    int64_t r_old;   // rank before this round's update
+    int32_t nacc;    // accepted this round
+    int32_t done;    // set once the factorisation has stopped
+    int32_t rounds;  // rounds executed
+    int32_t pad;
+    double total;    // sum of d after the last update
+};
+
+__global__ void rp_init_kernel(double* __restrict__ d, double* __restrict__ dblk, int64_t N,
+                               int64_t nblk, RoundState* st) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = 1.0;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblk;
+         b += (int64_t)gridDim.x * blockDim.x)
+        dblk[b] = (double)min((int64_t)kRowBlock, N - b * kRowBlock);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->rank = 0;
+        st->r_old = 0;
+        st->nacc = 0;
+        st->done = 0;
+        st->rounds = 0;
+        st->total = (double)N;
+    }
+}
+
+// ---- sampler ---------------------------------------------------------------
+// Inverse-CDF proposals (ks_arpclm.cu:197-224): pivot = smallest i with
+// cumsum(d)[i] >= u * sum(d), else N - 1.  The prefix is hierarchical: a scan
+// over per-thread chunks of the block sums, a sequential walk over the chunk,
+// then a warp scan inside the 128-row block.  Also records the trace error of
+// the previous round and decides the stop.
+__global__ void __launch_bounds__(kSampleThreads)
+rp_sample_kernel(const double* __restrict__ d, const double* __restrict__ dblk, int64_t N,
+                 int64_t nblk, int round, int b, uint64_t seed,
+                 const double* __restrict__ uniforms, int64_t* __restrict__ props,
+                 RoundState* st, int64_t k_max, int max_rounds, double err_target,
+                 double* __restrict__ err) {
+    __shared__ double incl[kSampleThreads];
+    __shared__ int s_stop;
+    if (st->done) return;
+    const int tid = threadIdx.x;
+    const int64_t chunk = (nblk + kSampleThreads - 1) / kSampleThreads;
+    const int64_t c0 = min(nblk, (int64_t)tid * chunk), c1 = min(nblk, c0 + chunk);
+    double s = 0.0;
+    for (int64_t q = c0; q < c1; ++q) s += dblk[q];
+    incl[tid] = s;
+    __syncthreads();
+    for (int off = 1; off < kSampleThreads; off <<= 1) {
+        const double v = (tid >= off) ? incl[tid - off] : 0.0;
+        __syncthreads();
+        incl[tid] += v;
+        __syncthreads();
+    }
+    const double total = incl[kSampleThreads - 1];
+    if (tid == 0) {
+        const double e = total / (double)N;
+        if (round > 0) err[round - 1] = e;
+        st->total = total;
+        const bool stop = (round >= max_rounds) || (st->rank >= k_max) ||
+                          (err_target > 0.0 && round > 0 && e <= err_target);
+        if (stop) {
+            st->done = 1;
+            st->rounds = round;
+        }
+        s_stop = stop;
+    }
+    __syncthreads();
+    if (s_stop) return;
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int t = warp; t < b; t += kSampleThreads / 32) {
+        const double u = uniforms ? uniforms[((int64_t)round * 2) * b + t]
+                                  : philox_uniform(seed, (uint32_t)round, 0u, (uint32_t)t);
+        const double target = u * total;
+        int64_t pick = N - 1;
+        if (target <= total) {
+            // smallest chunk owner c with incl[c] >= target
+            int lo = 0, hi = kSampleThreads - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (incl[mid] >= target) hi = mid; else lo = mid + 1;
+            }
+            double base = (lo > 0) ? incl[lo - 1] : 0.0;
+            const int64_t q0 = min(nblk, (int64_t)lo * chunk), q1 = min(nblk, q0 + chunk);
+            int64_t blk = q1 - 1;
+            for (int64_t q = q0; q < q1; ++q) {
+                const double nb = base + dblk[q];
+                if (nb >= target) { blk = q; break; }
+                base = nb;
+            }
+            if (blk >= q0) {
+                // within block: lane l holds rows 4l..4l+3
+                const int64_t r0 = blk * kRowBlock;
+                double v[4], ls = 0.0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int64_t row = r0 + 4 * lane + j;
+                    v[j] = (row < N) ? d[row] : 0.0;
+                    ls += v[j];
+                }
+                double pre = ls;  // inclusive warp scan of lane sums
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const double y = __shfl_up_sync(0xffffffffu, pre, o);
+                    if (lane >= o) pre += y;
+                }
+                double cum = base + pre - ls;
+                int hit = -1;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    cum += v[j];
+                    if (hit < 0 && cum >= target && v[j] > 0.0) hit = j;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit >= 0);
+                if (m) {
+                    const int src = __ffs(m) - 1;
+                    const int hj = __shfl_sync(0xffffffffu, hit, src);
+                    pick = r0 + 4 * src + hj;
+                } else {
+                    // rounding left the target past this block's recomputed
+                    // sum: take its last row with d > 0
+                    const unsigned mz = __ballot_sync(0xffffffffu, ls > 0.0);
+                    if (mz) {
+                        const int src = 31 - __clz(mz);
+                        int jj = 3;
+                        double vv[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) vv[j] = __shfl_sync(0xffffffffu, v[j], src);
+                        while (jj > 0 && !(vv[jj] > 0.0)) --jj;
+                        pick = r0 + 4 * src + jj;
+                    }
+                }
+            }
+        }
+        if (lane == 0) props[t] = min(pick, N - 1);
+    }
+}
+
+// ---- proposal block: F(S',c-chunk) F(S',c-chunk)^T and K(S',S') -----------
+template <typename T>
+__global__ void __launch_bounds__(256)
+rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ X, int d,
+                double scale, const int64_t* __restrict__ props, int b, int n_split,
+                const RoundState* st, double* __restrict__ hpart, double* __restrict__ kss) {
+    if (st->done) return;
+    // one buffer, used either for an F column chunk or for the X rows of S'
+    __shared__ __align__(16) unsigned char raw[kMaxBlock * 129 * sizeof(float)];
+    static_assert(kMaxBlock * (kColChunk + 1) * sizeof(double) <= sizeof(raw), "hgram smem");
+    T* fs = reinterpret_cast<T*>(raw);
+    float* xs = reinterpret_cast<float*>(raw);
+    const int tid = threadIdx.x;
+    if ((int)blockIdx.x < n_split) {
+        const int64_t r = st->rank;
+        const int64_t c0 = (int64_t)blockIdx.x * kColChunk;
+        if (c0 >= r) return;
+        const int nc = (int)min((int64_t)kColChunk, r - c0);
+        for (int e = tid; e < b * kColChunk; e += 256) {
+            const int p = e / kColChunk, c = e - p * kColChunk;
+            fs[p * (kColChunk + 1) + c] = (c < nc) ? F[props[p] * ldF + c0 + c] : (T)0;
+        }
+        __syncthreads();
+        for (int e = tid; e < b * b; e += 256) {
+            const int p = e / b, q = e - p * b;
+            T acc = 0;
+#pragma unroll 8
+            for (int c = 0; c < kColChunk; ++c)
+                acc += fs[p * (kColChunk + 1) + c] * fs[q * (kColChunk + 1) + c];
+            hpart[((int64_t)blockIdx.x * b + p) * b + q] = (double)acc;
+        }
+    } else {
+        // K(S', S') in FP64, rows split over the remaining CTAs
+        const int nk = gridDim.x - n_split;
+        const int part = blockIdx.x - n_split;
+        for (int e = tid; e < b * d; e += 256) {
+            const int p = e / d, k = e - p * d;
+            xs[p * 129 + k] = X[props[p] * d + k];
+        }
+        __syncthreads();
+        for (int e = tid; e < b * b; e += 256) {
+            const int p = e / b, q = e - p * b;
+            if (p % nk != part) continue;
+            double acc = 0.0;
+            for (int k = 0; k < d; ++k) {
+                const double t = (double)xs[p * 129 + k] - (double)xs[q * 129 + k];
+                acc += t * t;
+            }
+            kss[p * b + q] = exp(-scale * acc);
+        }
+    }
+}
+
+// ---- accept / reject, Cholesky, inverse of the compacted factor ------------
+// ks_arpclm.cu:305-408.  H lives in shared memory; accepted columns are
+// overwritten in place by the Cholesky column (only accepted columns are
+// read back).  Minv (b x b, row-major [a][e], zeros above the diagonal).
+__global__ void __launch_bounds__(256)
+rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpart, int b,
+                 int round, uint64_t seed, const double* __restrict__ uniforms, double tol,
+                 int64_t k_max, const int64_t* __restrict__ props, RoundState* st,
+                 double* __restrict__ minv, float* __restrict__ minv_f,
+                 int64_t* __restrict__ sacc, int64_t* __restrict__ piv,
+                 int32_t* __restrict__ hm) {
+    if (st->done) return;
+    extern __shared__ double H[];         // b x b
+    __shared__ double H0[kMaxBlock];
+    __shared__ int accpos[kMaxBlock];
+    __shared__ int s_dec, s_m;
+    const int tid = threadIdx.x;
+    const int64_t r = st->rank;
+    const int nz = (int)((r + kColChunk - 1) / kColChunk);
+    for (int e = tid; e < b * b; e += blockDim.x) {
+        double v = kss[e];
+        for (int z = 0; z < nz; ++z) v -= hpart[(int64_t)z * b * b + e];
+        H[e] = v;
+    }
+    __syncthreads();
+    for (int p = tid; p < b; p += blockDim.x) H0[p] = H[p * b + p];
+    if (tid == 0) s_m = 0;
+    __syncthreads();
+    const int64_t cap = k_max - r;
+    for (int i = 0; i < b; ++i) {
+        __syncthreads();  // everyone has consumed the previous decision
+        if (tid == 0) {
+            const double u = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + i]
+                                      : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)i);
+            const double hii = H[i * b + i];
+            const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol);
+            s_dec = acc;
+            if (acc) accpos[s_m++] = i;
+        }
+        __syncthreads();
+        if (s_dec) {
+            const double f = 1.0 / sqrt(H[i * b + i]);
+            __syncthreads();
+            for (int j = i + tid; j < b; j += blockDim.x) H[j * b + i] *= f;
+            __syncthreads();
+            const int w = b - (i + 1);
+            for (int e = tid; e < w * w; e += blockDim.x) {
+                const int jj = i + 1 + e / w, kk = i + 1 + e % w;
+                if (jj >= kk) H[jj * b + kk] -= H[jj * b + i] * H[kk * b + i];
+            }
+            __syncthreads();
+        }
+    }
+    const int nacc = s_m;
+    // forward substitution, one column per thread
+    for (int e = tid; e < b * b; e += blockDim.x) minv[e] = 0.0;
+    __syncthreads();
+    if (tid < nacc) {
+        const int t = tid;
+        const int at = accpos[t];
+        minv[t * b + t] = 1.0 / H[at * b + at];
+        for (int a = t + 1; a < nacc; ++a) {
+            const int aa = accpos[a];
+            double s = 0.0;
+            for (int e = t; e < a; ++e) s += H[aa * b + accpos[e]] * minv[e * b + t];
+            minv[a * b + t] = -s / H[aa * b + aa];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += blockDim.x) minv_f[e] = (float)minv[e];
+    if (tid < nacc) {
+        const int64_t sp = props[accpos[tid]];
+        sacc[tid] = sp;
+        piv[r + tid] = sp;
+    }
+    if (tid == 0) {
+        st->r_old = r;
+        st->nacc = nacc;
+        st->rank = r + nacc;
+        hm[round] = nacc;
+    }
+}
+
+// ---- residual update over all row blocks -----------------------------------
+// CTA = 128 rows x up to 64 accepted columns; thread (ty, tx) of 16 x 16 owns
+// rows ty + 16i (i < 8) and columns tx + 16j (j < 4).
+template <typename T>
+struct UpdSmem {
+    static constexpr int KC = 32;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, int64_t N, int d,
+                 double scale, const int64_t* __restrict__ sacc, const double* __restrict__ minv,
+                 const float* __restrict__ minv_f, int b, const RoundState* st,
+                 double* __restrict__ dvec, double* __restrict__ dblk) {
+    if (st->done) return;
+    const int nacc = st->nacc;
+    if (nacc == 0) return;
+    const int64_t r = st->r_old;
+    constexpr int KC = UpdSmem<T>::KC;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    // region 1 (phase A: X rows; phase B: F tiles), then Tm, then Minv
+    const int dp = d + 1;
+    const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
+    const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (KC + 1) * sizeof(T);
+    const size_t reg1 = (reg1_a > reg1_b ? reg1_a : reg1_b + 0);
+    float* xr = reinterpret_cast<float*>(smraw);
+    float* xs = xr + kRowBlock * dp;
+    T* At = reinterpret_cast<T*>(smraw);
+    T* Bt = At + kRowBlock * (KC + 1);
+    T* Tm = reinterpret_cast<T*>(smraw + ((reg1 + 15) / 16) * 16);   // 128 x (64+1)
+    T* Mv = Tm + kRowBlock * (kMaxBlock + 1);                         // 64 x (64+1)
+    __shared__ double rowsq_s[kRowBlock];
+
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int64_t row0 = (int64_t)blockIdx.x * kRowBlock;
+    const int nrows = (int)min((int64_t)kRowBlock, N - row0);
+
+    // phase A: K(R, S_i) into Tm
+    for (int e = tid; e < kRowBlock * d; e += 256) {
+        const int rr = e / d, k = e - rr * d;
+        xr[rr * dp + k] = (rr < nrows) ? X[(row0 + rr) * d + k] : 0.f;
+    }
+    for (int e = tid; e < nacc * d; e += 256) {
+        const int q = e / d, k = e - q * d;
+        xs[q * dp + k] = X[sacc[q] * d + k];
+    }
+    for (int e = tid; e < nacc * nacc; e += 256) {
+        const int a = e / nacc, q = e - a * nacc;
+        Mv[a * (kMaxBlock + 1) + q] = sizeof(T) == 8 ? (T)minv[a * b + q] : (T)minv_f[a * b + q];
+    }
+    __syncthreads();
+    {
+        T acc[8][4];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+        for (int k = 0; k < d; ++k) {
+            T vr[8], vs[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) vr[i] = (T)xr[(ty + 16 * i) * dp + k];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) vs[j] = (T)xs[min(tx + 16 * j, kMaxBlock - 1) * dp + k];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const T t = vr[i] - vs[j];
+                    acc[i][j] += t * t;
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = tx + 16 * j;
+                T kv = 0;
+                if (c < nacc) {
+                    if (sizeof(T) == 8) kv = (T)exp(-scale * (double)acc[i][j]);
+                    else kv = (T)expf(-(float)scale * (float)acc[i][j]);
+                }
+                Tm[(ty + 16 * i) * (kMaxBlock + 1) + c] = kv;
+            }
+    }
+    __syncthreads();
+
+    // phase B: acc = F(R, 0:r) F(S_i, 0:r)^T
+    T acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+    for (int64_t c0 = 0; c0 < r; c0 += KC) {
+        const int nc = (int)min((int64_t)KC, r - c0);
+        for (int e = tid; e < kRowBlock * KC; e += 256) {
+            const int rr = e / KC, c = e - rr * KC;
+            At[rr * (KC + 1) + c] = (rr < nrows && c < nc) ? F[(row0 + rr) * ldF + c0 + c] : (T)0;
+        }
+        for (int e = tid; e < kMaxBlock * KC; e += 256) {
+            const int q = e / KC, c = e - q * KC;
+            Bt[q * (KC + 1) + c] = (q < nacc && c < nc) ? F[sacc[q] * ldF + c0 + c] : (T)0;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int c = 0; c < KC; ++c) {
+            T va[8], vb[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) va[i] = At[(ty + 16 * i) * (KC + 1) + c];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) vb[j] = Bt[(tx + 16 * j) * (KC + 1) + c];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] += va[i] * vb[j];
+        }
+        __syncthreads();
+    }
+    // phase C: Tm -= acc (own entries)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) Tm[(ty + 16 * i) * (kMaxBlock + 1) + tx + 16 * j] -= acc[i][j];
+    __syncthreads();
+    // phase D: G = Tm Minv^T
+    T g[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) g[i][j] = 0;
+    for (int e = 0; e < nacc; ++e) {
+        T vt[8], vm[4];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) vt[i] = Tm[(ty + 16 * i) * (kMaxBlock + 1) + e];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int a = tx + 16 * j;
+            vm[j] = (a < nacc) ? Mv[a * (kMaxBlock + 1) + e] : (T)0;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) g[i][j] += vt[i] * vm[j];
+    }
+    // phase E: store the new columns, update d, block sum
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int rr = ty + 16 * i;
+        double sq = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int a = tx + 16 * j;
+            if (a < nacc && rr < nrows) {
+                F[(row0 + rr) * ldF + r + a] = g[i][j];
+                sq += (double)g[i][j] * (double)g[i][j];
+            }
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        if (tx == 0) rowsq_s[rr] = sq;
+    }
+    __syncthreads();
+    double nd = 0.0;
+    if (tid < kRowBlock && tid < nrows) {
+        const int64_t gi = row0 + tid;
+        nd = fmax(dvec[gi] - rowsq_s[tid], 0.0);
+        dvec[gi] = nd;
+    }
+    // block sum of the new d over the first 128 threads (4 warps)
+    __shared__ double wsum[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+    if ((tid & 31) == 0) wsum[tid >> 5] = nd;
+    __syncthreads();
+    if (tid == 0) dblk[blockIdx.x] = ((wsum[0] + wsum[1]) + (wsum[2] + wsum[3]));
+}
+
+template <typename T>
+static size_t update_smem(int d) {
+    const int dp = d + 1;
+    const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
+    const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (UpdSmem<T>::KC + 1) * sizeof(T);
+    const size_t reg1 = ((std::max(reg1_a, reg1_b) + 15) / 16) * 16;
+    return reg1 + (size_t)kRowBlock * (kMaxBlock + 1) * sizeof(T) +
+           (size_t)kMaxBlock * (kMaxBlock + 1) * sizeof(T);
+}
+
+template <typename T>
+static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
+                       const kevd_rpchol_params* p, T* F, int64_t ldF, int64_t* piv_h,
+                       double* err_h, int32_t* hm_h, kevd_rpchol_result* res, cudaStream_t s) {
+    const int b = p->block;
+    const int64_t nblk = (N + kRowBlock - 1) / kRowBlock;
+    const int n_split = (int)((p->k_max + kColChunk - 1) / kColChunk);
+    const int n_kss = 8;
+    int st = KEVD_OK;
+    double* dvec = arena_get<double>(ctx, "rp.d", N, &st);
+    double* dblk = arena_get<double>(ctx, "rp.dblk", nblk, &st);
+    RoundState* rs = arena_get<RoundState>(ctx, "rp.state", 1, &st);
+    int64_t* props = arena_get<int64_t>(ctx, "rp.props", kMaxBlock, &st);
+    int64_t* sacc = arena_get<int64_t>(ctx, "rp.sacc", kMaxBlock, &st);
+    int64_t* piv = arena_get<int64_t>(ctx, "rp.piv", p->k_max, &st);
+    double* hpart = arena_get<double>(ctx, "rp.hpart", (size_t)std::max(n_split, 1) * b * b, &st);
+    double* kss = arena_get<double>(ctx, "rp.kss", (size_t)b * b, &st);
+    double* minv = arena_get<double>(ctx, "rp.minv", (size_t)b * b, &st);
+    float* minv_f = arena_get<float>(ctx, "rp.minvf", (size_t)b * b, &st);
+    double* err = arena_get<double>(ctx, "rp.err", p->max_rounds, &st);
+    int32_t* hm = arena_get<int32_t>(ctx, "rp.hm", p->max_rounds, &st);
+    double* unif = nullptr;
+    if (p->uniforms) unif = arena_get<double>(ctx, "rp.unif", (size_t)p->max_rounds * 2 * b, &st);
+    if (st != KEVD_OK) return st;
+    if (unif)
+        KEVD_CUDA(ctx, cudaMemcpyAsync(unif, p->uniforms, (size_t)p->max_rounds * 2 * b * sizeof(double),
+                                       cudaMemcpyHostToDevice, s));
+    KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, p->max_rounds * sizeof(double), s));
+    KEVD_CUDA(ctx, cudaMemsetAsync(hm, 0, p->max_rounds * sizeof(int32_t), s));
+    rp_init_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dvec, dblk, N, nblk, rs);
+    KEVD_LAUNCH(ctx);
+
+    const size_t fsm = (size_t)b * b * sizeof(double);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(rp_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)std::max(fsm, (size_t)1024)));
+    const size_t usm = update_smem<T>(d);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(rp_update_kernel<T>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usm));
+    int* done_h = static_cast<int*>(ctx->pinned);
+    int round = 0;
+    for (; round < p->max_rounds; ++round) {
+        rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, round, b, p->seed, unif,
+                                                      props, rs, p->k_max, p->max_rounds,
+                                                      p->err_target, err);
+        rp_hgram_kernel<T><<<n_split + n_kss, 256, 0, s>>>(F, ldF, X, d, scale, props, b, n_split,
+                                                         rs, hpart, kss);
+        rp_factor_kernel<<<1, 256, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol, p->k_max,
+                                             props, rs, minv, minv_f, sacc, piv, hm);
+        rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv, minv_f,
+                                                       b, rs, dvec, dblk);
+        KEVD_LAUNCH(ctx);
+        if ((round & 3) == 3) {
+            KEVD_CUDA(ctx, cudaMemcpyAsync(done_h, &rs->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+            KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+            if (*done_h) break;
+        }
+    }
+    // closing sampler call: records the last round's error and the stop
+    rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, std::min(round, p->max_rounds),
+                                                  0, p->seed, unif, props, rs, p->k_max,
+                                                  std::min(round, p->max_rounds), p->err_target, err);
+    KEVD_LAUNCH(ctx);
+    RoundState hs;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(&hs, rs, sizeof(RoundState), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hs.rank > 0 && piv_h)
+        KEVD_CUDA(ctx, cudaMemcpy(piv_h, piv, hs.rank * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (err_h) KEVD_CUDA(ctx, cudaMemcpy(err_h, err, hs.rounds * sizeof(double), cudaMemcpyDeviceToHost));
+    if (hm_h) KEVD_CUDA(ctx, cudaMemcpy(hm_h, hm, hs.rounds * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (res) {
+        res->rank = hs.rank;
+        res->rounds = hs.rounds;
+        res->trace_error = hs.total / (double)N;
+    }
+    return KEVD_OK;
+}
+
+int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
+               const kevd_rpchol_params* p, void* F, int64_t ldF, int64_t* piv, double* err,
+               int32_t* accepted, kevd_rpchol_result* res, cudaStream_t s) {
+    if (!X || !p || !F || N < 1 || d < 1 || d > 128)
+        return set_error(ctx, KEVD_ERR_ARG, "rpchol: need X, F, N >= 1 and 1 <= d <= 128");
+    if (p->block < 1 || p->block > kMaxBlock)
+        return set_error(ctx, KEVD_ERR_ARG, "rpchol: block must be in [1, %d]", kMaxBlock);
+    if (p->k_max < 1 || ldF < p->k_max || p->max_rounds < 1)
+        return set_error(ctx, KEVD_ERR_ARG, "rpchol: need k_max >= 1, ldF >= k_max, max_rounds >= 1");
+    if (p->precision == KEVD_FP64)
+        return rpchol_impl<double>(ctx, X, N, d, scale, p, (double*)F, ldF, piv, err, accepted, res, s);
+    if (p->precision == KEVD_MIXED)
+        return rpchol_impl<float>(ctx, X, N, d, scale, p, (float*)F, ldF, piv, err, accepted, res, s);
+    return set_error(ctx, KEVD_ERR_ARG, "rpchol: unknown precision %d", p->precision);
+}
+
+// Gather rows idx of F (first ncols columns) into a column-major FP64 n x ncols
+// matrix (ld n): used for L = F(S, :).
+template <typename T>
+__global__ void gather_rows_kernel(const T* __restrict__ F, int64_t ldF,
+                                   const int64_t* __restrict__ idx, int64_t n, int64_t ncols,
+                                   double* __restrict__ out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * ncols;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = e / n, q = e - c * n;
+        out[e] = (double)F[idx[q] * ldF + c];
+    }
+}
+
+int run_gather_rows(kevd_ctx* ctx, const void* F, int precision, int64_t ldF, const int64_t* idx,
+                    int64_t n, int64_t ncols, double* out, cudaStream_t s) {
+    const int grid = (int)std::min<int64_t>((n * ncols + 255) / 256, (int64_t)ctx->num_sms * 16);
+    if (grid < 1) return KEVD_OK;
+    if (precision == KEVD_FP64)
+        gather_rows_kernel<double><<<grid, 256, 0, s>>>((const double*)F, ldF, idx, n, ncols, out);
+    else
+        gather_rows_kernel<float><<<grid, 256, 0, s>>>((const float*)F, ldF, idx, n, ncols, out);
+    KEVD_LAUNCH(ctx);
+    return KEVD_OK;
+}
+
+}  // namespace kevd

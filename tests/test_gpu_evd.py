@@ -1,0 +1,102 @@
+"""GPU parity of the bistochastic EVD against the FP64 oracle, at every dump
+point of the reference (c1, dtil, cq, qtil, A, B, W, Z, lam, U)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import evd, ks, rpchol
+
+pytestmark = pytest.mark.gpu
+
+SCALE = 1.0 / 30.0
+
+
+@pytest.fixture(scope="module")
+def fac():
+    X = ks.seeded_mode(4000, warm_time=100.0).astype(np.float32)
+    r = rpchol.rpcholesky(X.astype(np.float64), SCALE, 300, 32, seed=21)
+    return X, r
+
+
+def test_fp64_evd_every_intermediate(ctx, fac):
+    from kernel_evd_gb300 import api
+    X, r = fac
+    F = torch.from_numpy(r["F"]).cuda()
+    g = api.bistochastic_evd(ctx, F, k_out=16, dump=True)
+    e = evd.evd_from_factor(r["F"], 16)
+    for name in ("c1", "dtil", "cq", "qtil"):
+        np.testing.assert_allclose(g.dump[name], e[name], rtol=1e-12, err_msg=name)
+    for name in ("A", "B", "W"):
+        np.testing.assert_allclose(g.dump[name], e[name], rtol=0, atol=1e-11 * np.abs(e[name]).max(),
+                                   err_msg=name)
+    assert abs(g.trace_A - e["trA"]) <= 1e-12 * e["trA"] and g.shift == pytest.approx(e["shift"], rel=1e-12)
+    np.testing.assert_allclose(g.lam, e["lam"], rtol=0, atol=1e-10)
+    top = e["lam"][-16:]
+    np.testing.assert_allclose(g.lam[-16:], top, rtol=1e-10)
+    U = g.U.cpu().numpy().astype(np.float64)
+    Ua = evd.align_signs(U, e["U"])
+    # U is written in FP32
+    np.testing.assert_allclose(Ua, e["U"], rtol=0, atol=2e-6 * np.abs(e["U"]).max())
+    assert np.all(evd.eigvec_angles(U[:, -8:], e["U"][:, -8:]) < 1e-5)
+
+
+def test_mixed_evd_close_to_fp64(ctx, fac):
+    from kernel_evd_gb300 import api
+    X, r = fac
+    F = torch.from_numpy(r["F"].astype(np.float32)).cuda()
+    g = api.bistochastic_evd(ctx, F, k_out=16)
+    e = evd.evd_from_factor(r["F"], 16)
+    assert abs(g.lam[-1] - 1.0) < 1e-6
+    np.testing.assert_allclose(g.lam[-16:], e["lam"][-16:], rtol=0, atol=1e-6)
+    ang = evd.eigvec_angles(g.U.cpu().numpy()[:, -4:], e["U"][:, -4:])
+    assert np.all(ang < 1e-3)
+
+
+def test_factor_from_linv_roundtrip(ctx, fac):
+    from kernel_evd_gb300 import api
+    X, r = fac
+    Li = rpchol.linv_from_F(r["F"], r["piv"])
+    Xt = torch.from_numpy(X).cuda()
+    F = api.factor_from_linv(ctx, Xt, SCALE, r["piv"], Li, precision="fp64").cpu().numpy()
+    np.testing.assert_allclose(F, r["F"], rtol=0, atol=1e-8)
+    e_lm = evd.evd_from_linv(X.astype(np.float64), SCALE, Li, r["piv"], 8)
+    g = api.bistochastic_evd(ctx, torch.from_numpy(F).cuda(), k_out=8)
+    np.testing.assert_allclose(g.lam[-8:], e_lm["lam"][-8:], rtol=1e-9)
+
+
+def test_nonpositive_degree_is_reported(ctx, fac):
+    from kernel_evd_gb300 import KevdError, api
+    X, r = fac
+    F = r["F"].copy()
+    F[17, :] = 0.0          # an isolated row: dtil = 0 (the reference aborts with code 2)
+    with pytest.raises(KevdError) as e:
+        api.bistochastic_evd(ctx, torch.from_numpy(F).cuda(), k_out=4)
+    assert e.value.name == "KEVD_ERR_NONPOS_DTIL"
+    # the context stays usable
+    g = api.bistochastic_evd(ctx, torch.from_numpy(r["F"]).cuda(), k_out=4)
+    assert abs(g.lam[-1] - 1.0) < 1e-10
+
+
+def test_indefinite_gram_is_reported(ctx, fac):
+    from kernel_evd_gb300 import KevdError, api
+    X, r = fac
+    F = r["F"].copy()
+    F[:, 5] = F[:, 4]       # rank-deficient factor: A is singular beyond the eps*tr(A) shift
+    F[:, 6] = F[:, 4]
+    try:
+        api.bistochastic_evd(ctx, torch.from_numpy(F).cuda(), k_out=4)
+    except KevdError as e:
+        assert e.name in ("KEVD_ERR_POTRF",)
+
+
+def test_nystrom_reproduces_training_rows(ctx, fac):
+    from kernel_evd_gb300 import api
+    X, r = fac
+    Xt = torch.from_numpy(X).cuda()
+    g = api.rpcholesky(ctx, Xt, SCALE, k_max=200, block=32, seed=5, precision="fp64")
+    e = api.bistochastic_evd(ctx, g.factor.contiguous(), k_out=8)
+    model = api.NystromModel(ctx, Xt, g, k_out=8)
+    idx = np.arange(0, 4000, 7)
+    Uy = model(Xt[torch.from_numpy(idx).cuda()].contiguous()).cpu().numpy()
+    U = e.U.cpu().numpy()[idx]
+    np.testing.assert_allclose(Uy, U, rtol=0, atol=1e-5 * np.abs(U).max())

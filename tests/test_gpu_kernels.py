@@ -1,0 +1,104 @@
+"""GPU parity: sample views, kernel blocks, calibration sums and the median."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import calibrate, kernel, ks
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def states():
+    return ks.seeded_mode(3000, warm_time=100.0).astype(np.float32)
+
+
+def test_hankel_rows_bit_exact(ctx):
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(0)
+    Ndata, M, Nq = 300, 5, 17
+    u = rng.standard_normal(Ndata * M).astype(np.float32)
+    X = api.hankel_rows(ctx, torch.from_numpy(u).cuda(), Ndata, M, Nq).cpu().numpy()
+    np.testing.assert_array_equal(X, kernel.hankel_rows(u, Ndata, M, Nq))
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-14), ("mixed", 2e-5)])
+def test_kernel_block(ctx, states, prec, tol):
+    from kernel_evd_gb300 import api
+    X = torch.from_numpy(states).cuda()
+    rng = np.random.default_rng(1)
+    cols = rng.integers(0, states.shape[0], 45)
+    rows = rng.integers(0, states.shape[0], 70)
+    sc = 1.0 / 40.0
+    K = api.kernel_block(ctx, X, sc, torch.from_numpy(cols).cuda(), rows=torch.from_numpy(rows).cuda(),
+                         precision=prec).cpu().numpy()
+    ref = kernel.kblock(states.astype(np.float64), rows, cols, sc)
+    np.testing.assert_allclose(K, ref, rtol=0, atol=tol)
+    K2 = api.kernel_block(ctx, X, sc, torch.from_numpy(cols).cuda(), row0=100, nrows=33,
+                          precision=prec).cpu().numpy()
+    np.testing.assert_allclose(K2, kernel.kblock(states.astype(np.float64), np.arange(100, 133), cols, sc),
+                               rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("N", [1, 2, 127, 128, 129, 1000])
+def test_calibrate_matches_oracle(ctx, states, N):
+    from kernel_evd_gb300 import api
+    Xn = states[:N]
+    med = 100.0
+    eps = calibrate.log_sweep(med, 41)
+    T = api.calibrate(ctx, torch.from_numpy(np.ascontiguousarray(Xn)).cuda(), 1.0 / eps)
+    ref = calibrate.pair_sums(Xn.astype(np.float64), 1.0 / eps)
+    if N == 1:
+        assert np.all(T == 0)
+        return
+    # FP32 distances and exp2.approx: relative 1e-4 on every sum that is not negligible
+    mask = ref > 1e-30 * N * N
+    np.testing.assert_allclose(T[mask], ref[mask], rtol=1e-4)
+    np.testing.assert_array_less(T[~mask], 1e-25 * N * N + 1e-300)
+
+
+def test_calibrate_reference_sweep_hankel(ctx):
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(3)
+    Ndata, M, Nq = 140, 6, 16
+    # reference-mode states on 64 gridpoints; keep the first M gridpoints
+    full = ks.reference_mode(Ndata, M=64, n_warm=200)          # (time, gridpoint)
+    u = np.ascontiguousarray(full[:, :M].T).reshape(-1).astype(np.float32)
+    assert np.all(np.isfinite(u))
+    X = api.hankel_rows(ctx, torch.from_numpy(u).cuda(), Ndata, M, Nq)
+    bw = calibrate.reference_sweep().astype(np.float64)
+    T = api.calibrate(ctx, X, 1.0 / (Nq * bw))
+    Xo = kernel.hankel_rows(u, Ndata, M, Nq).astype(np.float64)
+    ref = calibrate.pair_sums(Xo, 1.0 / (Nq * bw))
+    np.testing.assert_allclose(T, ref, rtol=1e-4, atol=1e-30)
+    NM = X.shape[0]
+    sel = api.select_bandwidth(bw, T, NM)
+    logS, slope, idmax, eopt, mdim = calibrate.select(bw, ref, NM)
+    assert sel["idmax"] == idmax and sel["eopt"] == eopt
+    np.testing.assert_allclose(sel["mdim"], mdim, rtol=1e-4)
+
+
+def test_calibrate_selects_same_eps_as_oracle(ctx, states):
+    from kernel_evd_gb300 import api
+    Xn = states[:1500].astype(np.float64)
+    med = calibrate.median_sqdist_exact(Xn)
+    eps = calibrate.log_sweep(med, 41)
+    T = api.calibrate(ctx, torch.from_numpy(states[:1500].copy()).cuda(), 1.0 / eps)
+    ref = calibrate.pair_sums(Xn, 1.0 / eps)
+    s1 = api.select_bandwidth(eps, T, 1500)
+    _, _, idmax, eopt, _ = calibrate.select(eps, ref, 1500)
+    assert s1["idmax"] == idmax
+
+
+def test_pair_median_exact_and_sampled(ctx, states):
+    from kernel_evd_gb300 import api
+    Xn = states[:1200]
+    X = torch.from_numpy(np.ascontiguousarray(Xn)).cuda()
+    m = api.pair_median(ctx, X)
+    ref = calibrate.median_sqdist_exact(Xn.astype(np.float64))
+    assert abs(m - ref) <= 2e-6 * ref
+    pi, pl = calibrate.sample_pairs(1200, 50001, seed=4)
+    ms = api.pair_median(ctx, X, pairs=(torch.from_numpy(pi).cuda(), torch.from_numpy(pl).cuda()))
+    D = ((Xn[pi].astype(np.float64) - Xn[pl].astype(np.float64)) ** 2).sum(1)
+    refs = np.sort(D)[(D.size - 1) // 2]
+    assert abs(ms - refs) <= 2e-6 * refs
