@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark: rank-2000 bistochastic kernel EVD of N = 2,000,000 KS states (d = 64)
+on one GB300, mixed precision vs the plain FP64 form.
+
+Workload (the block-RPCholesky + bistochastic-EVD configuration at scale):
+KS L = 22, 64 gridpoints, seed 0, 1000 time units discarded, one state per
+0.25; eps from the calibration procedure (41 log-spaced eps in 2^-10..2^10 x
+the median squared distance, max slope of log S vs log eps; median over a
+seeded 1e7-pair sample, sweep over a 100k-state strided subsample); block
+b = 64, rank k = 2000, top 32 eigenpairs.
+
+One step = rpcholesky(mixed) + bistochastic_evd on X resident in HBM; value
+is seconds per step (lower is better).  e2e repeats the step through the same
+public API with the host->device copy of X and the device->host copy of U and
+lam inside the timed region.  Inputs (X 512 MB, F 16 GB) are larger than L2.
+
+``--impl reference`` times the CPU implementation of the same pipeline
+(NumPy/OpenBLAS FP64 stored-factor RPCholesky + bistochastic EVD, the oracle
+port) on a row sample of the same workload with all host threads, and
+extrapolates to N rows (rows-proportional work x N/n_s + k x k dense work).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rank-2000 kernel-EVD time at 1e-6 trace err, mixed vs FP64 (1 GB300); p50/p99 lat"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=2_000_000)
+    ap.add_argument("--k", type=int, default=2000)
+    ap.add_argument("--b", type=int, default=64)
+    ap.add_argument("--kout", type=int, default=32)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--cpu-rows", type=int, default=40000, help="row sample of the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def sample_pairs(N: int, n_pairs: int, seed: int = 0):
+    rng = np.random.default_rng(seed)
+    i = rng.integers(0, N, n_pairs, dtype=np.int64)
+    l = rng.integers(0, N - 1, n_pairs, dtype=np.int64)
+    return i, l + (l >= i)
+
+
+def make_workload(n: int):
+    from kernel_evd_gb300 import datagen
+    t0 = time.time()
+    X = datagen.seeded_states(n, L=22.0, M=64, seed=0, warm_time=1000.0, dt=0.25)
+    return X, time.time() - t0
+
+
+def calibrate_eps(ctx, Xd, n):
+    """Median from a seeded 1e7-pair sample, 41-eps sweep on a strided subsample."""
+    import torch
+    from kernel_evd_gb300 import api
+    pi, pl = sample_pairs(n, min(10_000_000, max(1000, n * (n - 1) // 2)), seed=0)
+    med = api.pair_median(ctx, Xd, pairs=(torch.from_numpy(pi).cuda(), torch.from_numpy(pl).cuda()))
+    stride = max(1, n // 100_000)
+    Xs = Xd[::stride].contiguous()
+    eps = api.log_sweep(med, 41)
+    sums = api.calibrate(ctx, Xs, 1.0 / eps)
+    sel = api.select_bandwidth(eps, sums, Xs.shape[0])
+    return sel["eopt"], med, Xs.shape[0]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.rows = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(index)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4) if r[2 + j].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def reference_arm(args, n_gpus):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import baseline
+    X, _ = make_workload(args.n)
+    # eps on the CPU: same procedure with NumPy on a smaller subsample
+    from oracle import calibrate
+    med = calibrate.median_sqdist_sampled(X, n_pairs=1_000_000, seed=0)
+    stride = max(1, args.n // 20_000)
+    Xs = X[::stride].astype(np.float64)
+    eps_s = calibrate.log_sweep(med, 41)
+    T = calibrate.pair_sums(Xs, 1.0 / eps_s)
+    eps = calibrate.select(eps_s, T, Xs.shape[0])[3]
+    n_s = min(args.cpu_rows, args.n)
+    times = []
+    for _ in range(max(1, args.steps)):
+        t = baseline.timed_pipeline(X[:n_s], 1.0 / eps, args.k, args.b, args.kout)
+        times.append(t["stream_s"] * args.n / n_s + t["dense_s"])
+    v = float(np.median(times))
+    cores = os.cpu_count()
+    sample = (f"first {n_s} of {args.n} states, same k={args.k}, b={args.b}; rows-proportional time "
+              f"x {args.n}/{n_s} + k x k dense time; OPENBLAS_NUM_THREADS="
+              f"{os.environ.get('OPENBLAS_NUM_THREADS', 'default')}")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": n_gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic KS states (L=22, seed 0)",
+            "config": {"workload": f"block RPCholesky + bistochastic EVD, N={args.n}, d=64, k={args.k}, "
+                                   f"b={args.b}, top {args.kout}", "eps": eps},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_info()
+    n_gpus = ws if ws > 1 else args.gpus
+    if args.impl == "reference":
+        reference_arm(args, n_gpus)
+        return
+    import torch
+    from kernel_evd_gb300 import api
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    X, gen_s = make_workload(args.n)
+    N, d = X.shape
+    ctx = api.Context(local)
+    Xh = torch.from_numpy(X).pin_memory()
+    Xd = Xh.cuda()
+    eps, med, n_cal = calibrate_eps(ctx, Xd, N)
+    scale = 1.0 / eps
+    F = torch.empty((N, args.k), dtype=torch.float32, device="cuda")
+    U = torch.empty((N, args.kout), dtype=torch.float32, device="cuda")
+
+    def step(Xdev):
+        fac = api.rpcholesky(ctx, Xdev, scale, k_max=args.k, block=args.b, seed=1234, precision="mixed", F=F)
+        ev = api.bistochastic_evd(ctx, fac.factor, k_out=args.kout, U=U)
+        return fac, ev
+
+    for _ in range(args.warmup):
+        step(Xd)
+    barrier()
+    # --- device-resident timed region
+    stream = torch.cuda.current_stream()
+    api.profile_enable(ctx, True)
+    launches0 = api.launch_count(ctx)
+    clk = ClockSampler(local) if rank == 0 else None
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fac, ev = step(Xd)
+    e1.record(stream)
+    barrier()
+    clocks = clk.stop() if clk else None
+    launches = api.launch_count(ctx) - launches0
+    prof = api.profile_read(ctx)
+    api.profile_enable(ctx, False)
+    ms = e0.elapsed_time(e1) / args.steps
+    # --- end to end through the public API with host buffers
+    Uh = torch.empty((N, args.kout), dtype=torch.float32).pin_memory()
+    for _ in range(1):
+        Xd.copy_(Xh, non_blocking=True)
+        step(Xd)
+        Uh.copy_(U, non_blocking=True)
+    barrier()
+    h0 = torch.cuda.Event(enable_timing=True)
+    h1 = torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for _ in range(args.steps):
+        Xd.copy_(Xh, non_blocking=True)
+        fac_e, ev_e = step(Xd)
+        Uh.copy_(U, non_blocking=True)
+    h1.record(stream)
+    barrier()
+    e2e_ms = h0.elapsed_time(h1) / args.steps
+    lam_mixed = ev.lam.copy()
+    U_mixed = U.cpu().numpy().astype(np.float64)
+    result = {}
+    # --- plain FP64 form on the same workload and draws
+    if not args.no_fp64:
+        F64 = torch.empty((N, args.k), dtype=torch.float64, device="cuda")
+        U64 = torch.empty((N, args.kout), dtype=torch.float32, device="cuda")
+        small = Xd[:20000].contiguous()
+        api.bistochastic_evd(ctx, api.rpcholesky(ctx, small, scale, k_max=128, block=args.b, precision="fp64").factor,
+                             k_out=8)
+        barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        fac64 = api.rpcholesky(ctx, Xd, scale, k_max=args.k, block=args.b, seed=1234, precision="fp64", F=F64)
+        ev64 = api.bistochastic_evd(ctx, fac64.factor, k_out=args.kout, U=U64)
+        f1.record(stream)
+        barrier()
+        fp64_ms = f0.elapsed_time(f1)
+        top = args.kout
+        lam_err = np.abs(lam_mixed[-top:] - ev64.lam[-top:])
+        U64h = U64.cpu().numpy().astype(np.float64)
+        c = np.abs(np.einsum("ij,ij->j", U_mixed, U64h)) / (
+            np.linalg.norm(U_mixed, axis=0) * np.linalg.norm(U64h, axis=0))
+        ang = np.arccos(np.clip(c, 0, 1))
+        same = int(np.argmax(fac.piv != fac64.piv)) if np.any(fac.piv != fac64.piv) else int(fac.rank)
+        result["fp64"] = {"seconds": fp64_ms / 1e3, "speedup_mixed_vs_fp64": fp64_ms / ms,
+                          "trace_error": fac64.trace_error, "rank": fac64.rank,
+                          "top_eig_abs_err_max": float(lam_err.max()),
+                          "top_eig_abs_err_leading8": [float(x) for x in lam_err[::-1][:8]],
+                          "eigvec_angle_max_rad": float(ang.max()),
+                          "eigvec_angle_leading4_rad": [float(x) for x in ang[::-1][:4]],
+                          "common_pivot_prefix": same}
+        del F64, U64
+    # --- roofline of the dominant kernel over the timed region
+    kernels = {k: {"ms_total": v[0] / args.steps, "launches": v[1] // args.steps} for k, v in prof.items()}
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tc = peaks.get("bf16_tflops", 1897.9)
+    src = "of measured" if peaks else "of fallback"
+    k = fac.rank
+    acc = fac.accepted
+    r_old = np.concatenate([[0], np.cumsum(acc)[:-1]])
+    upd_bytes = float(np.sum(N * (4.0 * r_old + 4.0 * acc + 4.0 * d + 16.0)))
+    gram_flops = 2.0 * N * k * (k + 1)     # two Grams, lower triangle incl. diagonal
+    roof = {}
+    if "rp_update" in prof:
+        t = prof["rp_update"][0] / args.steps / 1e3
+        nl = max(1, prof["rp_update"][1] // args.steps)
+        roof["rp_update"] = {"bound": "hbm", "achieved": upd_bytes / t / 1e9, "peak": hbm, "unit": "GB/s",
+                             "frac": upd_bytes / t / 1e9 / hbm, "traffic": None,
+                             "bytes_per_launch": upd_bytes / nl, "note": src}
+    if "ev_gram" in prof:
+        t = prof["ev_gram"][0] / args.steps / 1e3
+        roof["ev_gram"] = {"bound": "tensor", "achieved": gram_flops / t / 1e12, "peak": tc, "unit": "TFLOP/s",
+                           "frac": gram_flops / t / 1e12 / tc, "traffic": None,
+                           "flops_per_launch": gram_flops / 2, "note": src + " bf16 dense"}
+    dom = max(prof, key=lambda k_: prof[k_][0]) if prof else None
+    roofline = roof.get(dom) or (next(iter(roof.values())) if roof else None)
+    if roofline is not None:
+        roofline = dict(roofline, kernel=dom)
+    # --- CPU baseline on rank 0 (bounded sample)
+    cpu = None
+    if rank == 0 and ws == 1:
+        from oracle import baseline
+        n_s = min(args.cpu_rows, N)
+        tb = baseline.timed_pipeline(X[:n_s], scale, args.k, args.b, args.kout)
+        est = tb["stream_s"] * N / n_s + tb["dense_s"]
+        cpu = {"value": est, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"first {n_s} of {N} states, k={args.k}, b={args.b}: rows-proportional "
+                         f"{tb['stream_s']:.2f} s x {N}/{n_s} + dense {tb['dense_s']:.2f} s"}
+    # --- max over ranks
+    val = ms / 1e3
+    if dist is not None:
+        t = torch.tensor([val, e2e_ms / 1e3], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        val, e2e_s = float(t[0]), float(t[1])
+    else:
+        e2e_s = e2e_ms / 1e3
+    if rank == 0:
+        line = {"metric": METRIC, "value": val, "unit": "s", "n_gpus": n_gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": val * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor / f64 pivot, diag, kxk",
+                "data": "synthetic KS states (L=22, d=64, seed 0; host ETDRK4 generator)",
+                "config": {"workload": f"block RPCholesky + bistochastic EVD, N={N}, d={d}, k={args.k}, "
+                                       f"b={args.b}, top {args.kout}, mixed precision",
+                           "eps": eps, "median_sqdist": med, "calibration_rows": n_cal,
+                           "l2": "inputs larger than L2 (X 512 MB, F 16 GB)",
+                           "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"},
+                "rank": int(fac.rank), "rounds": int(fac.rounds), "trace_error": fac.trace_error,
+                "lam_top": float(lam_mixed[-1]),
+                "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(N * d * 4),
+                        "d2h_bytes_per_step": int(N * args.kout * 4)},
+                "gpu_launches": int(launches // args.steps) * args.steps,
+                "roofline": roofline, "roofline_by_kernel": roof, "kernels": kernels,
+                "clocks": clocks, "cpu_baseline": cpu, "datagen_s": gen_s}
+        line.update(result)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -64,6 +64,16 @@ const char* kevd_last_error(const kevd_ctx* ctx);
 const char* kevd_status_name(int status);
 int kevd_abi_version(void);
 
+/* Profiling.  While enabled, CUDA events are recorded on the launching stream
+ * around each of this library's kernels; kevd_profile_read returns, for the
+ * idx-th kernel name, its accumulated device time and launch count (it
+ * synchronises the pending events).  Enabling resets the counters.
+ * kevd_launch_count counts every kernel this library launched. */
+int kevd_profile_enable(kevd_ctx* ctx, int on);
+int kevd_profile_read(kevd_ctx* ctx, int idx, char* name, int name_len,
+                      double* total_ms, int64_t* count);
+int64_t kevd_launch_count(const kevd_ctx* ctx);
+
 /* ---- sample views ------------------------------------------------------ */
 
 /* Materialise the delay-embedded samples of the reference programs as rows.

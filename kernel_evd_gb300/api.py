@@ -312,3 +312,30 @@ class NystromModel:
             self.close()
         except Exception:
             pass
+
+
+# ---- profiling ---------------------------------------------------------------
+def profile_enable(ctx: Context, on: bool = True):
+    """Record per-kernel device time (CUDA events on the launching stream)."""
+    ctx._check(ctx.lib.kevd_profile_enable(ctx.h, 1 if on else 0))
+
+
+def profile_read(ctx: Context) -> dict:
+    """{kernel name: (total ms, launches)} accumulated since profile_enable."""
+    out = {}
+    buf = C.create_string_buffer(128)
+    i = 0
+    while True:
+        ms = C.c_double()
+        cnt = C.c_int64()
+        st = ctx.lib.kevd_profile_read(ctx.h, i, buf, 128, C.byref(ms), C.byref(cnt))
+        if st != 0:
+            break
+        out[buf.value.decode()] = (ms.value, cnt.value)
+        i += 1
+    return out
+
+
+def launch_count(ctx: Context) -> int:
+    """Kernels launched by this library through ctx so far."""
+    return int(ctx.lib.kevd_launch_count(ctx.h))

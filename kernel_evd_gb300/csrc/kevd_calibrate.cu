@@ -167,8 +167,11 @@ int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double*
     const size_t smem = calib_smem(d);
     KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_tiles_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, c2, n_scales, n_tiles, partial);
-    KEVD_LAUNCH(ctx);
+    {
+        ProfScope ps(ctx, "calibrate_tiles", s);
+        calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, c2, n_scales, n_tiles, partial);
+        KEVD_LAUNCH(ctx);
+    }
     reduce_partials_kernel<<<1, kCalMaxScales, 0, s>>>(partial, grid, n_scales, out);
     KEVD_LAUNCH(ctx);
     KEVD_CUDA(ctx, cudaMemcpyAsync(sums, out, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -3,6 +3,7 @@
 #include "kevd_internal.cuh"
 
 #include <cmath>
+#include <iterator>
 #include <cstdarg>
 #include <cstring>
 #include <vector>
@@ -69,6 +70,24 @@ using namespace kevd;
 #define KEVD_CHECK_CTX(ctx) \
     if (!(ctx)) return KEVD_ERR_ARG
 
+static void resolve_profile(kevd_ctx* ctx) {
+    for (auto& r : ctx->pending) {
+        float ms = 0.f;
+        cudaEventSynchronize(r.b);
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            auto& acc = ctx->prof_acc[r.name];
+            acc.first += ms;
+            acc.second += 1;
+        } else {
+            cudaGetLastError();
+        }
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->pending.clear();
+}
+
+
 extern "C" {
 
 int kevd_abi_version(void) { return 1; }
@@ -114,6 +133,8 @@ int kevd_ctx_create(int device, kevd_ctx** out) {
 void kevd_ctx_destroy(kevd_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    resolve_profile(ctx);
+    for (cudaEvent_t e : ctx->pool) cudaEventDestroy(e);
     ctx->arena.release();
     if (ctx->blas) cublasDestroy(ctx->blas);
     if (ctx->solver) cusolverDnDestroy(ctx->solver);
@@ -122,6 +143,32 @@ void kevd_ctx_destroy(kevd_ctx* ctx) {
 }
 
 const char* kevd_last_error(const kevd_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int kevd_profile_enable(kevd_ctx* ctx, int on) {
+    KEVD_CHECK_CTX(ctx);
+    resolve_profile(ctx);
+    ctx->prof_acc.clear();
+    ctx->prof = on != 0;
+    return KEVD_OK;
+}
+
+int kevd_profile_read(kevd_ctx* ctx, int idx, char* name, int name_len, double* total_ms,
+                      int64_t* count) {
+    KEVD_CHECK_CTX(ctx);
+    resolve_profile(ctx);
+    if (idx < 0 || idx >= (int)ctx->prof_acc.size()) return KEVD_ERR_ARG;
+    auto it = ctx->prof_acc.begin();
+    std::advance(it, idx);
+    if (name && name_len > 0) {
+        std::strncpy(name, it->first.c_str(), name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    if (total_ms) *total_ms = it->second.first;
+    if (count) *count = it->second.second;
+    return KEVD_OK;
+}
+
+int64_t kevd_launch_count(const kevd_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 int kevd_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M, int64_t Nq, float* X,
                      void* stream) {

@@ -271,6 +271,7 @@ static int colsum(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, 
     int st = KEVD_OK;
     double* partial = arena_get<double>(ctx, "ev.cpart", (size_t)ny * k, &st);
     if (st != KEVD_OK) return st;
+    ProfScope ps(ctx, "ev_colsum", s);
     ev_colsum_kernel<T><<<dim3(ceil_div(k, 256), ny), 256, 0, s>>>(F, ldF, N, k, w, rows_per, partial);
     KEVD_LAUNCH(ctx);
     ev_sum_partials_kernel<<<ceil_div(k, 256), 256, 0, s>>>(partial, ny, k, out);
@@ -285,6 +286,7 @@ static int rowdot(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, 
     KEVD_CUDA(ctx, cudaFuncSetAttribute(ev_rowdot_kernel<T>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<int64_t>((N + 7) / 8, (int64_t)ctx->num_sms * 8);
+    ProfScope ps(ctx, "ev_rowdot", s);
     ev_rowdot_kernel<T><<<grid, 256, smem, s>>>(F, ldF, N, k, v, y, yinv, bad);
     KEVD_LAUNCH(ctx);
     return KEVD_OK;
@@ -301,8 +303,11 @@ static int gram(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, co
     int st = KEVD_OK;
     double* partial = arena_get<double>(ctx, "ev.gpart", (size_t)n_split * n_tiles * kGT * kGT, &st);
     if (st != KEVD_OK) return st;
-    ev_gram_kernel<T><<<dim3(n_tiles, n_split), 256, 0, s>>>(F, ldF, N, k, w, rows_per, partial);
-    KEVD_LAUNCH(ctx);
+    {
+        ProfScope ps(ctx, "ev_gram", s);
+        ev_gram_kernel<T><<<dim3(n_tiles, n_split), 256, 0, s>>>(F, ldF, N, k, w, rows_per, partial);
+        KEVD_LAUNCH(ctx);
+    }
     ev_gram_reduce_kernel<<<n_tiles, 256, 0, s>>>(partial, n_tiles, n_split, k, G);
     KEVD_LAUNCH(ctx);
     return KEVD_OK;
@@ -363,6 +368,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     }
 
     // dense 1: shift, Cholesky A + sI = L L^T
+    ProfScope ps_dense(ctx, "dense_kxk", s);
     ev_trace_shift_kernel<<<1, 1024, 0, s>>>(A, k, trsh);
     KEVD_LAUNCH(ctx);
     KEVD_SOLVER(ctx, cusolverDnSetStream(ctx->solver, s));
@@ -396,8 +402,11 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
                                CUBLAS_DIAG_NON_UNIT, (int)k, k_out, &one, A, (int)k, Z, (int)k));
     // pass 4: U = Dtil^{-1} F Z
-    ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
-    KEVD_LAUNCH(ctx);
+    {
+        ProfScope ps(ctx, "ev_u", s);
+        ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
+        KEVD_LAUNCH(ctx);
+    }
     if (dump) KEVD_TRY(d2h(ctx, dump->Z, Z, (size_t)k * k_out, s));
     double htr[2];
     KEVD_CUDA(ctx, cudaMemcpyAsync(htr, trsh, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "../../include/kevd.h"
 
@@ -49,6 +50,17 @@ struct kevd_ctx {
     void* pinned = nullptr;  // small pinned host staging area
     size_t pinned_bytes = 0;
     std::string last_error;
+    // profiling: CUDA events recorded on the launching stream around each
+    // kernel (only while enabled) and a count of this library's launches
+    bool prof = false;
+    int64_t launches = 0;
+    struct Rec {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    std::map<std::string, std::pair<double, int64_t>> prof_acc;
 };
 
 namespace kevd {
@@ -65,6 +77,7 @@ int set_error(kevd_ctx* ctx, int code, const char* fmt, ...);
 
 #define KEVD_LAUNCH(ctx)                                                              \
     do {                                                                              \
+        ++(ctx)->launches;                                                            \
         cudaError_t e_ = cudaGetLastError();                                          \
         if (e_ != cudaSuccess)                                                        \
             return ::kevd::set_error((ctx), KEVD_ERR_CUDA, "%s:%d launch: %s",        \
@@ -92,6 +105,43 @@ int set_error(kevd_ctx* ctx, int code, const char* fmt, ...);
         int st_ = (expr);              \
         if (st_ != KEVD_OK) return st_; \
     } while (0)
+
+// Times the kernels launched on stream s during its lifetime under name.
+class ProfScope {
+  public:
+    ProfScope(kevd_ctx* ctx, const char* name, cudaStream_t s) : ctx_(ctx), name_(name), s_(s) {
+        if (ctx_->prof) {
+            a_ = take();
+            if (a_) cudaEventRecord(a_, s_);
+        }
+    }
+    ~ProfScope() {
+        if (!a_) return;
+        cudaEvent_t b = take();
+        if (!b) return;
+        cudaEventRecord(b, s_);
+        ctx_->pending.push_back({name_, a_, b});
+    }
+
+  private:
+    cudaEvent_t take() {
+        if (!ctx_->pool.empty()) {
+            cudaEvent_t e = ctx_->pool.back();
+            ctx_->pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return e;
+    }
+    kevd_ctx* ctx_;
+    const char* name_;
+    cudaStream_t s_;
+    cudaEvent_t a_ = nullptr;
+};
 
 template <typename T>
 T* arena_get(kevd_ctx* ctx, const char* name, size_t count, int* st) {

@@ -537,16 +537,31 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     int* done_h = static_cast<int*>(ctx->pinned);
     int round = 0;
     for (; round < p->max_rounds; ++round) {
-        rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, round, b, p->seed, unif,
-                                                      props, rs, p->k_max, p->max_rounds,
-                                                      p->err_target, err);
-        rp_hgram_kernel<T><<<n_split + n_kss, 256, 0, s>>>(F, ldF, X, d, scale, props, b, n_split,
-                                                         rs, hpart, kss);
-        rp_factor_kernel<<<1, 256, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol, p->k_max,
-                                             props, rs, minv, minv_f, sacc, piv, hm);
-        rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv, minv_f,
-                                                       b, rs, dvec, dblk);
-        KEVD_LAUNCH(ctx);
+        {
+            ProfScope ps(ctx, "rp_sample", s);
+            rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, round, b, p->seed,
+                                                          unif, props, rs, p->k_max, p->max_rounds,
+                                                          p->err_target, err);
+            KEVD_LAUNCH(ctx);
+        }
+        {
+            ProfScope ps(ctx, "rp_hgram", s);
+            rp_hgram_kernel<T><<<n_split + n_kss, 256, 0, s>>>(F, ldF, X, d, scale, props, b,
+                                                             n_split, rs, hpart, kss);
+            KEVD_LAUNCH(ctx);
+        }
+        {
+            ProfScope ps(ctx, "rp_factor", s);
+            rp_factor_kernel<<<1, 256, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
+                                                 p->k_max, props, rs, minv, minv_f, sacc, piv, hm);
+            KEVD_LAUNCH(ctx);
+        }
+        {
+            ProfScope ps(ctx, "rp_update", s);
+            rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv,
+                                                           minv_f, b, rs, dvec, dblk);
+            KEVD_LAUNCH(ctx);
+        }
         if ((round & 3) == 3) {
             KEVD_CUDA(ctx, cudaMemcpyAsync(done_h, &rs->done, sizeof(int), cudaMemcpyDeviceToHost, s));
             KEVD_CUDA(ctx, cudaStreamSynchronize(s));

@@ -71,11 +71,13 @@ def reject_and_factor(H: np.ndarray, ua: np.ndarray, tol: float, cap: int):
 
 
 def rpcholesky(X, scale: float, k_max: int, b: int, tol: float = 1e-10, seed: int = 1234,
-               n_rounds: int | None = None, draw=None, err_target: float = 0.0):
+               n_rounds: int | None = None, draw=None, err_target: float = 0.0,
+               timing: dict | None = None):
     """Stored-factor block RPCholesky.
 
     Returns dict(F (N x r), piv (r,), err (per round), hm (accepted per round),
-    proposals (per round), accpos (per round))."""
+    proposals (per round), accpos (per round)).  ``timing``, if given, receives
+    the seconds spent in the b x b accept/factor steps (``factor_s``)."""
     X = np.asarray(X)
     N = X.shape[0]
     if draw is None:
@@ -94,7 +96,12 @@ def rpcholesky(X, scale: float, k_max: int, b: int, tol: float = 1e-10, seed: in
         ua = draw(rnd, 1, b)
         Fp = F[Sp, :r]
         H = kblock(X, Sp, Sp, scale) - Fp @ Fp.T
+        if timing is not None:
+            import time
+            t0 = time.perf_counter()
         accpos, Lc, Minv = reject_and_factor(H, ua, tol, k_max - r)
+        if timing is not None:
+            timing["factor_s"] = timing.get("factor_s", 0.0) + time.perf_counter() - t0
         nacc = accpos.size
         if nacc > 0:
             Si = Sp[accpos]
