@@ -177,6 +177,15 @@ typedef struct {
     double* Z;     /* k x k_out  R^{-1} V[:, top k_out] (column-major)       */
 } kevd_evd_dump;
 
+/* Weighted Gram G = F^T diag(s)^2 F (k x k, column-major, both triangles) --
+ * the Atil / Btil accumulation of ks_kevd.cu:1091-1159, :1627-1685 on a stored
+ * factor.  F: device N x ldF (double for KEVD_FP64, float for KEVD_MIXED: the
+ * FP32 factor is contracted on the tensor cores in 3xTF32 with FP64
+ * accumulation across row chunks).  s: device, N doubles.  G: device. */
+int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision,
+                       int64_t N, int64_t k, int64_t ldF, const double* s,
+                       double* G, void* stream);
+
 /* Bistochastic EVD of Khat = F F^T.  F: device N x ldF (double or float by
  * precision).  lam: host, k eigenvalues ascending.  U: device, N x k_out
  * float row-major, columns ascending (the last is the leading eigenvector),

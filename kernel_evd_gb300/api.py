@@ -278,6 +278,20 @@ def bistochastic_evd(ctx: Context, F: torch.Tensor, k: int | None = None, k_out:
     return Eigendecomposition(lam=lam, U=U, trace_A=info.trace_A, shift=info.shift, dump=host)
 
 
+def weighted_gram(ctx: Context, F: torch.Tensor, s: torch.Tensor, k: int | None = None) -> torch.Tensor:
+    """G = F^T diag(s)^2 F (k x k FP64 on the device; FP32 F runs on the tensor cores)."""
+    if not (F.is_cuda and F.dtype in (torch.float32, torch.float64) and F.stride(1) == 1):
+        raise ValueError("F must be a CUDA float32/float64 tensor with unit column stride")
+    _need_cuda(s, torch.float64, "s")
+    p = KEVD_FP64 if F.dtype == torch.float64 else KEVD_MIXED
+    N = F.shape[0]
+    if k is None:
+        k = F.shape[1]
+    G = torch.empty((k, k), dtype=torch.float64, device=F.device)
+    ctx._check(ctx.lib.kevd_weighted_gram(ctx.h, _ptr(F), p, N, k, F.stride(0), _ptr(s), _ptr(G), _stream()))
+    return G.T.contiguous()   # column-major storage -> row-major view
+
+
 class NystromModel:
     """Resident landmarks + eigenfunction coefficients for out-of-sample states."""
 

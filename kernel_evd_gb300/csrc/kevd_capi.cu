@@ -259,6 +259,12 @@ int kevd_bistochastic_evd(kevd_ctx* ctx, const void* F, int32_t precision, int64
                                 as_stream(stream));
 }
 
+int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision, int64_t N, int64_t k, int64_t ldF,
+                       const double* s, double* G, void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_weighted_gram(ctx, F, precision, N, k, ldF, s, G, as_stream(stream));
+}
+
 __global__ void cast_d2f_kernel(const double* __restrict__ a, int64_t rows, int64_t cols,
                                 int64_t lda, float* __restrict__ b, int64_t ldb) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols;

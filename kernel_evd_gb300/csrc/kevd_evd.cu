@@ -25,6 +25,9 @@
 
 namespace kevd {
 
+int run_gram_tc(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, const double* s, double* G,
+                cudaStream_t st);
+
 // ---- column sums c = F^T w (w == nullptr: ones) ----------------------------
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -171,6 +174,12 @@ __global__ void ev_gram_reduce_kernel(const double* __restrict__ partial, int n_
 }
 
 // ---- small helpers ---------------------------------------------------------
+__global__ void ev_rsqrt_kernel(const double* __restrict__ q, double* __restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = 1.0 / sqrt(q[i]);
+}
+
 __global__ void ev_square_kernel(const double* __restrict__ x, double* __restrict__ y, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -263,6 +272,223 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
     }
 }
 
+// ---- Rayleigh-Ritz refinement of the leading eigenpairs (FP32 factor) -------
+// With U = Dtil^{-1} F Z (N x m), U^T P U = T1^T B T1 where T1 = F^T Dtil^{-1} U
+// (k x m) and B = F^T Qtil^{-1} F, so
+//     H = U^T P U = sum_i w_i w_i^T / qtil_i,  w_i = F_i T1,
+//     M = U^T U   = sum_i u_i u_i^T.
+// Both are formed in streaming passes over F with FP32 products (round to
+// nearest, unbiased) summed in FP64 across rows; the m x m pencil (H, M) gives
+// Ritz values accurate to the square of the eigenvector error of the Gram path.
+
+// T1 partial: rows [r0, r1) of this CTA, 64 columns of F x 32 columns of U.
+// thread: column c = c0 + (tid & 63), U columns 8 (tid >> 6) .. +8.
+template <typename T>
+__global__ void __launch_bounds__(256)
+rr_t1_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const float* __restrict__ U, int m,
+             const double* __restrict__ dinv, int j0, int64_t rows_per, double* __restrict__ partial) {
+    __shared__ float Fs[32][65];
+    __shared__ float Ws[32][33];
+    const int tc = threadIdx.x & 63, tj = threadIdx.x >> 6;
+    const int64_t c0 = (int64_t)blockIdx.x * 64;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
+    double acc64[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc64[q] = 0.0;
+    for (int64_t i0 = r0; i0 < r1; i0 += 32) {
+        for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+            const int rr = e >> 6, cc = e & 63;
+            const int64_t i = i0 + rr, c = c0 + cc;
+            Fs[rr][cc] = (i < r1 && c < k) ? (float)F[i * ldF + c] : 0.f;
+        }
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int rr = e >> 5, jj = e & 31;
+            const int64_t i = i0 + rr;
+            const int j = j0 + jj;
+            Ws[rr][jj] = (i < r1 && j < m) ? (float)((double)U[i * m + j] * dinv[i]) : 0.f;
+        }
+        __syncthreads();
+        float acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+#pragma unroll 8
+        for (int rr = 0; rr < 32; ++rr) {
+            const float f = Fs[rr][tc];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] = fmaf(f, Ws[rr][8 * tj + q], acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc64[q] += (double)acc[q];
+        __syncthreads();
+    }
+    const int64_t c = c0 + tc;
+    if (c < k) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = j0 + 8 * tj + q;
+            if (j < m) partial[((int64_t)blockIdx.y * k + c) * m + j] = acc64[q];
+        }
+    }
+}
+
+__global__ void rr_sum_kernel(const double* __restrict__ partial, int n_parts, int64_t len,
+                              double* __restrict__ out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < len;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int p = 0; p < n_parts; ++p) s += partial[(int64_t)p * len + e];
+        out[e] = s;
+    }
+}
+
+// H and M partials over 64-row tiles: w = F_i T1 (64 x m) accumulated over
+// 32-column chunks of F in FP32; then H += (w/sqrt(q))^T (w/sqrt(q)) and
+// M += u^T u over the tile, per-tile FP32 sums added into FP64 accumulators.
+// m <= 32.  Thread layout for w: rows 4 (tid >> 4) .. +4, U columns 2 (tid & 15) .. +2.
+template <typename T>
+__global__ void __launch_bounds__(256)
+rr_hm_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ T1, int m,
+             const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
+    __shared__ float Fs[64][33];
+    __shared__ float Ts[32][33];
+    __shared__ float Ws[64][33];
+    __shared__ float Us[64][33];
+    const int tid = threadIdx.x;
+    const int wr = 4 * (tid >> 4), wj = 2 * (tid & 15);
+    // H / M ownership: entries e = tid + 256 q (q < 4) of the 32 x 32 matrices
+    double h64[4] = {0, 0, 0, 0}, m64[4] = {0, 0, 0, 0};
+    const int64_t n_tiles = (N + 63) / 64;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const int64_t i0 = t * 64;
+        float w[4][2];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) w[a][0] = w[a][1] = 0.f;
+        for (int64_t c0 = 0; c0 < k; c0 += 32) {
+            __syncthreads();
+            for (int e = tid; e < 64 * 32; e += 256) {
+                const int rr = e >> 5, cc = e & 31;
+                const int64_t i = i0 + rr, c = c0 + cc;
+                Fs[rr][cc] = (i < N && c < k) ? (float)F[i * ldF + c] : 0.f;
+            }
+            for (int e = tid; e < 32 * 32; e += 256) {
+                const int cc = e >> 5, jj = e & 31;
+                const int64_t c = c0 + cc;
+                Ts[cc][jj] = (c < k && jj < m) ? (float)T1[c * m + jj] : 0.f;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int cc = 0; cc < 32; ++cc) {
+                const float t0 = Ts[cc][wj], t1 = Ts[cc][wj + 1];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float f = Fs[wr + a][cc];
+                    w[a][0] = fmaf(f, t0, w[a][0]);
+                    w[a][1] = fmaf(f, t1, w[a][1]);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int64_t i = i0 + wr + a;
+            const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
+            Ws[wr + a][wj] = w[a][0] * sq;
+            Ws[wr + a][wj + 1] = w[a][1] * sq;
+        }
+        for (int e = tid; e < 64 * 32; e += 256) {
+            const int rr = e >> 5, jj = e & 31;
+            const int64_t i = i0 + rr;
+            Us[rr][jj] = (i < N && jj < m) ? U[i * m + jj] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + 256 * q;
+            const int ja = e >> 5, jb = e & 31;
+            float hs = 0.f, ms = 0.f;
+            for (int rr = 0; rr < 64; ++rr) {
+                hs = fmaf(Ws[rr][ja], Ws[rr][jb], hs);
+                ms = fmaf(Us[rr][ja], Us[rr][jb], ms);
+            }
+            h64[q] += (double)hs;
+            m64[q] += (double)ms;
+        }
+    }
+    double* out = partial + (int64_t)blockIdx.x * 2048;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        out[tid + 256 * q] = h64[q];
+        out[1024 + tid + 256 * q] = m64[q];
+    }
+}
+
+// U <- U C (N x m times m x m), C column-major.
+__global__ void rr_rotate_kernel(float* __restrict__ U, int64_t N, int m, const double* __restrict__ C) {
+    __shared__ double Cs[32 * 32];
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) Cs[e] = C[e];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        float u[32], v[32];
+        for (int j = 0; j < m; ++j) u[j] = U[i * m + j];
+        for (int j = 0; j < m; ++j) {
+            double s = 0.0;
+            for (int q = 0; q < m; ++q) s += (double)u[q] * Cs[j * m + q];
+            v[j] = (float)s;
+        }
+        for (int j = 0; j < m; ++j) U[i * m + j] = v[j];
+    }
+}
+
+template <typename T>
+static int rayleigh_ritz(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, int m, float* U,
+                         const double* dinv, const double* qinv, double* lam_top, cudaStream_t s) {
+    ProfScope ps(ctx, "ev_ritz", s);
+    int st = KEVD_OK;
+    const int ny = (int)std::min<int64_t>((N + 4095) / 4096, (int64_t)ctx->num_sms * 2);
+    const int64_t rows_per = ((N + ny - 1) / ny + 31) / 32 * 32;
+    double* tpart = arena_get<double>(ctx, "rr.tpart", (size_t)ny * k * m, &st);
+    double* T1 = arena_get<double>(ctx, "rr.T1", (size_t)k * m, &st);
+    const int nhm = ctx->num_sms * 2;
+    double* hmpart = arena_get<double>(ctx, "rr.hmpart", (size_t)nhm * 2048, &st);
+    double* HM = arena_get<double>(ctx, "rr.HM", 2048, &st);
+    double* w = arena_get<double>(ctx, "rr.w", 64, &st);
+    int* info = arena_get<int>(ctx, "rr.info", 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
+    for (int j0 = 0; j0 < m; j0 += 32) {
+        rr_t1_kernel<T><<<dim3(ceil_div(k, 64), ny), 256, 0, s>>>(F, ldF, N, k, U, m, dinv, j0, rows_per, tpart);
+        KEVD_LAUNCH(ctx);
+    }
+    rr_sum_kernel<<<ceil_div(k * m, 256), 256, 0, s>>>(tpart, ny, k * m, T1);
+    KEVD_LAUNCH(ctx);
+    rr_hm_kernel<T><<<nhm, 256, 0, s>>>(F, ldF, N, k, T1, m, U, qinv, hmpart);
+    KEVD_LAUNCH(ctx);
+    rr_sum_kernel<<<8, 256, 0, s>>>(hmpart, nhm, 2048, HM);
+    KEVD_LAUNCH(ctx);
+    // H and M are stored 32 x 32 (row-major = column-major, symmetric); use the
+    // leading m x m with leading dimension 32
+    int lwork = 0;
+    KEVD_SOLVER(ctx, cusolverDnDsygvd_bufferSize(ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                                 CUBLAS_FILL_MODE_LOWER, m, HM, 32, HM + 1024, 32, w, &lwork));
+    double* work = arena_get<double>(ctx, "rr.work", (size_t)lwork + 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
+    KEVD_SOLVER(ctx, cusolverDnDsygvd(ctx->solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
+                                      CUBLAS_FILL_MODE_LOWER, m, HM, 32, HM + 1024, 32, w, work, lwork, info));
+    // eigenvectors C (m x m, ld 32) -> compact ld m for the rotation
+    double* C = arena_get<double>(ctx, "rr.C", (size_t)m * m, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
+    KEVD_CUDA(ctx, cudaMemcpy2DAsync(C, m * sizeof(double), HM, 32 * sizeof(double), m * sizeof(double), m,
+                                     cudaMemcpyDeviceToDevice, s));
+    rr_rotate_kernel<<<ctx->num_sms * 4, 128, 0, s>>>(U, N, m, C);
+    KEVD_LAUNCH(ctx);
+    int hinfo = 0;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(lam_top, w, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hinfo != 0) return set_error(ctx, KEVD_ERR_SYEVD, "rayleigh_ritz: sygvd failed, info %d", hinfo);
+    return KEVD_OK;
+}
+
 template <typename T>
 static int colsum(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, const double* w,
                   double* out, cudaStream_t s) {
@@ -353,11 +579,19 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     if (hflags[0]) return set_error(ctx, KEVD_ERR_NONPOS_DTIL, "bistochastic_evd: nonpositive dtil");
     if (hflags[1]) return set_error(ctx, KEVD_ERR_NONPOS_QTIL, "bistochastic_evd: nonpositive qtil");
 
-    // Grams
-    ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
-    KEVD_LAUNCH(ctx);
-    KEVD_TRY(gram<T>(ctx, F, ldF, N, k, w2, A, s));
-    KEVD_TRY(gram<T>(ctx, F, ldF, N, k, qinv, B, s));
+    // Grams: A = (Dtil^{-1} F)^T (Dtil^{-1} F), B = (Qtil^{-1/2} F)^T (Qtil^{-1/2} F)
+    if (sizeof(T) == 4) {
+        // FP32 factor: 3xTF32 tcgen05 Gram with FP64 accumulation across row chunks
+        ev_rsqrt_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(qtil, w2, N);
+        KEVD_LAUNCH(ctx);
+        KEVD_TRY(run_gram_tc(ctx, (const float*)F, ldF, N, k, dinv, A, s));
+        KEVD_TRY(run_gram_tc(ctx, (const float*)F, ldF, N, k, w2, B, s));
+    } else {
+        ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
+        KEVD_LAUNCH(ctx);
+        KEVD_TRY(gram<T>(ctx, F, ldF, N, k, w2, A, s));
+        KEVD_TRY(gram<T>(ctx, F, ldF, N, k, qinv, B, s));
+    }
     if (dump) {
         KEVD_TRY(d2h(ctx, dump->c1, c1, k, s));
         KEVD_TRY(d2h(ctx, dump->dtil, dtil, N, s));
@@ -413,6 +647,13 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     KEVD_CUDA(ctx, cudaMemcpyAsync(hflags, flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (lam_h) KEVD_CUDA(ctx, cudaMemcpyAsync(lam_h, lam, k * sizeof(double), cudaMemcpyDeviceToHost, s));
     KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (sizeof(T) == 4 && hflags[2] == 0 && hflags[3] == 0 && k_out <= 32) {
+        // FP32 factor: refine the leading k_out eigenpairs by Rayleigh-Ritz in FP64
+        double top[32];
+        KEVD_TRY(rayleigh_ritz<T>(ctx, F, ldF, N, k, k_out, U, dinv, qinv, top, s));
+        if (lam_h)
+            for (int j = 0; j < k_out; ++j) lam_h[k - k_out + j] = top[j];
+    }
     if (info) {
         info->trace_A = htr[0];
         info->shift = htr[1];
@@ -421,6 +662,22 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
         return set_error(ctx, KEVD_ERR_POTRF, "bistochastic_evd: potrf failed, info %d", hflags[2]);
     if (hflags[3] != 0)
         return set_error(ctx, KEVD_ERR_SYEVD, "bistochastic_evd: syevd failed, info %d", hflags[3]);
+    return KEVD_OK;
+}
+
+int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
+                      const double* s_dev, double* G, cudaStream_t st) {
+    if (!F || !s_dev || !G || N < 1 || k < 1 || ldF < k)
+        return set_error(ctx, KEVD_ERR_ARG, "weighted_gram: bad arguments");
+    if (precision == KEVD_MIXED) return run_gram_tc(ctx, (const float*)F, ldF, N, k, s_dev, G, st);
+    if (precision != KEVD_FP64) return set_error(ctx, KEVD_ERR_ARG, "weighted_gram: unknown precision");
+    int rc = KEVD_OK;
+    double* w2 = arena_get<double>(ctx, "wg.w2", N, &rc);
+    if (rc != KEVD_OK) return set_error(ctx, rc, "weighted_gram: out of device memory");
+    ev_square_kernel<<<ctx->num_sms * 4, 256, 0, st>>>(s_dev, w2, N);
+    KEVD_LAUNCH(ctx);
+    KEVD_TRY(gram<double>(ctx, (const double*)F, ldF, N, k, w2, G, st));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(st));
     return KEVD_OK;
 }
 

@@ -1,0 +1,342 @@
+// Weighted Gram G = Y^T Y, Y = diag(s) F, of an FP32 factor on the tcgen05
+// tensor cores (the A and B Grams of the bistochastic EVD).
+//
+// Precision: 4xTF32.  Each element y is split as hi = rn_tf32(y) and
+// lo = rn_tf32(y - hi) (both exact tf32 values, so every product is exact in
+// FP32 and the split error is unbiased, about 2^-23 |y|); a 128 x 128 output
+// tile accumulates lo_a lo_b^T + hi_a lo_b^T + lo_a hi_b^T + hi_a hi_b^T in
+// FP32 in Tensor Memory.  The tensor-core accumulator rounds each update
+// with a one-sided bias, so the FP32 partial is kept short: every 1024 rows it
+// is added into an FP64 tile in global memory and the long sum over N rows is
+// FP64 (the Gram accumulators of the reference are FP64,
+// ks_kevd.cu:1152-1158).  The relative error of a Gram entry is about 1e-5;
+// eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
+//
+// CTA roles (416 threads):
+//   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
+//               lanes 32q..32q+31 = tile rows)
+//   warps 4-11  converters: coalesced float4 loads of 32 rows x 128 columns
+//               of F for the a and b column blocks, row scaling, tf32 split,
+//               transposed stores into K-major SW128 operand tiles
+//   warp 12     TMEM allocation and the single MMA-issuing thread
+// A 3-stage shared-memory ring (64 KB per stage: a_hi, a_lo, b_hi, b_lo)
+// and a double-buffered TMEM accumulator (2 x 128 columns) are handed over
+// with mbarriers; every wait is bounded and sets an error flag on timeout.
+#include "kevd_internal.cuh"
+#include "kevd_tc.cuh"
+
+#include <algorithm>
+
+namespace kevd {
+
+namespace {
+
+constexpr int kTT = 128;               // output tile edge
+constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
+constexpr int kStages = 3;
+constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
+constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
+constexpr int kStageBytes = 4 * kOpBytes;   // a_hi, a_lo, b_hi, b_lo
+constexpr int kEpiWarps = 4;
+constexpr int kCvtWarps = 8;
+constexpr int kMmaWarp = kEpiWarps + kCvtWarps;
+constexpr int kThreads = (kMmaWarp + 1) * 32;
+constexpr uint32_t kTmemCols = 256;
+constexpr uint64_t kTimeoutNs = 4000000000ull;
+
+struct Barriers {
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t accf[2];
+    uint64_t acce[2];
+    uint64_t done;
+    uint32_t tmem_base;
+};
+
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
+
+__device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
+    int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    ta = i;
+    tb = t - i * (i + 1) / 2;
+}
+
+// A converter lane owns 4 rows (4kq .. 4kq+3 of the stage) x 4 columns
+// (m0 .. m0+3 of the tile): one float4 per row on the load side, one 16-byte
+// K-chunk per column on the store side.  Lanes 8j..8j+7 take kq = 0..7 for
+// the same columns, so each 8-lane store phase hits 8 distinct 16-byte bank
+// groups of the swizzled tile.
+struct Frag {
+    float v[4][4];   // [row t][col u]
+    float s[4];      // row scales
+};
+
+__device__ __forceinline__ void load_frag(const float* __restrict__ F, int64_t ldF, int64_t k, int64_t r1,
+                                          const double* __restrict__ srow, int64_t i_base, int64_t col,
+                                          bool vec4, Frag& f) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int64_t i = i_base + t;
+        f.s[t] = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) f.v[t][u] = 0.f;
+        if (i < r1) {
+            f.s[t] = (float)srow[i];
+            const float* p = F + i * ldF + col;
+            if (vec4 && col + 3 < k) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+                f.v[t][0] = q.x;
+                f.v[t][1] = q.y;
+                f.v[t][2] = q.z;
+                f.v[t][3] = q.w;
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (col + u < k) f.v[t][u] = __ldg(p + u);
+            }
+        }
+    }
+}
+
+// Writes the fragment as 4 K-chunks (k = 4kq .. 4kq+3) of columns m0 .. m0+3
+// of the K-major hi / lo tiles.
+__device__ __forceinline__ void store_frag(const Frag& f, uint8_t* hi, uint8_t* lo, int m0, int kq) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        float h[4], l[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const float y = f.v[t][u] * f.s[t];
+            h[t] = tc::tf32_rn(y);
+            l[t] = tc::tf32_rn(y - h[t]);
+        }
+        const uint32_t off = tc::sw128_off((uint32_t)(m0 + u), (uint32_t)(4 * kq));
+        *reinterpret_cast<float4*>(hi + off) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(lo + off) = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// Converter step for stage s: prefetch stage s+1 into (na, nb), wait for the
+// ring slot, publish (ca, cb) as hi/lo operand tiles.
+__device__ __forceinline__ bool cvt_stage(int64_t s, int64_t n_stages, const float* __restrict__ F, int64_t ldF,
+                                          int64_t k, int64_t r0, int64_t r1, const double* __restrict__ srow,
+                                          int64_t a0, int64_t b0, int m0, int kq, int lane, int vec4, bool diag,
+                                          uint8_t* base, Barriers* bar, int* err, const Frag& ca, const Frag& cb,
+                                          Frag& na, Frag& nb) {
+    if (s + 1 < n_stages) {
+        const int64_t ib = r0 + (s + 1) * kTK + 4 * kq;
+        load_frag(F, ldF, k, r1, srow, ib, a0 + m0, vec4, na);
+        if (!diag) load_frag(F, ldF, k, r1, srow, ib, b0 + m0, vec4, nb);
+    }
+    const int slot = (int)(s % kStages);
+    const uint32_t use = (uint32_t)(s / kStages);
+    if (!tc::mbar_wait(&bar->empty[slot], (use & 1u) ^ 1u, kTimeoutNs)) {
+        atomicExch(err, 1);
+        return false;
+    }
+    uint8_t* st = base + (size_t)slot * kStageBytes;
+    store_frag(ca, st, st + kOpBytes, m0, kq);
+    if (!diag) store_frag(cb, st + 2 * kOpBytes, st + 3 * kOpBytes, m0, kq);
+    tc::fence_async_smem();
+    __syncwarp();
+    if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+gram_tc_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ srow,
+               int n_tiles, int64_t rows_per, int vec4, double* __restrict__ partial, int* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageBytes);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int64_t tix = blockIdx.x % n_tiles;
+    const int64_t split = blockIdx.x / n_tiles;
+    int64_t ta, tb;
+    tile_of(tix, ta, tb);
+    const bool diag = (ta == tb);
+    const int64_t a0 = ta * kTT, b0 = tb * kTT;
+    const int64_t r0 = split * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
+    const int64_t n_stages = (r1 > r0) ? (r1 - r0 + kTK - 1) / kTK : 0;
+    const int64_t n_chunks = (n_stages + kFlushStages - 1) / kFlushStages;
+    double* out = partial + (int64_t)blockIdx.x * kTT * kTT;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            tc::mbar_init(&bar->full[s], kCvtWarps);
+            tc::mbar_init(&bar->empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&bar->accf[b], 1);
+            tc::mbar_init(&bar->acce[b], kEpiWarps * 32);
+        }
+        tc::mbar_init(&bar->done, 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == kMmaWarp) {
+        tc::tmem_alloc(&bar->tmem_base, kTmemCols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tbase = bar->tmem_base;
+
+    if (warp >= kEpiWarps && warp < kMmaWarp) {
+        // ---------------- converters
+        const int cw = warp - kEpiWarps;
+        const int kq = lane & 7;                      // K chunk: stage rows 4kq .. 4kq+3
+        const int m0 = 16 * cw + 4 * (lane >> 3);     // tile columns m0 .. m0+3
+        Frag f0a, f0b, f1a, f1b;
+        if (n_stages > 0) {
+            const int64_t ib = r0 + 4 * kq;
+            load_frag(F, ldF, k, r1, srow, ib, a0 + m0, vec4, f0a);
+            if (!diag) load_frag(F, ldF, k, r1, srow, ib, b0 + m0, vec4, f0b);
+        }
+        for (int64_t s = 0; s < n_stages; s += 2) {
+            if (!cvt_stage(s, n_stages, F, ldF, k, r0, r1, srow, a0, b0, m0, kq, lane, vec4, diag, base, bar,
+                           err, f0a, f0b, f1a, f1b))
+                break;
+            if (s + 1 < n_stages &&
+                !cvt_stage(s + 1, n_stages, F, ldF, k, r0, r1, srow, a0, b0, m0, kq, lane, vec4, diag, base,
+                           bar, err, f1a, f1b, f0a, f0b))
+                break;
+        }
+    } else if (warp == kMmaWarp) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_tf32(kTT, kTT);
+            bool ok = true;
+            for (int64_t c = 0; c < n_chunks && ok; ++c) {
+                const int tb_ = (int)(c & 1);
+                const uint32_t tuse = (uint32_t)(c >> 1);
+                if (!tc::mbar_wait(&bar->acce[tb_], (tuse & 1u) ^ 1u, kTimeoutNs)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t d = tbase + (uint32_t)(tb_ * kTT);
+                const int64_t s0 = c * kFlushStages;
+                const int64_t s1 = min(n_stages, s0 + kFlushStages);
+                for (int64_t s = s0; s < s1; ++s) {
+                    const int slot = (int)(s % kStages);
+                    const uint32_t use = (uint32_t)(s / kStages);
+                    if (!tc::mbar_wait(&bar->full[slot], use & 1u, kTimeoutNs)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    uint8_t* st = base + (size_t)slot * kStageBytes;
+                    const uint32_t ahi = tc::smem_u32(st), alo = tc::smem_u32(st + kOpBytes);
+                    const uint32_t bhi = diag ? ahi : tc::smem_u32(st + 2 * kOpBytes);
+                    const uint32_t blo = diag ? alo : tc::smem_u32(st + 3 * kOpBytes);
+#pragma unroll
+                    for (int j = 0; j < kTK / 8; ++j) {
+                        const uint32_t koff = (uint32_t)(j * 32);   // 8 tf32 = 32 bytes
+                        const uint64_t dah = tc::desc_kmajor_sw128(ahi + koff);
+                        const uint64_t dal = tc::desc_kmajor_sw128(alo + koff);
+                        const uint64_t dbh = tc::desc_kmajor_sw128(bhi + koff);
+                        const uint64_t dbl = tc::desc_kmajor_sw128(blo + koff);
+                        tc::mma_tf32(d, dal, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
+                        tc::mma_tf32(d, dah, dbl, idesc, 1u);
+                        tc::mma_tf32(d, dal, dbh, idesc, 1u);
+                        tc::mma_tf32(d, dah, dbh, idesc, 1u);
+                    }
+                    tc::mma_commit(&bar->empty[slot]);
+                }
+                if (ok) tc::mma_commit(&bar->accf[tb_]);
+            }
+            if (!ok) atomicExch(err, 2);
+            // retire every issued MMA before the TMEM is released
+            tc::mma_commit(&bar->done);
+            if (!tc::mbar_wait(&bar->done, 0u, kTimeoutNs)) atomicExch(err, 3);
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: warp q owns tile rows 32q..32q+31; the FP64
+        // tile is stored column-major ([n][m]) so a warp's accesses coalesce
+        const int m = warp * 32 + lane;
+        double* orow = out + m;
+        for (int n = 0; n < kTT; ++n) orow[n * kTT] = 0.0;
+        for (int64_t c = 0; c < n_chunks; ++c) {
+            const int tb_ = (int)(c & 1);
+            const uint32_t use = (uint32_t)(c >> 1);
+            if (!tc::mbar_wait(&bar->accf[tb_], use & 1u, kTimeoutNs)) {
+                atomicExch(err, 4);
+                break;
+            }
+            tc::tc_fence_after();
+#pragma unroll 1
+            for (int cb = 0; cb < kTT / 32; ++cb) {
+                float v[32];
+                tc::tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tb_ * kTT + 32 * cb), v);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int n = 0; n < 32; ++n) orow[(32 * cb + n) * kTT] += (double)v[n];
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&bar->acce[tb_]);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == kMmaWarp) tc::tmem_dealloc(tbase, kTmemCols);
+}
+
+// Sum the row-split partial tiles and write the full symmetric k x k matrix
+// (column-major).
+__global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_tiles, int n_split, int64_t k,
+                                      double* __restrict__ G) {
+    const int64_t t = blockIdx.x;
+    int64_t ta, tb;
+    tile_of(t, ta, tb);
+    for (int e = threadIdx.x; e < kTT * kTT; e += blockDim.x) {
+        const int ib = e / kTT, ia = e - ib * kTT;   // partial tiles are [n][m]
+        const int64_t ga = ta * kTT + ia, gb = tb * kTT + ib;
+        if (ga >= k || gb >= k) continue;
+        double s = 0.0;
+        for (int p = 0; p < n_split; ++p) s += partial[((int64_t)p * n_tiles + t) * kTT * kTT + e];
+        G[gb * k + ga] = s;
+        G[ga * k + gb] = s;
+    }
+}
+
+}  // namespace
+
+// G (k x k, column-major, full) = F^T diag(s)^2 F for an FP32 factor.
+int run_gram_tc(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, const double* s, double* G,
+                cudaStream_t st) {
+    const int nt = ceil_div(k, kTT);
+    const int n_tiles = nt * (nt + 1) / 2;
+    int n_split = std::max(1, ctx->num_sms / n_tiles);
+    n_split = (int)std::min<int64_t>(n_split, std::max<int64_t>(1, N / 4096));
+    const int64_t rows_per = ((N + n_split - 1) / n_split + kTK - 1) / kTK * kTK;
+    int rc = KEVD_OK;
+    double* partial = arena_get<double>(ctx, "tc.gpart", (size_t)n_split * n_tiles * kTT * kTT, &rc);
+    int* err = arena_get<int>(ctx, "tc.err", 1, &rc);
+    if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
+    KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kSmemBytes));
+    const int vec4 = ((ldF % 4) == 0 && ((uintptr_t)F % 16) == 0) ? 1 : 0;
+    {
+        ProfScope ps(ctx, "gram_tc", st);
+        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(F, ldF, N, k, s, n_tiles, rows_per, vec4,
+                                                                       partial, err);
+        KEVD_LAUNCH(ctx);
+    }
+    gram_tc_reduce_kernel<<<n_tiles, 256, 0, st>>>(partial, n_tiles, n_split, k, G);
+    KEVD_LAUNCH(ctx);
+    int herr = 0;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(st));
+    if (herr != 0) return set_error(ctx, KEVD_ERR_TIMEOUT, "gram_tc: pipeline wait timed out (code %d)", herr);
+    return KEVD_OK;
+}
+
+}  // namespace kevd

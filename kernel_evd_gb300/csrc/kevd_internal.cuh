@@ -169,6 +169,8 @@ int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
 int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k,
                          int64_t ldF, int k_out, double* lam, float* U, kevd_evd_info* info,
                          kevd_evd_dump* dump, cudaStream_t s);
+int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
+                      const double* s_dev, double* G, cudaStream_t st);
 int run_gather_rows(kevd_ctx* ctx, const void* F, int precision, int64_t ldF, const int64_t* idx,
                     int64_t n, int64_t ncols, double* out, cudaStream_t s);
 

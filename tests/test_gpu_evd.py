@@ -45,11 +45,15 @@ def test_mixed_evd_close_to_fp64(ctx, fac):
     X, r = fac
     F = torch.from_numpy(r["F"].astype(np.float32)).cuda()
     g = api.bistochastic_evd(ctx, F, k_out=16)
-    e = evd.evd_from_factor(r["F"], 16)
-    assert abs(g.lam[-1] - 1.0) < 1e-6
-    np.testing.assert_allclose(g.lam[-16:], e["lam"][-16:], rtol=0, atol=1e-6)
+    e = evd.evd_from_factor(r["F"].astype(np.float32).astype(np.float64), 16)
+    # the leading eigenpairs of the FP32 factor are Rayleigh-Ritz refined in FP64:
+    # eigenvalue error <= 1e-8 against the FP64 EVD of the same factor
+    assert abs(g.lam[-1] - 1.0) < 1e-8
+    np.testing.assert_allclose(g.lam[-16:], e["lam"][-16:], rtol=0, atol=1e-8)
     ang = evd.eigvec_angles(g.U.cpu().numpy()[:, -4:], e["U"][:, -4:])
-    assert np.all(ang < 1e-3)
+    assert np.all(ang < 1e-4)
+    # the rest of the spectrum comes from the 4xTF32 Gram path
+    np.testing.assert_allclose(g.lam[:-16], e["lam"][:-16], rtol=0, atol=1e-4)
 
 
 def test_factor_from_linv_roundtrip(ctx, fac):

@@ -1,0 +1,41 @@
+"""Weighted Gram G = F^T diag(s)^2 F: the FP32 factor on the tcgen05 tensor cores
+(3xTF32, FP64 across row chunks) and the FP64 factor on the FP64 path, against
+NumPy FP64 on the same inputs."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref(F, s):
+    Y = F.astype(np.float64) * s[:, None]
+    return Y.T @ Y
+
+
+@pytest.mark.parametrize("N,k,ld", [(5000, 300, 300), (4097, 128, 128), (100, 2, 2), (9000, 257, 257),
+                                    (7000, 250, 256), (33, 129, 132), (20000, 130, 130)])
+def test_gram_tc_fp32_factor(ctx, N, k, ld):
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(N + k)
+    Fb = rng.standard_normal((N, ld)).astype(np.float32)
+    Fb[:, : k // 3] = np.abs(Fb[:, : k // 3]) + 0.5     # some columns with a large mean, like a kernel factor
+    s = rng.uniform(0.5, 2.0, N)
+    G = api.weighted_gram(ctx, torch.from_numpy(Fb).cuda()[:, :k] if ld != k else torch.from_numpy(Fb).cuda(),
+                          torch.from_numpy(s).cuda(), k=k).cpu().numpy()
+    R = _ref(Fb[:, :k], s)
+    scale = np.sqrt(np.outer(np.diag(R), np.diag(R)))
+    err = np.abs(G - R) / scale
+    # 4xTF32 products are exact; the tensor-core FP32 accumulator over 1024-row
+    # chunks limits the relative error (FP64 across chunks)
+    assert err.max() < 3e-5, err.max()
+    np.testing.assert_allclose(G, G.T, rtol=0, atol=0)
+
+
+def test_gram_fp64_factor(ctx):
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(3)
+    F = rng.standard_normal((3000, 170))
+    s = rng.uniform(0.5, 2.0, 3000)
+    G = api.weighted_gram(ctx, torch.from_numpy(F).cuda(), torch.from_numpy(s).cuda()).cpu().numpy()
+    np.testing.assert_allclose(G, _ref(F, s), rtol=1e-12, atol=1e-10)
