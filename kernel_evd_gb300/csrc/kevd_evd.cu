@@ -351,7 +351,8 @@ __global__ void __launch_bounds__(256)
 rr_hm_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ T1, int m,
              const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
     __shared__ float Fs[64][33];
-    __shared__ float Ts[32][33];
+    __shared__ float Ts[32][33];   // T1 = Ts + Tl: the hi/lo FP32 pair keeps T1 to ~2^-48
+    __shared__ float Tl[32][33];
     __shared__ float Ws[64][33];
     __shared__ float Us[64][33];
     const int tid = threadIdx.x;
@@ -374,17 +375,21 @@ rr_hm_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const d
             for (int e = tid; e < 32 * 32; e += 256) {
                 const int cc = e >> 5, jj = e & 31;
                 const int64_t c = c0 + cc;
-                Ts[cc][jj] = (c < k && jj < m) ? (float)T1[c * m + jj] : 0.f;
+                const double t = (c < k && jj < m) ? T1[c * m + jj] : 0.0;
+                const float th = (float)t;
+                Ts[cc][jj] = th;
+                Tl[cc][jj] = (float)(t - (double)th);
             }
             __syncthreads();
 #pragma unroll 8
             for (int cc = 0; cc < 32; ++cc) {
                 const float t0 = Ts[cc][wj], t1 = Ts[cc][wj + 1];
+                const float l0 = Tl[cc][wj], l1 = Tl[cc][wj + 1];
 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
                     const float f = Fs[wr + a][cc];
-                    w[a][0] = fmaf(f, t0, w[a][0]);
-                    w[a][1] = fmaf(f, t1, w[a][1]);
+                    w[a][0] = fmaf(f, t0, fmaf(f, l0, w[a][0]));
+                    w[a][1] = fmaf(f, t1, fmaf(f, l1, w[a][1]));
                 }
             }
         }
