@@ -28,6 +28,11 @@
 
 namespace kevd {
 
+bool update_tc_supported(const float* F, int64_t ldF, int d, int b);
+int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_max, const float* X, int d,
+                     double scale, const int64_t* sacc, const float* minv_f, int b, const void* round_state,
+                     double* dvec, double* dblk, int* err, cudaStream_t s);
+
 constexpr int kRowBlock = 128;   // rows per update CTA (= rows per d partial sum)
 constexpr int kMaxBlock = 64;    // proposals per round supported by the SIMT update
 constexpr int kColChunk = 32;    // F columns per hgram CTA
@@ -535,6 +540,11 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     KEVD_CUDA(ctx, cudaFuncSetAttribute(rp_update_kernel<T>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usm));
     int* done_h = static_cast<int*>(ctx->pinned);
+    // FP32 factors take the tensor-core residual update when the layout allows TMA
+    const bool use_tc = sizeof(T) == 4 && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d, b);
+    int* tc_err = arena_get<int>(ctx, "rp.tcerr", 1, &st);
+    if (st != KEVD_OK) return st;
+    KEVD_CUDA(ctx, cudaMemsetAsync(tc_err, 0, sizeof(int), s));
     int round = 0;
     for (; round < p->max_rounds; ++round) {
         {
@@ -556,7 +566,10 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                                                  p->k_max, props, rs, minv, minv_f, sacc, piv, hm);
             KEVD_LAUNCH(ctx);
         }
-        {
+        if (use_tc) {
+            KEVD_TRY(launch_update_tc(ctx, reinterpret_cast<float*>(F), ldF, N, p->k_max, X, d, scale, sacc,
+                                      minv_f, b, rs, dvec, dblk, tc_err, s));
+        } else {
             ProfScope ps(ctx, "rp_update", s);
             rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv,
                                                            minv_f, b, rs, dvec, dblk);
@@ -574,8 +587,12 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                                                   std::min(round, p->max_rounds), p->err_target, err);
     KEVD_LAUNCH(ctx);
     RoundState hs;
+    int herr = 0;
     KEVD_CUDA(ctx, cudaMemcpyAsync(&hs, rs, sizeof(RoundState), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(&herr, tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (herr != 0)
+        return set_error(ctx, KEVD_ERR_TIMEOUT, "rpchol: tensor-core update pipeline timed out (code %d)", herr);
     if (hs.rank > 0 && piv_h)
         KEVD_CUDA(ctx, cudaMemcpy(piv_h, piv, hs.rank * sizeof(int64_t), cudaMemcpyDeviceToHost));
     if (err_h) KEVD_CUDA(ctx, cudaMemcpy(err_h, err, hs.rounds * sizeof(double), cudaMemcpyDeviceToHost));

@@ -1,0 +1,413 @@
+// Residual update of one block-RPCholesky round for an FP32 factor, on the
+// tcgen05 tensor cores (the row-block loop of ks_arpclm.cu:933-995 with the
+// factor stored):
+//
+//   for every 128-row block R:
+//     P = F(R, 0:r) F(S_i, 0:r)^T                    tcgen05, 3xTF32
+//     T = K(R, S_i) - P                               FP32, direct distances
+//     G = T L_i^{-T};  F(R, r:r+nacc) = G
+//     d(R) <- max(d(R) - rowsq(G), 0)  (FP64);  block sum of d for the sampler
+//
+// Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
+// lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
+// stage accumulates hi_a hi_b + hi_a lo_b + lo_a hi_b in a fresh TMEM partial
+// (12 MMA updates), and the epilogue sums the stage partials in FP32 registers
+// with round-to-nearest, so the tensor-core accumulator's rounding bias never
+// builds up over r.
+//
+// CTA (320 threads, persistent over row blocks):
+//   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
+//              and the pre-split S_i tiles (bulk copy)
+//   warp 1     TMEM allocation and the single MMA-issuing thread
+//   warps 2,3,8,9  converters: in-place hi / separate lo of the F tile, columns
+//              >= r zeroed
+//   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
+// Ring of 3 shared-memory stages and 4 TMEM partial buffers of 64 columns,
+// handed over with mbarriers; every wait is bounded (error flag on timeout).
+#include "kevd_internal.cuh"
+#include "kevd_tc.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
+namespace kevd {
+
+namespace {
+
+constexpr int kRows = 128;          // rows per block (MMA M)
+constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
+constexpr int kKs = 32;             // F columns per stage
+constexpr int kStages = 3;
+constexpr int kBufs = 4;            // TMEM partial buffers
+constexpr int kAOp = kRows * kKs * 4;     // 16 KB
+constexpr int kBOp = kCols * kKs * 4;     // 8 KB
+constexpr int kStageBytes = 2 * kAOp + 2 * kBOp;   // a_hi, a_lo, b_hi, b_lo
+constexpr int kThreads = 320;
+constexpr uint64_t kTimeoutNs = 4000000000ull;
+constexpr int kMaxD = 128;
+
+struct Bars {
+    uint64_t tma_full[kStages];
+    uint64_t cvt_full[kStages];
+    uint64_t empty[kStages];
+    uint64_t accf[kBufs];
+    uint64_t acce[kBufs];
+    uint64_t done;
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || w == 8 || w == 9; }
+__device__ __forceinline__ int cvt_index(int w) { return w < 4 ? w - 2 : w - 6; }
+
+struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
+    int64_t rank;
+    int64_t r_old;
+    int32_t nacc;
+    int32_t done;
+    int32_t rounds;
+    int32_t pad;
+    double total;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F, int64_t ldF, int64_t N,
+                 const float* __restrict__ X, int d, float scale, const int64_t* __restrict__ sacc,
+                 const float* __restrict__ minv_f, int b, const uint8_t* __restrict__ bprep,
+                 const RoundView* st, double* __restrict__ dvec, double* __restrict__ dblk,
+                 int* __restrict__ err) {
+    if (st->done) return;
+    const int nacc = st->nacc;
+    if (nacc == 0) return;
+    const int64_t r = st->r_old;
+    const int n_st = (int)((r + kKs - 1) / kKs);
+    const int64_t nblk = (N + kRows - 1) / kRows;
+
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float* xs = reinterpret_cast<float*>(base + (size_t)kStages * kStageBytes);   // kCols x d
+    float* mv = xs + kCols * d;                                                    // kCols x kCols
+    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // pivot rows and L_i^{-1} (FP32) for the epilogue
+    for (int e = threadIdx.x; e < kCols * d; e += kThreads) {
+        const int q = e / d, kk = e - q * d;
+        xs[e] = (q < nacc) ? X[sacc[q] * d + kk] : 0.f;
+    }
+    for (int e = threadIdx.x; e < kCols * kCols; e += kThreads) {
+        const int a = e / kCols, q = e - a * kCols;
+        mv[e] = (a < nacc && q < nacc) ? minv_f[a * b + q] : 0.f;
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            tc::mbar_init(&bar->tma_full[s], 1);
+            tc::mbar_init(&bar->cvt_full[s], 4);
+            tc::mbar_init(&bar->empty[s], 1);
+        }
+        for (int t = 0; t < kBufs; ++t) {
+            tc::mbar_init(&bar->accf[t], 1);
+            tc::mbar_init(&bar->acce[t], 128);
+        }
+        tc::mbar_init(&bar->done, 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(&bar->tmem_base, kBufs * kCols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tbase = bar->tmem_base;
+
+    if (warp == 0) {
+        // ---------------- TMA producer
+        if (lane == 0) {
+            int64_t g = 0;
+            bool ok = true;
+            for (int64_t rb = blockIdx.x; rb < nblk && ok; rb += gridDim.x) {
+                for (int s = 0; s < n_st; ++s, ++g) {
+                    const int slot = (int)(g % kStages);
+                    const uint32_t use = (uint32_t)(g / kStages);
+                    if (!tc::mbar_wait(&bar->empty[slot], (use & 1u) ^ 1u, kTimeoutNs)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* stg = base + (size_t)slot * kStageBytes;
+                    tc::mbar_arrive_expect_tx(&bar->tma_full[slot], kAOp + 2 * kBOp);
+                    tc::tma_load_2d(stg, &tmap, s * kKs, (int)(rb * kRows), &bar->tma_full[slot]);
+                    tc::bulk_load(stg + 2 * kAOp, bprep + (size_t)s * 2 * kBOp, 2 * kBOp, &bar->tma_full[slot]);
+                }
+            }
+            if (!ok) atomicExch(err, 11);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
+            int64_t g = 0;
+            bool ok = true;
+            for (int64_t rb = blockIdx.x; rb < nblk && ok; rb += gridDim.x) {
+                for (int s = 0; s < n_st; ++s, ++g) {
+                    const int slot = (int)(g % kStages);
+                    const uint32_t use = (uint32_t)(g / kStages);
+                    const int tb = (int)(g % kBufs);
+                    const uint32_t tuse = (uint32_t)(g / kBufs);
+                    if (!tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs) ||
+                        !tc::mbar_wait(&bar->cvt_full[slot], use & 1u, kTimeoutNs)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    uint8_t* stg = base + (size_t)slot * kStageBytes;
+                    const uint32_t ahi = tc::smem_u32(stg), alo = tc::smem_u32(stg + kAOp);
+                    const uint32_t bhi = tc::smem_u32(stg + 2 * kAOp), blo = tc::smem_u32(stg + 2 * kAOp + kBOp);
+                    const uint32_t dt = tbase + (uint32_t)(tb * kCols);
+#pragma unroll
+                    for (int j = 0; j < kKs / 8; ++j) {
+                        const uint32_t ko = (uint32_t)(j * 32);
+                        const uint64_t dah = tc::desc_kmajor_sw128(ahi + ko);
+                        const uint64_t dal = tc::desc_kmajor_sw128(alo + ko);
+                        const uint64_t dbh = tc::desc_kmajor_sw128(bhi + ko);
+                        const uint64_t dbl = tc::desc_kmajor_sw128(blo + ko);
+                        tc::mma_tf32(dt, dal, dbh, idesc, j > 0 ? 1u : 0u);
+                        tc::mma_tf32(dt, dah, dbl, idesc, 1u);
+                        tc::mma_tf32(dt, dah, dbh, idesc, 1u);
+                    }
+                    tc::mma_commit(&bar->empty[slot]);
+                    tc::mma_commit(&bar->accf[tb]);
+                }
+            }
+            if (!ok) atomicExch(err, 12);
+            tc::mma_commit(&bar->done);
+            if (!tc::mbar_wait(&bar->done, 0u, kTimeoutNs)) atomicExch(err, 13);
+        }
+        __syncwarp();
+    } else if (is_cvt_warp(warp)) {
+        // ---------------- converters: 128 threads, 8 float4 each per stage
+        const int ct = cvt_index(warp) * 32 + lane;
+        int64_t g = 0;
+        for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
+            bool ok = true;
+            for (int s = 0; s < n_st; ++s, ++g) {
+                const int slot = (int)(g % kStages);
+                const uint32_t use = (uint32_t)(g / kStages);
+                if (!tc::mbar_wait(&bar->tma_full[slot], use & 1u, kTimeoutNs)) {
+                    atomicExch(err, 14);
+                    ok = false;
+                    break;
+                }
+                uint8_t* stg = base + (size_t)slot * kStageBytes;
+                const int64_t cbase = (int64_t)s * kKs;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;   // 16-byte chunk
+                    const uint32_t row = off >> 7;
+                    const uint32_t chunk = ((off >> 4) & 7u) ^ (row & 7u);  // logical K chunk
+                    float4 a = *reinterpret_cast<float4*>(stg + off);
+                    float v[4] = {a.x, a.y, a.z, a.w};
+                    float h[4], l[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int64_t col = cbase + 4 * chunk + u;
+                        const float x = (col < r) ? v[u] : 0.f;
+                        h[u] = tc::tf32_rn(x);
+                        l[u] = tc::tf32_rn(x - h[u]);
+                    }
+                    *reinterpret_cast<float4*>(stg + off) = make_float4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<float4*>(stg + kAOp + off) = make_float4(l[0], l[1], l[2], l[3]);
+                }
+                tc::fence_async_smem();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&bar->cvt_full[slot]);
+            }
+            if (!ok) break;
+        }
+    } else {
+        // ---------------- epilogue: warps 4..7, TMEM lane quarter q = warp - 4.
+        // After a timed-out wait the warp stops waiting but keeps walking the
+        // row blocks, so all four warps meet the same named barriers.
+        const int q = warp - 4;
+        const int rloc = 32 * q + lane;
+        int64_t g = 0;
+        bool ok = true;
+        const float nscale = -scale;
+        __shared__ double wsum[4];
+        for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
+            float acc[kCols];
+#pragma unroll
+            for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
+            for (int s = 0; s < n_st; ++s, ++g) {
+                if (!ok) continue;
+                const int tb = (int)(g % kBufs);
+                const uint32_t use = (uint32_t)(g / kBufs);
+                if (!tc::mbar_wait(&bar->accf[tb], use & 1u, kTimeoutNs)) {
+                    atomicExch(err, 15);
+                    ok = false;
+                    continue;
+                }
+                tc::tc_fence_after();
+                float v[32];
+                const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kCols);
+                tc::tmem_ld32(ta, v);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) acc[j] += v[j];
+                tc::tmem_ld32(ta + 32, v);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int j = 0; j < 32; ++j) acc[32 + j] += v[j];
+                tc::tc_fence_before();
+                tc::mbar_arrive(&bar->acce[tb]);
+            }
+            const int64_t i = rb * kRows + rloc;
+            double nd = 0.0;
+            if (ok && i < N) {
+                // T = K(i, S_i) - P, direct FP32 distances
+                const float* xi = X + i * d;
+#pragma unroll
+                for (int c = 0; c < kCols; ++c) {
+                    if (c < nacc) {
+                        float dd = 0.f;
+                        const float* xq = xs + c * d;
+                        for (int kk = 0; kk < d; ++kk) {
+                            const float t = __ldg(xi + kk) - xq[kk];
+                            dd = fmaf(t, t, dd);
+                        }
+                        acc[c] = expf(nscale * dd) - acc[c];
+                    }
+                }
+                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc)
+                float sq = 0.f;
+                float* frow = F + i * ldF + r;
+                for (int a = 0; a < nacc; ++a) {
+                    float gsum = 0.f;
+                    const float* ma = mv + a * kCols;
+#pragma unroll
+                    for (int e = 0; e < kCols; ++e) gsum = fmaf(acc[e], ma[e], gsum);
+                    frow[a] = gsum;
+                    sq = fmaf(gsum, gsum, sq);
+                }
+                nd = fmax(dvec[i] - (double)sq, 0.0);
+                dvec[i] = nd;
+            } else if (i < N) {
+                nd = dvec[i];
+            }
+            // block sum of the new d over the 128 epilogue threads
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+            if (lane == 0) wsum[q] = nd;
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (rloc == 0) dblk[rb] = (wsum[0] + wsum[1]) + (wsum[2] + wsum[3]);
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 1) tc::tmem_dealloc(tbase, kBufs * kCols);
+}
+
+// Split the accepted rows F(S_i, 0:r) into pre-swizzled hi / lo tiles:
+// stage s -> [hi: 64 rows x 32 cols][lo], K-major SW128 (rows >= nacc and
+// columns >= r are zero).
+__global__ void update_prep_kernel(const float* __restrict__ F, int64_t ldF, const int64_t* __restrict__ sacc,
+                                   const RoundView* st, int n_stages_max, uint8_t* __restrict__ bprep) {
+    if (st->done || st->nacc == 0) return;
+    const int nacc = st->nacc;
+    const int64_t r = st->r_old;
+    const int n_st = (int)((r + kKs - 1) / kKs);
+    const int64_t total = (int64_t)n_st * kCols * kKs;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(e / (kCols * kKs));
+        const int rem = (int)(e - (int64_t)s * kCols * kKs);
+        const int qrow = rem / kKs, kk = rem - qrow * kKs;
+        const int64_t c = (int64_t)s * kKs + kk;
+        const float v = (qrow < nacc && c < r) ? F[sacc[qrow] * ldF + c] : 0.f;
+        const float h = tc::tf32_rn(v), l = tc::tf32_rn(v - h);
+        uint8_t* t = bprep + (size_t)s * 2 * kBOp;
+        const uint32_t off = tc::sw128_off((uint32_t)qrow, (uint32_t)kk);
+        *reinterpret_cast<float*>(t + off) = h;
+        *reinterpret_cast<float*>(t + kBOp + off) = l;
+    }
+    (void)n_stages_max;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+}  // namespace
+
+constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + (size_t)kCols * kMaxD * 4 + kCols * kCols * 4 +
+                            sizeof(Bars) + 1024;
+
+// Whether the tensor-core update can run for this factor layout.
+bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
+    return get_encode() != nullptr && (ldF % 4) == 0 && ((uintptr_t)F % 16) == 0 && d <= kMaxD && b <= kCols &&
+           ldF * 4 < (1ll << 40);
+}
+
+// Enqueue one round's residual update (reads nacc / r_old from the device
+// round state).  k_max bounds the number of stages of the pre-split buffer.
+int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_max, const float* X, int d,
+                     double scale, const int64_t* sacc, const float* minv_f, int b, const void* round_state,
+                     double* dvec, double* dblk, int* err, cudaStream_t s) {
+    static thread_local const void* last_F = nullptr;
+    static thread_local int64_t last_ld = -1, last_N = -1;
+    static thread_local CUtensorMap tmap;
+    if (F != last_F || ldF != last_ld || N != last_N) {
+        PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode();
+        if (!enc) return set_error(ctx, KEVD_ERR_CUDA, "update_tc: cuTensorMapEncodeTiled unavailable");
+        const cuuint64_t gdim[2] = {(cuuint64_t)ldF, (cuuint64_t)N};
+        const cuuint64_t gstride[1] = {(cuuint64_t)ldF * 4};
+        const cuuint32_t box[2] = {(cuuint32_t)kKs, (cuuint32_t)kRows};
+        const cuuint32_t estr[2] = {1, 1};
+        CUresult cr = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)F, gdim, gstride, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS) return set_error(ctx, KEVD_ERR_CUDA, "update_tc: tensor map encode failed (%d)", (int)cr);
+        last_F = F;
+        last_ld = ldF;
+        last_N = N;
+    }
+    const int n_stages_max = (int)((k_max + kKs - 1) / kKs);
+    int rc = KEVD_OK;
+    uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
+    if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
+    const RoundView* rv = static_cast<const RoundView*>(round_state);
+    {
+        ProfScope ps(ctx, "rp_update_prep", s);
+        update_prep_kernel<<<std::max(1, std::min(n_stages_max * 8, ctx->num_sms * 4)), 256, 0, s>>>(
+            F, ldF, sacc, rv, n_stages_max, bprep);
+        KEVD_LAUNCH(ctx);
+    }
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kUpdSmem));
+    const int64_t nblk = (N + kRows - 1) / kRows;
+    const int grid = (int)std::min<int64_t>(nblk, ctx->num_sms);
+    {
+        ProfScope ps(ctx, "rp_update", s);
+        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, F, ldF, N, X, d, (float)scale, sacc, minv_f, b,
+                                                          bprep, rv, dvec, dblk, err);
+        KEVD_LAUNCH(ctx);
+    }
+    return KEVD_OK;
+}
+
+}  // namespace kevd

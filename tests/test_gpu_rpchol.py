@@ -81,6 +81,20 @@ def test_mixed_trace_error_close_to_fp64(ctx, states):
     assert abs(direct - g.trace_error) <= 1e-5 * max(1.0, g.trace_error)
 
 
+@pytest.mark.parametrize("N,b", [(5000, 64), (3001, 17), (640, 1)])
+def test_mixed_factor_columns_match_oracle(ctx, states, N, b):
+    """With the same draws, the FP32 factor (tensor-core residual update) agrees
+    with the FP64 oracle column by column while the pivot sequences agree."""
+    X = states[:N]
+    k = 3 * b if b > 1 else 40
+    ref = rpchol.rpcholesky(X.astype(np.float64), SCALE, k, b, seed=77)
+    g = _gpu(ctx, X, k_max=k, block=b, seed=77, precision="mixed")
+    same = int(np.argmax(g.piv != ref["piv"])) if np.any(g.piv != ref["piv"]) else min(g.rank, ref["piv"].size)
+    assert same >= min(k, 2 * b)
+    F = g.factor.double().cpu().numpy()[:, :same]
+    np.testing.assert_allclose(F, ref["F"][:, :same], rtol=0, atol=2e-5)
+
+
 def test_linv_matches_oracle(ctx, states):
     from kernel_evd_gb300 import api
     X = states[:2000]
