@@ -4,7 +4,7 @@
 //
 //   for every 128-row block R:
 //     P = F(R, 0:r) F(S_i, 0:r)^T                    tcgen05, 3xTF32
-//     T = K(R, S_i) - P                               FP32, direct distances
+//     T = K(R, S_i) - P      (K(:, S_i) by update_kcols_kernel, FP32 direct distances)
 //     G = T L_i^{-T};  F(R, r:r+nacc) = G
 //     d(R) <- max(d(R) - rowsq(G), 0)  (FP64);  block sum of d for the sampler
 //
@@ -22,7 +22,7 @@
 //   warps 2,3,8,9  converters: in-place hi / separate lo of the F tile, columns
 //              >= r zeroed
 //   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
-// Ring of 3 shared-memory stages and 4 TMEM partial buffers of 64 columns,
+// Ring of 3 shared-memory stages and 8 TMEM partial buffers of 64 columns,
 // handed over with mbarriers; every wait is bounded (error flag on timeout).
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
@@ -40,7 +40,7 @@ constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
 constexpr int kStages = 3;
-constexpr int kBufs = 4;            // TMEM partial buffers
+constexpr int kBufs = 8;            // TMEM partial buffers (8 x 64 = all 512 columns)
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
 constexpr int kStageBytes = 2 * kAOp + 2 * kBOp;   // a_hi, a_lo, b_hi, b_lo
@@ -73,10 +73,9 @@ struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
 
 __global__ void __launch_bounds__(kThreads, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F, int64_t ldF, int64_t N,
-                 const float* __restrict__ X, int d, float scale, const int64_t* __restrict__ sacc,
-                 const float* __restrict__ minv_f, int b, const uint8_t* __restrict__ bprep,
-                 const RoundView* st, double* __restrict__ dvec, double* __restrict__ dblk,
-                 int* __restrict__ err) {
+                 const float* __restrict__ Kc, const float* __restrict__ minv_f, int b,
+                 const uint8_t* __restrict__ bprep, const RoundView* st, double* __restrict__ dvec,
+                 double* __restrict__ dblk, int* __restrict__ err) {
     if (st->done) return;
     const int nacc = st->nacc;
     if (nacc == 0) return;
@@ -86,16 +85,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float* xs = reinterpret_cast<float*>(base + (size_t)kStages * kStageBytes);   // kCols x d
-    float* mv = xs + kCols * d;                                                    // kCols x kCols
+    float* mv = reinterpret_cast<float*>(base + (size_t)kStages * kStageBytes);   // kCols x kCols
     Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // pivot rows and L_i^{-1} (FP32) for the epilogue
-    for (int e = threadIdx.x; e < kCols * d; e += kThreads) {
-        const int q = e / d, kk = e - q * d;
-        xs[e] = (q < nacc) ? X[sacc[q] * d + kk] : 0.f;
-    }
+    // L_i^{-1} (FP32) for the epilogue
     for (int e = threadIdx.x; e < kCols * kCols; e += kThreads) {
         const int a = e / kCols, q = e - a * kCols;
         mv[e] = (a < nacc && q < nacc) ? minv_f[a * b + q] : 0.f;
@@ -234,7 +228,6 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
         const int rloc = 32 * q + lane;
         int64_t g = 0;
         bool ok = true;
-        const float nscale = -scale;
         __shared__ double wsum[4];
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
             float acc[kCols];
@@ -266,30 +259,29 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
             const int64_t i = rb * kRows + rloc;
             double nd = 0.0;
             if (ok && i < N) {
-                // T = K(i, S_i) - P, direct FP32 distances
-                const float* xi = X + i * d;
+                // T = K(i, S_i) - P  (K(:, S_i) precomputed by update_kcols_kernel)
+                const float4* kr = reinterpret_cast<const float4*>(Kc + i * kCols);
 #pragma unroll
-                for (int c = 0; c < kCols; ++c) {
-                    if (c < nacc) {
-                        float dd = 0.f;
-                        const float* xq = xs + c * d;
-                        for (int kk = 0; kk < d; ++kk) {
-                            const float t = __ldg(xi + kk) - xq[kk];
-                            dd = fmaf(t, t, dd);
-                        }
-                        acc[c] = expf(nscale * dd) - acc[c];
-                    }
+                for (int c4 = 0; c4 < kCols / 4; ++c4) {
+                    const float4 kv = __ldg(kr + c4);
+                    acc[4 * c4 + 0] = kv.x - acc[4 * c4 + 0];
+                    acc[4 * c4 + 1] = kv.y - acc[4 * c4 + 1];
+                    acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
+                    acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
                 }
                 // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc)
                 float sq = 0.f;
                 float* frow = F + i * ldF + r;
-                for (int a = 0; a < nacc; ++a) {
-                    float gsum = 0.f;
-                    const float* ma = mv + a * kCols;
 #pragma unroll
-                    for (int e = 0; e < kCols; ++e) gsum = fmaf(acc[e], ma[e], gsum);
-                    frow[a] = gsum;
-                    sq = fmaf(gsum, gsum, sq);
+                for (int a = 0; a < kCols; ++a) {
+                    if (a < nacc) {
+                        float gsum = 0.f;
+                        const float* ma = mv + a * kCols;
+#pragma unroll
+                        for (int e = 0; e <= a; ++e) gsum = fmaf(acc[e], ma[e], gsum);
+                        frow[a] = gsum;
+                        sq = fmaf(gsum, gsum, sq);
+                    }
                 }
                 nd = fmax(dvec[i] - (double)sq, 0.0);
                 dvec[i] = nd;
@@ -309,6 +301,61 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
     __syncthreads();
     tc::tc_fence_after();
     if (warp == 1) tc::tmem_dealloc(tbase, kBufs * kCols);
+}
+
+// K(:, S_i) for the round, FP32 from direct differences: Kc[i][c], 64 columns
+// per row (zero beyond nacc).  CTA = 128 rows x 64 pivots; thread (ty, tx) of
+// 16 x 16 computes rows ty + 16a (a < 8) and columns tx + 16b (b < 4).
+__global__ void __launch_bounds__(256)
+update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, const int64_t* __restrict__ sacc,
+                    const RoundView* st, float* __restrict__ Kc) {
+    if (st->done || st->nacc == 0) return;
+    const int nacc = st->nacc;
+    extern __shared__ float ksm[];
+    const int dp = d + 1;
+    float* xr = ksm;                 // 128 x dp
+    float* xq = ksm + kRows * dp;    // 64 x dp
+    const int64_t row0 = (int64_t)blockIdx.x * kRows;
+    for (int e = threadIdx.x; e < kRows * d; e += 256) {
+        const int rr = e / d, kk = e - rr * d;
+        const int64_t i = row0 + rr;
+        xr[rr * dp + kk] = (i < N) ? X[i * d + kk] : 0.f;
+    }
+    for (int e = threadIdx.x; e < kCols * d; e += 256) {
+        const int q = e / d, kk = e - q * d;
+        xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + kk] : 0.f;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[a][c] = 0.f;
+    for (int kk = 0; kk < d; ++kk) {
+        float vr[8], vq[4];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float t = vr[a] - vq[c];
+                acc[a][c] = fmaf(t, t, acc[a][c]);
+            }
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const int64_t i = row0 + ty + 16 * a;
+        if (i >= N) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int col = tx + 16 * c;
+            Kc[i * kCols + col] = (col < nacc) ? expf(-scale * acc[a][c]) : 0.f;
+        }
+    }
 }
 
 // Split the accepted rows F(S_i, 0:r) into pre-swizzled hi / lo tiles:
@@ -354,8 +401,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + (size_t)kCols * kMaxD * 4 + kCols * kCols * 4 +
-                            sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + kCols * kCols * 4 + sizeof(Bars) + 1024;
 
 // Whether the tensor-core update can run for this factor layout.
 bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
@@ -391,6 +437,16 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
     const RoundView* rv = static_cast<const RoundView*>(round_state);
+    float* Kc = arena_get<float>(ctx, "utc.kc", (size_t)N * kCols, &rc);
+    if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
+    {
+        ProfScope ps(ctx, "rp_update_kcols", s);
+        const size_t ksm = (size_t)(kRows + kCols) * (d + 1) * sizeof(float);
+        KEVD_CUDA(ctx, cudaFuncSetAttribute(update_kcols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)ksm));
+        update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
+        KEVD_LAUNCH(ctx);
+    }
     {
         ProfScope ps(ctx, "rp_update_prep", s);
         update_prep_kernel<<<std::max(1, std::min(n_stages_max * 8, ctx->num_sms * 4)), 256, 0, s>>>(
@@ -403,8 +459,8 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     const int grid = (int)std::min<int64_t>(nblk, ctx->num_sms);
     {
         ProfScope ps(ctx, "rp_update", s);
-        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, F, ldF, N, X, d, (float)scale, sacc, minv_f, b,
-                                                          bprep, rv, dvec, dblk, err);
+        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, F, ldF, N, Kc, minv_f, b, bprep, rv, dvec, dblk,
+                                                          err);
         KEVD_LAUNCH(ctx);
     }
     return KEVD_OK;
