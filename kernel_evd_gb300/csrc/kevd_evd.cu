@@ -25,8 +25,20 @@
 
 namespace kevd {
 
-int run_gram_tc(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, const double* s, double* G,
+int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s, double* G,
                 cudaStream_t st);
+int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
+                      cudaStream_t st);
+
+// Column-major copy of an FP32 factor for the tensor-core Grams (K-major TMA tiles).
+static int transposed(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float** FT,
+                      int64_t* ldT, cudaStream_t s) {
+    *ldT = (N + 3) / 4 * 4;
+    int st = KEVD_OK;
+    *FT = arena_get<float>(ctx, "ev.FT", (size_t)k * (size_t)(*ldT), &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "transpose: out of device memory");
+    return run_transpose_f32(ctx, F, ldF, N, k, *FT, *ldT, s);
+}
 
 // ---- column sums c = F^T w (w == nullptr: ones) ----------------------------
 template <typename T>
@@ -589,8 +601,11 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
         // FP32 factor: 3xTF32 tcgen05 Gram with FP64 accumulation across row chunks
         ev_rsqrt_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(qtil, w2, N);
         KEVD_LAUNCH(ctx);
-        KEVD_TRY(run_gram_tc(ctx, (const float*)F, ldF, N, k, dinv, A, s));
-        KEVD_TRY(run_gram_tc(ctx, (const float*)F, ldF, N, k, w2, B, s));
+        float* FT = nullptr;
+        int64_t ldT = 0;
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, s));
+        KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, dinv, A, s));
+        KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, w2, B, s));
     } else {
         ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
         KEVD_LAUNCH(ctx);
@@ -620,21 +635,30 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
                                                  &lwork2));
     double* work = arena_get<double>(ctx, "ev.work", (size_t)std::max(lwork, lwork2) + 1, &st);
     if (st != KEVD_OK) return st;
-    KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A, (int)k, work,
-                                      lwork, flags + 2));
+    {
+        ProfScope p1(ctx, "dense_potrf", s);
+        KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A, (int)k, work,
+                                          lwork, flags + 2));
+    }
     // dense 2: W = L^T B L
     const double one = 1.0;
-    KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                               CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, B, (int)k, W,
-                               (int)k));
-    KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                               CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, W, (int)k, W,
-                               (int)k));
+    {
+        ProfScope p2(ctx, "dense_trmm", s);
+        KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                   CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, B, (int)k, W,
+                                   (int)k));
+        KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                                   CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, W, (int)k, W,
+                                   (int)k));
+    }
     ev_symmetrize_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(W, k);
     KEVD_LAUNCH(ctx);
     if (dump) KEVD_TRY(d2h(ctx, dump->W, W, (size_t)k * k, s));
-    KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                      (int)k, W, (int)k, lam, work, lwork2, flags + 3));
+    {
+        ProfScope p3(ctx, "dense_syevd", s);
+        KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                          (int)k, W, (int)k, lam, work, lwork2, flags + 3));
+    }
     // Z = L^{-T} V[:, k-k_out:]
     KEVD_CUDA(ctx, cudaMemcpyAsync(Z, W + (k - k_out) * k, (size_t)k * k_out * sizeof(double),
                                    cudaMemcpyDeviceToDevice, s));
@@ -674,7 +698,12 @@ int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, in
                       const double* s_dev, double* G, cudaStream_t st) {
     if (!F || !s_dev || !G || N < 1 || k < 1 || ldF < k)
         return set_error(ctx, KEVD_ERR_ARG, "weighted_gram: bad arguments");
-    if (precision == KEVD_MIXED) return run_gram_tc(ctx, (const float*)F, ldF, N, k, s_dev, G, st);
+    if (precision == KEVD_MIXED) {
+        float* FT = nullptr;
+        int64_t ldT = 0;
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, st));
+        return run_gram_tc(ctx, FT, ldT, N, k, s_dev, G, st);
+    }
     if (precision != KEVD_FP64) return set_error(ctx, KEVD_ERR_ARG, "weighted_gram: unknown precision");
     int rc = KEVD_OK;
     double* w2 = arena_get<double>(ctx, "wg.w2", N, &rc);

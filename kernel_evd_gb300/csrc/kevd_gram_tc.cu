@@ -25,6 +25,9 @@
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 namespace kevd {
@@ -37,14 +40,17 @@ constexpr int kStages = 3;
 constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
 constexpr int kStageBytes = 4 * kOpBytes;   // a_hi, a_lo, b_hi, b_lo
-constexpr int kEpiWarps = 4;
-constexpr int kCvtWarps = 8;
-constexpr int kMmaWarp = kEpiWarps + kCvtWarps;
-constexpr int kThreads = (kMmaWarp + 1) * 32;
+constexpr int kEpiWarps = 4;        // warps 0-3
+constexpr int kCvtWarp0 = 4;        // warps 4-7
+constexpr int kCvtWarps = 4;
+constexpr int kProdWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr int kThreads = 10 * 32;
 constexpr uint32_t kTmemCols = 256;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
+    uint64_t tma[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
     uint64_t accf[2];
@@ -53,7 +59,7 @@ struct Barriers {
     uint32_t tmem_base;
 };
 
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
+constexpr size_t kSmemBytes = (size_t)kStages * (4 * kOpBytes + 1024) + sizeof(Barriers) + 1024;
 
 __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
     int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -63,94 +69,43 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
     tb = t - i * (i + 1) / 2;
 }
 
-// A converter lane owns 4 rows (4kq .. 4kq+3 of the stage) x 4 columns
-// (m0 .. m0+3 of the tile): one float4 per row on the load side, one 16-byte
-// K-chunk per column on the store side.  Lanes 8j..8j+7 take kq = 0..7 for
-// the same columns, so each 8-lane store phase hits 8 distinct 16-byte bank
-// groups of the swizzled tile.
-struct Frag {
-    float v[4][4];   // [row t][col u]
-    float s[4];      // row scales
-};
+// Per stage (32 rows of F = 32 columns of FT):
+//   [a_hi 16 KB][a_lo 16 KB][b_hi 16 KB][b_lo 16 KB][s 256 B]
+// The TMA writes the raw FT boxes (128 factor columns x 32 rows, K-major,
+// SWIZZLE_128B) into the hi slots and the 32 row weights into s; the
+// converters overwrite hi in place with rn_tf32(y) and write lo = rn_tf32(y - hi),
+// y = s_i * F[i][c].  Element (m, k) of a slot sits at sw128_off(m, k), so a
+// 16-byte chunk holds 4 consecutive rows k of one column m.
+constexpr int kSOff = 4 * kOpBytes;
+constexpr int kStageAlloc = 4 * kOpBytes + 1024;   // keeps every stage 1024-aligned
 
-__device__ __forceinline__ void load_frag(const float* __restrict__ F, int64_t ldF, int64_t k, int64_t r1,
-                                          const double* __restrict__ srow, int64_t i_base, int64_t col,
-                                          bool vec4, Frag& f) {
+__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const double* sv, int64_t a0, int64_t k,
+                                           int ct) {
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        const int64_t i = i_base + t;
-        f.s[t] = 0.f;
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;
+        const uint32_t m = off >> 7;                                   // tile column
+        const uint32_t kc = ((off >> 4) & 7u) ^ (m & 7u);               // logical K chunk
+        float4 v = *reinterpret_cast<float4*>(hi + off);
+        const bool colok = (a0 + (int64_t)m) < k;
+        float x[4] = {v.x, v.y, v.z, v.w}, h[4], l[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) f.v[t][u] = 0.f;
-        if (i < r1) {
-            f.s[t] = (float)srow[i];
-            const float* p = F + i * ldF + col;
-            if (vec4 && col + 3 < k) {
-                const float4 q = __ldg(reinterpret_cast<const float4*>(p));
-                f.v[t][0] = q.x;
-                f.v[t][1] = q.y;
-                f.v[t][2] = q.z;
-                f.v[t][3] = q.w;
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (col + u < k) f.v[t][u] = __ldg(p + u);
-            }
+        for (int u = 0; u < 4; ++u) {
+            const float y = colok ? (float)((double)x[u] * sv[4 * kc + u]) : 0.f;
+            h[u] = tc::tf32_rn(y);
+            l[u] = tc::tf32_rn(y - h[u]);
         }
-    }
-}
-
-// Writes the fragment as 4 K-chunks (k = 4kq .. 4kq+3) of columns m0 .. m0+3
-// of the K-major hi / lo tiles.
-__device__ __forceinline__ void store_frag(const Frag& f, uint8_t* hi, uint8_t* lo, int m0, int kq) {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        float h[4], l[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const float y = f.v[t][u] * f.s[t];
-            h[t] = tc::tf32_rn(y);
-            l[t] = tc::tf32_rn(y - h[t]);
-        }
-        const uint32_t off = tc::sw128_off((uint32_t)(m0 + u), (uint32_t)(4 * kq));
         *reinterpret_cast<float4*>(hi + off) = make_float4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<float4*>(lo + off) = make_float4(l[0], l[1], l[2], l[3]);
     }
 }
 
-// Converter step for stage s: prefetch stage s+1 into (na, nb), wait for the
-// ring slot, publish (ca, cb) as hi/lo operand tiles.
-__device__ __forceinline__ bool cvt_stage(int64_t s, int64_t n_stages, const float* __restrict__ F, int64_t ldF,
-                                          int64_t k, int64_t r0, int64_t r1, const double* __restrict__ srow,
-                                          int64_t a0, int64_t b0, int m0, int kq, int lane, int vec4, bool diag,
-                                          uint8_t* base, Barriers* bar, int* err, const Frag& ca, const Frag& cb,
-                                          Frag& na, Frag& nb) {
-    if (s + 1 < n_stages) {
-        const int64_t ib = r0 + (s + 1) * kTK + 4 * kq;
-        load_frag(F, ldF, k, r1, srow, ib, a0 + m0, vec4, na);
-        if (!diag) load_frag(F, ldF, k, r1, srow, ib, b0 + m0, vec4, nb);
-    }
-    const int slot = (int)(s % kStages);
-    const uint32_t use = (uint32_t)(s / kStages);
-    if (!tc::mbar_wait(&bar->empty[slot], (use & 1u) ^ 1u, kTimeoutNs)) {
-        atomicExch(err, 1);
-        return false;
-    }
-    uint8_t* st = base + (size_t)slot * kStageBytes;
-    store_frag(ca, st, st + kOpBytes, m0, kq);
-    if (!diag) store_frag(cb, st + 2 * kOpBytes, st + 3 * kOpBytes, m0, kq);
-    tc::fence_async_smem();
-    __syncwarp();
-    if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
-    return true;
-}
-
 __global__ void __launch_bounds__(kThreads, 1)
-gram_tc_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ srow,
-               int n_tiles, int64_t rows_per, int vec4, double* __restrict__ partial, int* __restrict__ err) {
+gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmS, int64_t N,
+               int64_t k, int n_tiles, int64_t rows_per, double* __restrict__ partial, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageBytes);
+    Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageAlloc);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     const int64_t tix = blockIdx.x % n_tiles;
@@ -167,6 +122,7 @@ gram_tc_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k, c
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
+            tc::mbar_init(&bar->tma[s], 1);
             tc::mbar_init(&bar->full[s], kCvtWarps);
             tc::mbar_init(&bar->empty[s], 1);
         }
@@ -186,25 +142,43 @@ gram_tc_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k, c
     tc::tc_fence_after();
     const uint32_t tbase = bar->tmem_base;
 
-    if (warp >= kEpiWarps && warp < kMmaWarp) {
-        // ---------------- converters
-        const int cw = warp - kEpiWarps;
-        const int kq = lane & 7;                      // K chunk: stage rows 4kq .. 4kq+3
-        const int m0 = 16 * cw + 4 * (lane >> 3);     // tile columns m0 .. m0+3
-        Frag f0a, f0b, f1a, f1b;
-        if (n_stages > 0) {
-            const int64_t ib = r0 + 4 * kq;
-            load_frag(F, ldF, k, r1, srow, ib, a0 + m0, vec4, f0a);
-            if (!diag) load_frag(F, ldF, k, r1, srow, ib, b0 + m0, vec4, f0b);
+    if (warp == kProdWarp) {
+        // ---------------- TMA producer
+        if (lane == 0) {
+            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes) + 256u;
+            for (int64_t s = 0; s < n_stages; ++s) {
+                const int slot = (int)(s % kStages);
+                const uint32_t use = (uint32_t)(s / kStages);
+                if (!tc::mbar_wait(&bar->empty[slot], (use & 1u) ^ 1u, kTimeoutNs)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                uint8_t* st = base + (size_t)slot * kStageAlloc;
+                const int x = (int)(r0 + s * kTK);
+                tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
+                tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
+                if (!diag) tc::tma_load_2d(st + 2 * kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
+                tc::tma_load_1d(st + kSOff, &tmS, x, &bar->tma[slot]);
+            }
         }
-        for (int64_t s = 0; s < n_stages; s += 2) {
-            if (!cvt_stage(s, n_stages, F, ldF, k, r0, r1, srow, a0, b0, m0, kq, lane, vec4, diag, base, bar,
-                           err, f0a, f0b, f1a, f1b))
+        __syncwarp();
+    } else if (warp >= kCvtWarp0 && warp < kCvtWarp0 + kCvtWarps) {
+        // ---------------- converters (128 threads, 8 chunks of 16 B per tile each)
+        const int ct = (warp - kCvtWarp0) * 32 + lane;
+        for (int64_t s = 0; s < n_stages; ++s) {
+            const int slot = (int)(s % kStages);
+            const uint32_t use = (uint32_t)(s / kStages);
+            if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
+                atomicExch(err, 5);
                 break;
-            if (s + 1 < n_stages &&
-                !cvt_stage(s + 1, n_stages, F, ldF, k, r0, r1, srow, a0, b0, m0, kq, lane, vec4, diag, base,
-                           bar, err, f1a, f1b, f0a, f0b))
-                break;
+            }
+            uint8_t* st = base + (size_t)slot * kStageAlloc;
+            const double* sv = reinterpret_cast<const double*>(st + kSOff);
+            split_tile(st, st + kOpBytes, sv, a0, k, ct);
+            if (!diag) split_tile(st + 2 * kOpBytes, st + 3 * kOpBytes, sv, b0, k, ct);
+            tc::fence_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }
     } else if (warp == kMmaWarp) {
         // ---------------- MMA issuer
@@ -230,7 +204,7 @@ gram_tc_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k, c
                         break;
                     }
                     tc::tc_fence_after();
-                    uint8_t* st = base + (size_t)slot * kStageBytes;
+                    uint8_t* st = base + (size_t)slot * kStageAlloc;
                     const uint32_t ahi = tc::smem_u32(st), alo = tc::smem_u32(st + kOpBytes);
                     const uint32_t bhi = diag ? ahi : tc::smem_u32(st + 2 * kOpBytes);
                     const uint32_t blo = diag ? alo : tc::smem_u32(st + 3 * kOpBytes);
@@ -306,11 +280,82 @@ __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_
     }
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// FT[c * ldT + i] = F[i * ldF + c]: 32 x 32 tiles through shared memory.
+__global__ void transpose_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k,
+                                 float* __restrict__ FT, int64_t ldT) {
+    __shared__ float t[32][33];
+    const int64_t n_ti = (N + 31) / 32, n_tc = (k + 31) / 32;
+    for (int64_t tile = blockIdx.x; tile < n_ti * n_tc; tile += gridDim.x) {
+        const int64_t i0 = (tile % n_ti) * 32, c0 = (tile / n_ti) * 32;
+        __syncthreads();
+        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+            const int64_t i = i0 + r, c = c0 + threadIdx.x;
+            t[r][threadIdx.x] = (i < N && c < k) ? F[i * ldF + c] : 0.f;
+        }
+        __syncthreads();
+        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+            const int64_t c = c0 + r, i = i0 + threadIdx.x;
+            if (c < k && i < ldT) FT[c * ldT + i] = t[threadIdx.x][r];
+        }
+    }
+}
+
 }  // namespace
 
-// G (k x k, column-major, full) = F^T diag(s)^2 F for an FP32 factor.
-int run_gram_tc(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, const double* s, double* G,
+// Column-major copy FT (k x ldT, ldT = N rounded up to 4) of a row-major FP32 factor.
+int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
+                      cudaStream_t st) {
+    ProfScope ps(ctx, "ev_transpose", st);
+    const int64_t tiles = ((N + 31) / 32) * ((k + 31) / 32);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16);
+    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(F, ldF, N, k, FT, ldT);
+    KEVD_LAUNCH(ctx);
+    return KEVD_OK;
+}
+
+// G (k x k, column-major, full) = F^T diag(s)^2 F from the column-major FP32
+// factor FT (k x ldT).  s: device, N doubles.
+int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s, double* G,
                 cudaStream_t st) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: cuTensorMapEncodeTiled unavailable");
+    if ((ldT % 4) != 0 || ((uintptr_t)FT % 16) != 0 || ((uintptr_t)s % 16) != 0)
+        return set_error(ctx, KEVD_ERR_ARG, "gram_tc: FT / s must be 16-byte aligned with ldT %% 4 == 0");
+    CUtensorMap tmF, tmS;
+    {
+        const cuuint64_t gdim[2] = {(cuuint64_t)N, (cuuint64_t)k};
+        const cuuint64_t gstride[1] = {(cuuint64_t)ldT * 4};
+        const cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTT};
+        const cuuint32_t estr[2] = {1, 1};
+        CUresult cr = enc(&tmF, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)FT, gdim, gstride, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: tensor map (F) failed (%d)", (int)cr);
+    }
+    {
+        const cuuint64_t gdim[1] = {(cuuint64_t)N};
+        const cuuint32_t box[1] = {(cuuint32_t)kTK};
+        const cuuint32_t estr[1] = {1};
+        CUresult cr = enc(&tmS, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 1, (void*)s, gdim, nullptr, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: tensor map (s) failed (%d)", (int)cr);
+    }
     const int nt = ceil_div(k, kTT);
     const int n_tiles = nt * (nt + 1) / 2;
     int n_split = std::max(1, ctx->num_sms / n_tiles);
@@ -323,11 +368,10 @@ int run_gram_tc(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k
     KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
     KEVD_CUDA(ctx, cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)kSmemBytes));
-    const int vec4 = ((ldF % 4) == 0 && ((uintptr_t)F % 16) == 0) ? 1 : 0;
     {
         ProfScope ps(ctx, "gram_tc", st);
-        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(F, ldF, N, k, s, n_tiles, rows_per, vec4,
-                                                                       partial, err);
+        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, tmS, N, k, n_tiles, rows_per, partial,
+                                                                       err);
         KEVD_LAUNCH(ctx);
     }
     gram_tc_reduce_kernel<<<n_tiles, 256, 0, st>>>(partial, n_tiles, n_split, k, G);

@@ -86,7 +86,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float* mv = reinterpret_cast<float*>(base + (size_t)kStages * kStageBytes);   // kCols x kCols
-    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
+    float* kt = mv + kCols * kCols;              // kRows x (kCols + 1): K(R, S_i), then G
+    Bars* bar = reinterpret_cast<Bars*>(kt + kRows * (kCols + 1));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // L_i^{-1} (FP32) for the epilogue
@@ -230,6 +231,25 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
         bool ok = true;
         __shared__ double wsum[4];
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
+            // stage K(R, S_i) (contiguous 128 x 64 floats) into padded smem with
+            // coalesced loads; they complete while the block's MMAs run
+            const int64_t row0 = rb * kRows;
+            {
+                const float4* src = reinterpret_cast<const float4*>(Kc + row0 * kCols);
+                const int64_t n4 = (min((int64_t)kRows, N - row0) * kCols) / 4;
+#pragma unroll 4
+                for (int e = rloc; e < kRows * kCols / 4; e += 128) {
+                    const float4 v = (e < n4) ? __ldg(src + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const int rr = (4 * e) / kCols, cc = (4 * e) % kCols;
+                    float* dst = kt + rr * (kCols + 1) + cc;
+                    dst[0] = v.x;
+                    dst[1] = v.y;
+                    dst[2] = v.z;
+                    dst[3] = v.w;
+                }
+            }
+            const int64_t i = row0 + rloc;
+            const double d_old = (i < N) ? dvec[i] : 0.0;
             float acc[kCols];
 #pragma unroll
             for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
@@ -256,22 +276,15 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
             }
-            const int64_t i = rb * kRows + rloc;
-            double nd = 0.0;
+            asm volatile("bar.sync 1, 128;" ::: "memory");   // kt filled
+            double nd = d_old;
+            float* krow = kt + rloc * (kCols + 1);
             if (ok && i < N) {
                 // T = K(i, S_i) - P  (K(:, S_i) precomputed by update_kcols_kernel)
-                const float4* kr = reinterpret_cast<const float4*>(Kc + i * kCols);
 #pragma unroll
-                for (int c4 = 0; c4 < kCols / 4; ++c4) {
-                    const float4 kv = __ldg(kr + c4);
-                    acc[4 * c4 + 0] = kv.x - acc[4 * c4 + 0];
-                    acc[4 * c4 + 1] = kv.y - acc[4 * c4 + 1];
-                    acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
-                    acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
-                }
-                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc)
+                for (int c = 0; c < kCols; ++c) acc[c] = krow[c] - acc[c];
+                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc); G -> kt row
                 float sq = 0.f;
-                float* frow = F + i * ldF + r;
 #pragma unroll
                 for (int a = 0; a < kCols; ++a) {
                     if (a < nacc) {
@@ -279,14 +292,22 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
                         const float* ma = mv + a * kCols;
 #pragma unroll
                         for (int e = 0; e <= a; ++e) gsum = fmaf(acc[e], ma[e], gsum);
-                        frow[a] = gsum;
+                        krow[a] = gsum;
                         sq = fmaf(gsum, gsum, sq);
                     }
                 }
-                nd = fmax(dvec[i] - (double)sq, 0.0);
+                nd = fmax(d_old - (double)sq, 0.0);
                 dvec[i] = nd;
-            } else if (i < N) {
-                nd = dvec[i];
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");   // G rows in kt
+            // coalesced store of the new columns: warp q writes rows q, q+4, ...
+            if (ok) {
+                const int64_t nrows = min((int64_t)kRows, N - row0);
+                for (int rr = q; rr < nrows; rr += 4) {
+                    float* frow = F + (row0 + rr) * ldF + r;
+                    const float* grow = kt + rr * (kCols + 1);
+                    for (int a = lane; a < nacc; a += 32) frow[a] = grow[a];
+                }
             }
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
@@ -401,7 +422,8 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + kCols * kCols * 4 + sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + kCols * kCols * 4 + kRows * (kCols + 1) * 4 +
+                            sizeof(Bars) + 1024;
 
 // Whether the tensor-core update can run for this factor layout.
 bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
