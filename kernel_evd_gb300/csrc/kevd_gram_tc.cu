@@ -70,17 +70,17 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
 }
 
 // Per stage (32 rows of F = 32 columns of FT):
-//   [a_hi 16 KB][a_lo 16 KB][b_hi 16 KB][b_lo 16 KB][s 256 B]
+//   [a_hi 16 KB][a_lo 16 KB][b_hi 16 KB][b_lo 16 KB]
 // The TMA writes the raw FT boxes (128 factor columns x 32 rows, K-major,
-// SWIZZLE_128B) into the hi slots and the 32 row weights into s; the
+// SWIZZLE_128B) into the hi slots; the
 // converters overwrite hi in place with rn_tf32(y) and write lo = rn_tf32(y - hi),
 // y = s_i * F[i][c].  Element (m, k) of a slot sits at sw128_off(m, k), so a
 // 16-byte chunk holds 4 consecutive rows k of one column m.
-constexpr int kSOff = 4 * kOpBytes;
 constexpr int kStageAlloc = 4 * kOpBytes + 1024;   // keeps every stage 1024-aligned
 
-__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const double* sv, int64_t a0, int64_t k,
-                                           int ct) {
+// sv: this lane's row weight s[i0 + lane] (0 past N); weight of row k of the
+// stage = lane k's value.
+__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, double sv, int64_t a0, int64_t k, int ct) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;
@@ -91,7 +91,8 @@ __device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const doubl
         float x[4] = {v.x, v.y, v.z, v.w}, h[4], l[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const float y = colok ? (float)((double)x[u] * sv[4 * kc + u]) : 0.f;
+            const double w = __shfl_sync(0xffffffffu, sv, (int)(4 * kc + u));
+            const float y = colok ? (float)((double)x[u] * w) : 0.f;
             h[u] = tc::tf32_rn(y);
             l[u] = tc::tf32_rn(y - h[u]);
         }
@@ -101,8 +102,8 @@ __device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const doubl
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ CUtensorMap tmS, int64_t N,
-               int64_t k, int n_tiles, int64_t rows_per, double* __restrict__ partial, int* __restrict__ err) {
+gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict__ srow, int64_t N, int64_t k,
+               int n_tiles, int64_t rows_per, double* __restrict__ partial, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageAlloc);
@@ -145,7 +146,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ 
     if (warp == kProdWarp) {
         // ---------------- TMA producer
         if (lane == 0) {
-            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes) + 256u;
+            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes);
             for (int64_t s = 0; s < n_stages; ++s) {
                 const int slot = (int)(s % kStages);
                 const uint32_t use = (uint32_t)(s / kStages);
@@ -158,7 +159,6 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ 
                 tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
                 tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
                 if (!diag) tc::tma_load_2d(st + 2 * kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
-                tc::tma_load_1d(st + kSOff, &tmS, x, &bar->tma[slot]);
             }
         }
         __syncwarp();
@@ -168,12 +168,13 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const __grid_constant__ 
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
+            const int64_t irow = r0 + s * kTK + lane;
+            const double sv = (irow < r1) ? __ldg(srow + irow) : 0.0;   // issued before the wait
             if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
                 atomicExch(err, 5);
                 break;
             }
             uint8_t* st = base + (size_t)slot * kStageAlloc;
-            const double* sv = reinterpret_cast<const double*>(st + kSOff);
             split_tile(st, st + kOpBytes, sv, a0, k, ct);
             if (!diag) split_tile(st + 2 * kOpBytes, st + 3 * kOpBytes, sv, b0, k, ct);
             tc::fence_async_smem();
@@ -334,9 +335,9 @@ int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t 
                 cudaStream_t st) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     if (!enc) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: cuTensorMapEncodeTiled unavailable");
-    if ((ldT % 4) != 0 || ((uintptr_t)FT % 16) != 0 || ((uintptr_t)s % 16) != 0)
-        return set_error(ctx, KEVD_ERR_ARG, "gram_tc: FT / s must be 16-byte aligned with ldT %% 4 == 0");
-    CUtensorMap tmF, tmS;
+    if ((ldT % 4) != 0 || ((uintptr_t)FT % 16) != 0)
+        return set_error(ctx, KEVD_ERR_ARG, "gram_tc: FT must be 16-byte aligned with ldT %% 4 == 0");
+    CUtensorMap tmF;
     {
         const cuuint64_t gdim[2] = {(cuuint64_t)N, (cuuint64_t)k};
         const cuuint64_t gstride[1] = {(cuuint64_t)ldT * 4};
@@ -346,15 +347,6 @@ int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t 
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (cr != CUDA_SUCCESS) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: tensor map (F) failed (%d)", (int)cr);
-    }
-    {
-        const cuuint64_t gdim[1] = {(cuuint64_t)N};
-        const cuuint32_t box[1] = {(cuuint32_t)kTK};
-        const cuuint32_t estr[1] = {1};
-        CUresult cr = enc(&tmS, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 1, (void*)s, gdim, nullptr, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                          CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (cr != CUDA_SUCCESS) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: tensor map (s) failed (%d)", (int)cr);
     }
     const int nt = ceil_div(k, kTT);
     const int n_tiles = nt * (nt + 1) / 2;
@@ -370,7 +362,7 @@ int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t 
                                         (int)kSmemBytes));
     {
         ProfScope ps(ctx, "gram_tc", st);
-        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, tmS, N, k, n_tiles, rows_per, partial,
+        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, s, N, k, n_tiles, rows_per, partial,
                                                                        err);
         KEVD_LAUNCH(ctx);
     }
