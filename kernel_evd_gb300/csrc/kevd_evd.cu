@@ -284,6 +284,255 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
     }
 }
 
+// ---- streaming passes on the column-major FP32 factor FT (k x ldT) ------------
+// Reads are coalesced along rows; products are FP32 (round to nearest) and the
+// long sums over rows or columns are FP64.
+
+// c[j] = sum_i w_i FT[j][i]  (w == nullptr: ones).  One CTA per column.
+__global__ void __launch_bounds__(256)
+evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, const double* __restrict__ w,
+                  double* __restrict__ c) {
+    const int64_t j = blockIdx.x;
+    const float* col = FT + j * ldT;
+    double acc = 0.0;
+    float part = 0.f;
+    int cnt = 0;
+    for (int64_t i = threadIdx.x; i < N; i += 256) {
+        const float f = col[i];
+        part = w ? fmaf(f, (float)w[i], part) : part + f;
+        if (++cnt == 64) {
+            acc += (double)part;
+            part = 0.f;
+            cnt = 0;
+        }
+    }
+    acc += (double)part;
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c[j] = red[0];
+}
+
+// y_i = sum_j FT[j][i] v_j with v split into an FP32 hi/lo pair; FP64 every 32
+// terms; yinv = 1/y; bad |= (y <= 0).
+__global__ void __launch_bounds__(256)
+evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ v,
+                  double* __restrict__ y, double* __restrict__ yinv, int* __restrict__ bad) {
+    extern __shared__ float vhl[];   // 2k floats
+    for (int64_t j = threadIdx.x; j < k; j += blockDim.x) {
+        const float h = (float)v[j];
+        vhl[2 * j] = h;
+        vhl[2 * j + 1] = (float)(v[j] - (double)h);
+    }
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double acc = 0.0;
+    for (int64_t j0 = 0; j0 < k; j0 += 32) {
+        float part = 0.f;
+        const int64_t j1 = min(k, j0 + 32);
+        for (int64_t j = j0; j < j1; ++j) {
+            const float f = FT[j * ldT + i];
+            part = fmaf(f, vhl[2 * j], fmaf(f, vhl[2 * j + 1], part));
+        }
+        acc += (double)part;
+    }
+    y[i] = acc;
+    yinv[i] = 1.0 / acc;
+    if (!(acc > 0.0)) atomicOr(bad, 1);
+}
+
+// U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32)
+__global__ void __launch_bounds__(256)
+evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ Z, int m,
+             const double* __restrict__ dinv, float* __restrict__ U) {
+    __shared__ __align__(16) float Zs[128][32];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float acc[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) acc[q] = 0.f;
+    for (int64_t j0 = 0; j0 < k; j0 += 128) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
+            const int jj = e >> 5, q = e & 31;
+            const int64_t j = j0 + jj;
+            Zs[jj][q] = (j < k && q < m) ? (float)Z[(int64_t)q * k + j] : 0.f;
+        }
+        __syncthreads();
+        if (i < N) {
+            const int64_t jn = min((int64_t)128, k - j0);
+            for (int jj = 0; jj < jn; ++jj) {
+                const float f = FT[(j0 + jj) * ldT + i];
+                const float4* zr = reinterpret_cast<const float4*>(Zs[jj]);
+#pragma unroll
+                for (int q4 = 0; q4 < 8; ++q4) {
+                    const float4 z = zr[q4];
+                    acc[4 * q4 + 0] = fmaf(f, z.x, acc[4 * q4 + 0]);
+                    acc[4 * q4 + 1] = fmaf(f, z.y, acc[4 * q4 + 1]);
+                    acc[4 * q4 + 2] = fmaf(f, z.z, acc[4 * q4 + 2]);
+                    acc[4 * q4 + 3] = fmaf(f, z.w, acc[4 * q4 + 3]);
+                }
+            }
+        }
+    }
+    if (i >= N) return;
+    const double di = dinv[i];
+#pragma unroll
+    for (int q = 0; q < 32; ++q)
+        if (q < m) U[i * m + q] = (float)((double)acc[q] * di);
+}
+
+// Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
+// CTA's rows, for a block of 64 columns j.  thread: columns 4 (tid >> 4)..+4,
+// U columns 2 (tid & 15)..+2.
+__global__ void __launch_bounds__(256)
+evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
+              const double* __restrict__ dinv, int64_t rows_per, double* __restrict__ partial) {
+    __shared__ float Fs[64][65];
+    __shared__ __align__(16) float Ws[64][32];
+    const int tid = threadIdx.x;
+    const int jr = 4 * (tid >> 4), qc = 2 * (tid & 15);
+    const int64_t j0 = (int64_t)blockIdx.x * 64;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
+    double acc64[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    for (int64_t i0 = r0; i0 < r1; i0 += 64) {
+        __syncthreads();
+        for (int e = tid; e < 64 * 64; e += 256) {
+            const int jj = e >> 6, ii = e & 63;
+            const int64_t j = j0 + jj, i = i0 + ii;
+            Fs[jj][ii] = (j < k && i < r1) ? FT[j * ldT + i] : 0.f;
+        }
+        for (int e = tid; e < 64 * 32; e += 256) {
+            const int ii = e >> 5, q = e & 31;
+            const int64_t i = i0 + ii;
+            Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
+        }
+        __syncthreads();
+        float acc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+#pragma unroll 8
+        for (int ii = 0; ii < 64; ++ii) {
+            const float w0 = Ws[ii][qc], w1 = Ws[ii][qc + 1];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float f = Fs[jr + a][ii];
+                acc[a][0] = fmaf(f, w0, acc[a][0]);
+                acc[a][1] = fmaf(f, w1, acc[a][1]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            acc64[a][0] += (double)acc[a][0];
+            acc64[a][1] += (double)acc[a][1];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int64_t j = j0 + jr + a;
+        if (j >= k) continue;
+        for (int b = 0; b < 2; ++b) {
+            const int q = qc + b;
+            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = acc64[a][b];
+        }
+    }
+}
+
+// Rayleigh-Ritz H and M partials over 256-row tiles: w_i = F_i (T1h + T1l)
+// (T1 as an FP32 hi/lo pair, k x 32), H += (w/sqrt(q))(w/sqrt(q))^T, M += u u^T.
+__global__ void __launch_bounds__(256)
+evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ T1hl,
+              int m, const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
+    __shared__ __align__(16) float Ts[2][32][32];   // hi, lo for a 32-row chunk of T1
+    __shared__ float Ws[256][33];
+    const int tid = threadIdx.x;
+    double h64[4] = {0, 0, 0, 0}, m64[4] = {0, 0, 0, 0};
+    const int64_t n_tiles = (N + 255) / 256;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const int64_t i = t * 256 + tid;
+        float w[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) w[q] = 0.f;
+        for (int64_t j0 = 0; j0 < k; j0 += 32) {
+            __syncthreads();
+            for (int e = tid; e < 32 * 32; e += 256) {
+                const int jj = e >> 5, q = e & 31;
+                const int64_t j = j0 + jj;
+                Ts[0][jj][q] = (j < k) ? T1hl[(2 * j) * 32 + q] : 0.f;
+                Ts[1][jj][q] = (j < k) ? T1hl[(2 * j + 1) * 32 + q] : 0.f;
+            }
+            __syncthreads();
+            if (i < N) {
+                const int jn = (int)min((int64_t)32, k - j0);
+                for (int jj = 0; jj < jn; ++jj) {
+                    const float f = FT[(j0 + jj) * ldT + i];
+                    const float4* th = reinterpret_cast<const float4*>(Ts[0][jj]);
+                    const float4* tl = reinterpret_cast<const float4*>(Ts[1][jj]);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                        const float4 a = th[q4], b = tl[q4];
+                        w[4 * q4 + 0] = fmaf(f, a.x, fmaf(f, b.x, w[4 * q4 + 0]));
+                        w[4 * q4 + 1] = fmaf(f, a.y, fmaf(f, b.y, w[4 * q4 + 1]));
+                        w[4 * q4 + 2] = fmaf(f, a.z, fmaf(f, b.z, w[4 * q4 + 2]));
+                        w[4 * q4 + 3] = fmaf(f, a.w, fmaf(f, b.w, w[4 * q4 + 3]));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) Ws[tid][q] = (q < m) ? w[q] * sq : 0.f;
+        __syncthreads();
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) {
+            const int e = tid + 256 * qq;
+            const int ja = e >> 5, jb = e & 31;
+            float hs = 0.f;
+            for (int rr = 0; rr < 256; ++rr) hs = fmaf(Ws[rr][ja], Ws[rr][jb], hs);
+            h64[qq] += (double)hs;
+        }
+        __syncthreads();
+        {
+            float uu[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) uu[q] = (i < N && q < m) ? U[i * m + q] : 0.f;
+#pragma unroll
+            for (int q = 0; q < 32; ++q) Ws[tid][q] = uu[q];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) {
+            const int e = tid + 256 * qq;
+            const int ja = e >> 5, jb = e & 31;
+            float ms = 0.f;
+            for (int rr = 0; rr < 256; ++rr) ms = fmaf(Ws[rr][ja], Ws[rr][jb], ms);
+            m64[qq] += (double)ms;
+        }
+    }
+    double* out = partial + (int64_t)blockIdx.x * 2048;
+#pragma unroll
+    for (int qq = 0; qq < 4; ++qq) {
+        out[tid + 256 * qq] = h64[qq];
+        out[1024 + tid + 256 * qq] = m64[qq];
+    }
+}
+
+__global__ void evt_split_t1_kernel(const double* __restrict__ T1, int64_t k, int m, float* __restrict__ T1hl) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k * 32;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e >> 5;
+        const int q = (int)(e & 31);
+        const double t = (q < m) ? T1[j * m + q] : 0.0;
+        const float h = (float)t;
+        T1hl[(2 * j) * 32 + q] = h;
+        T1hl[(2 * j + 1) * 32 + q] = (float)(t - (double)h);
+    }
+}
+
 // ---- Rayleigh-Ritz refinement of the leading eigenpairs (FP32 factor) -------
 // With U = Dtil^{-1} F Z (N x m), U^T P U = T1^T B T1 where T1 = F^T Dtil^{-1} U
 // (k x m) and B = F^T Qtil^{-1} F, so
@@ -293,57 +542,6 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
 // nearest, unbiased) summed in FP64 across rows; the m x m pencil (H, M) gives
 // Ritz values accurate to the square of the eigenvector error of the Gram path.
 
-// T1 partial: rows [r0, r1) of this CTA, 64 columns of F x 32 columns of U.
-// thread: column c = c0 + (tid & 63), U columns 8 (tid >> 6) .. +8.
-template <typename T>
-__global__ void __launch_bounds__(256)
-rr_t1_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const float* __restrict__ U, int m,
-             const double* __restrict__ dinv, int j0, int64_t rows_per, double* __restrict__ partial) {
-    __shared__ float Fs[32][65];
-    __shared__ float Ws[32][33];
-    const int tc = threadIdx.x & 63, tj = threadIdx.x >> 6;
-    const int64_t c0 = (int64_t)blockIdx.x * 64;
-    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
-    const int64_t r1 = min(N, r0 + rows_per);
-    double acc64[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) acc64[q] = 0.0;
-    for (int64_t i0 = r0; i0 < r1; i0 += 32) {
-        for (int e = threadIdx.x; e < 32 * 64; e += 256) {
-            const int rr = e >> 6, cc = e & 63;
-            const int64_t i = i0 + rr, c = c0 + cc;
-            Fs[rr][cc] = (i < r1 && c < k) ? (float)F[i * ldF + c] : 0.f;
-        }
-        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
-            const int rr = e >> 5, jj = e & 31;
-            const int64_t i = i0 + rr;
-            const int j = j0 + jj;
-            Ws[rr][jj] = (i < r1 && j < m) ? (float)((double)U[i * m + j] * dinv[i]) : 0.f;
-        }
-        __syncthreads();
-        float acc[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc[q] = 0.f;
-#pragma unroll 8
-        for (int rr = 0; rr < 32; ++rr) {
-            const float f = Fs[rr][tc];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) acc[q] = fmaf(f, Ws[rr][8 * tj + q], acc[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc64[q] += (double)acc[q];
-        __syncthreads();
-    }
-    const int64_t c = c0 + tc;
-    if (c < k) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = j0 + 8 * tj + q;
-            if (j < m) partial[((int64_t)blockIdx.y * k + c) * m + j] = acc64[q];
-        }
-    }
-}
-
 __global__ void rr_sum_kernel(const double* __restrict__ partial, int n_parts, int64_t len,
                               double* __restrict__ out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < len;
@@ -351,92 +549,6 @@ __global__ void rr_sum_kernel(const double* __restrict__ partial, int n_parts, i
         double s = 0.0;
         for (int p = 0; p < n_parts; ++p) s += partial[(int64_t)p * len + e];
         out[e] = s;
-    }
-}
-
-// H and M partials over 64-row tiles: w = F_i T1 (64 x m) accumulated over
-// 32-column chunks of F in FP32; then H += (w/sqrt(q))^T (w/sqrt(q)) and
-// M += u^T u over the tile, per-tile FP32 sums added into FP64 accumulators.
-// m <= 32.  Thread layout for w: rows 4 (tid >> 4) .. +4, U columns 2 (tid & 15) .. +2.
-template <typename T>
-__global__ void __launch_bounds__(256)
-rr_hm_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ T1, int m,
-             const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
-    __shared__ float Fs[64][33];
-    __shared__ float Ts[32][33];   // T1 = Ts + Tl: the hi/lo FP32 pair keeps T1 to ~2^-48
-    __shared__ float Tl[32][33];
-    __shared__ float Ws[64][33];
-    __shared__ float Us[64][33];
-    const int tid = threadIdx.x;
-    const int wr = 4 * (tid >> 4), wj = 2 * (tid & 15);
-    // H / M ownership: entries e = tid + 256 q (q < 4) of the 32 x 32 matrices
-    double h64[4] = {0, 0, 0, 0}, m64[4] = {0, 0, 0, 0};
-    const int64_t n_tiles = (N + 63) / 64;
-    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const int64_t i0 = t * 64;
-        float w[4][2];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) w[a][0] = w[a][1] = 0.f;
-        for (int64_t c0 = 0; c0 < k; c0 += 32) {
-            __syncthreads();
-            for (int e = tid; e < 64 * 32; e += 256) {
-                const int rr = e >> 5, cc = e & 31;
-                const int64_t i = i0 + rr, c = c0 + cc;
-                Fs[rr][cc] = (i < N && c < k) ? (float)F[i * ldF + c] : 0.f;
-            }
-            for (int e = tid; e < 32 * 32; e += 256) {
-                const int cc = e >> 5, jj = e & 31;
-                const int64_t c = c0 + cc;
-                const double t = (c < k && jj < m) ? T1[c * m + jj] : 0.0;
-                const float th = (float)t;
-                Ts[cc][jj] = th;
-                Tl[cc][jj] = (float)(t - (double)th);
-            }
-            __syncthreads();
-#pragma unroll 8
-            for (int cc = 0; cc < 32; ++cc) {
-                const float t0 = Ts[cc][wj], t1 = Ts[cc][wj + 1];
-                const float l0 = Tl[cc][wj], l1 = Tl[cc][wj + 1];
-#pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const float f = Fs[wr + a][cc];
-                    w[a][0] = fmaf(f, t0, fmaf(f, l0, w[a][0]));
-                    w[a][1] = fmaf(f, t1, fmaf(f, l1, w[a][1]));
-                }
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int64_t i = i0 + wr + a;
-            const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
-            Ws[wr + a][wj] = w[a][0] * sq;
-            Ws[wr + a][wj + 1] = w[a][1] * sq;
-        }
-        for (int e = tid; e < 64 * 32; e += 256) {
-            const int rr = e >> 5, jj = e & 31;
-            const int64_t i = i0 + rr;
-            Us[rr][jj] = (i < N && jj < m) ? U[i * m + jj] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = tid + 256 * q;
-            const int ja = e >> 5, jb = e & 31;
-            float hs = 0.f, ms = 0.f;
-            for (int rr = 0; rr < 64; ++rr) {
-                hs = fmaf(Ws[rr][ja], Ws[rr][jb], hs);
-                ms = fmaf(Us[rr][ja], Us[rr][jb], ms);
-            }
-            h64[q] += (double)hs;
-            m64[q] += (double)ms;
-        }
-    }
-    double* out = partial + (int64_t)blockIdx.x * 2048;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        out[tid + 256 * q] = h64[q];
-        out[1024 + tid + 256 * q] = m64[q];
     }
 }
 
@@ -457,28 +569,29 @@ __global__ void rr_rotate_kernel(float* __restrict__ U, int64_t N, int m, const 
     }
 }
 
-template <typename T>
-static int rayleigh_ritz(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, int m, float* U,
+// On the column-major FP32 factor FT (k x ldT).
+static int rayleigh_ritz(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, int m, float* U,
                          const double* dinv, const double* qinv, double* lam_top, cudaStream_t s) {
     ProfScope ps(ctx, "ev_ritz", s);
     int st = KEVD_OK;
-    const int ny = (int)std::min<int64_t>((N + 4095) / 4096, (int64_t)ctx->num_sms * 2);
-    const int64_t rows_per = ((N + ny - 1) / ny + 31) / 32 * 32;
+    const int ny = (int)std::min<int64_t>((N + 8191) / 8192, (int64_t)ctx->num_sms * 2);
+    const int64_t rows_per = ((N + ny - 1) / ny + 63) / 64 * 64;
     double* tpart = arena_get<double>(ctx, "rr.tpart", (size_t)ny * k * m, &st);
     double* T1 = arena_get<double>(ctx, "rr.T1", (size_t)k * m, &st);
+    float* T1hl = arena_get<float>(ctx, "rr.T1hl", (size_t)k * 64, &st);
     const int nhm = ctx->num_sms * 2;
     double* hmpart = arena_get<double>(ctx, "rr.hmpart", (size_t)nhm * 2048, &st);
     double* HM = arena_get<double>(ctx, "rr.HM", 2048, &st);
     double* w = arena_get<double>(ctx, "rr.w", 64, &st);
     int* info = arena_get<int>(ctx, "rr.info", 1, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
-    for (int j0 = 0; j0 < m; j0 += 32) {
-        rr_t1_kernel<T><<<dim3(ceil_div(k, 64), ny), 256, 0, s>>>(F, ldF, N, k, U, m, dinv, j0, rows_per, tpart);
-        KEVD_LAUNCH(ctx);
-    }
+    evt_t1_kernel<<<dim3(ceil_div(k, 64), ny), 256, 0, s>>>(FT, ldT, N, k, U, m, dinv, rows_per, tpart);
+    KEVD_LAUNCH(ctx);
     rr_sum_kernel<<<ceil_div(k * m, 256), 256, 0, s>>>(tpart, ny, k * m, T1);
     KEVD_LAUNCH(ctx);
-    rr_hm_kernel<T><<<nhm, 256, 0, s>>>(F, ldF, N, k, T1, m, U, qinv, hmpart);
+    evt_split_t1_kernel<<<ceil_div(k * 32, 256), 256, 0, s>>>(T1, k, m, T1hl);
+    KEVD_LAUNCH(ctx);
+    evt_hm_kernel<<<nhm, 256, 0, s>>>(FT, ldT, N, k, T1hl, m, U, qinv, hmpart);
     KEVD_LAUNCH(ctx);
     rr_sum_kernel<<<8, 256, 0, s>>>(hmpart, nhm, 2048, HM);
     KEVD_LAUNCH(ctx);
@@ -585,12 +698,32 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     int* hflags = static_cast<int*>(ctx->pinned);
     KEVD_CUDA(ctx, cudaMemsetAsync(flags, 0, 4 * sizeof(int), s));
 
-    // pass 1: c1 = F^T 1;  pass 2: dtil = F c1, cq = F^T dtil^{-1}
-    KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, nullptr, c1, s));
-    KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, c1, dtil, dinv, flags + 0, s));
-    KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, dinv, cq, s));
-    // pass 3: qtil = F cq
-    KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, cq, qtil, qinv, flags + 1, s));
+    // FP32 factors run every streaming pass on a column-major copy (coalesced
+    // along rows, K-major tensor-core tiles for the Grams)
+    float* FT = nullptr;
+    int64_t ldT = 0;
+    if (sizeof(T) == 4) {
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, s));
+        const size_t vsm = (size_t)2 * k * sizeof(float);
+        KEVD_CUDA(ctx, cudaFuncSetAttribute(evt_rowdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)std::max(vsm, (size_t)1024)));
+        ProfScope ps(ctx, "ev_passes", s);
+        evt_colsum_kernel<<<(int)k, 256, 0, s>>>(FT, ldT, N, nullptr, c1);
+        KEVD_LAUNCH(ctx);
+        evt_rowdot_kernel<<<ceil_div(N, 256), 256, vsm, s>>>(FT, ldT, N, k, c1, dtil, dinv, flags + 0);
+        KEVD_LAUNCH(ctx);
+        evt_colsum_kernel<<<(int)k, 256, 0, s>>>(FT, ldT, N, dinv, cq);
+        KEVD_LAUNCH(ctx);
+        evt_rowdot_kernel<<<ceil_div(N, 256), 256, vsm, s>>>(FT, ldT, N, k, cq, qtil, qinv, flags + 1);
+        KEVD_LAUNCH(ctx);
+    } else {
+        // pass 1: c1 = F^T 1;  pass 2: dtil = F c1, cq = F^T dtil^{-1}
+        KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, nullptr, c1, s));
+        KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, c1, dtil, dinv, flags + 0, s));
+        KEVD_TRY(colsum<T>(ctx, F, ldF, N, k, dinv, cq, s));
+        // pass 3: qtil = F cq
+        KEVD_TRY(rowdot<T>(ctx, F, ldF, N, k, cq, qtil, qinv, flags + 1, s));
+    }
     KEVD_CUDA(ctx, cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     KEVD_CUDA(ctx, cudaStreamSynchronize(s));
     if (hflags[0]) return set_error(ctx, KEVD_ERR_NONPOS_DTIL, "bistochastic_evd: nonpositive dtil");
@@ -601,9 +734,6 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
         // FP32 factor: 3xTF32 tcgen05 Gram with FP64 accumulation across row chunks
         ev_rsqrt_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(qtil, w2, N);
         KEVD_LAUNCH(ctx);
-        float* FT = nullptr;
-        int64_t ldT = 0;
-        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, s));
         KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, dinv, A, s));
         KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, w2, B, s));
     } else {
@@ -667,7 +797,10 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     // pass 4: U = Dtil^{-1} F Z
     {
         ProfScope ps(ctx, "ev_u", s);
-        ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
+        if (sizeof(T) == 4 && k_out <= 32)
+            evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U);
+        else
+            ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
         KEVD_LAUNCH(ctx);
     }
     if (dump) KEVD_TRY(d2h(ctx, dump->Z, Z, (size_t)k * k_out, s));
@@ -679,7 +812,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     if (sizeof(T) == 4 && hflags[2] == 0 && hflags[3] == 0 && k_out <= 32) {
         // FP32 factor: refine the leading k_out eigenpairs by Rayleigh-Ritz in FP64
         double top[32];
-        KEVD_TRY(rayleigh_ritz<T>(ctx, F, ldF, N, k, k_out, U, dinv, qinv, top, s));
+        KEVD_TRY(rayleigh_ritz(ctx, FT, ldT, N, k, k_out, U, dinv, qinv, top, s));
         if (lam_h)
             for (int j = 0; j < k_out; ++j) lam_h[k - k_out + j] = top[j];
     }

@@ -78,21 +78,21 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
 // 16-byte chunk holds 4 consecutive rows k of one column m.
 constexpr int kStageAlloc = 4 * kOpBytes + 1024;   // keeps every stage 1024-aligned
 
-// sv: this lane's row weight s[i0 + lane] (0 past N); weight of row k of the
-// stage = lane k's value.
-__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, double sv, int64_t a0, int64_t k, int ct) {
+// Thread ct handles the 16-byte chunks ct + 128 q (q < 8) of a tile: row
+// m = (ct + 128 q) / 8 and logical K chunk kc = (ct & 7) ^ ((ct >> 3) & 7),
+// the same for every q, so it needs the weights of rows 4 kc .. 4 kc + 3 only.
+__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const float (&w)[4], int64_t a0, int64_t k,
+                                           int ct) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;
         const uint32_t m = off >> 7;                                   // tile column
-        const uint32_t kc = ((off >> 4) & 7u) ^ (m & 7u);               // logical K chunk
         float4 v = *reinterpret_cast<float4*>(hi + off);
         const bool colok = (a0 + (int64_t)m) < k;
         float x[4] = {v.x, v.y, v.z, v.w}, h[4], l[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const double w = __shfl_sync(0xffffffffu, sv, (int)(4 * kc + u));
-            const float y = colok ? (float)((double)x[u] * w) : 0.f;
+            const float y = colok ? x[u] * w[u] : 0.f;
             h[u] = tc::tf32_rn(y);
             l[u] = tc::tf32_rn(y - h[u]);
         }
@@ -165,18 +165,22 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
     } else if (warp >= kCvtWarp0 && warp < kCvtWarp0 + kCvtWarps) {
         // ---------------- converters (128 threads, 8 chunks of 16 B per tile each)
         const int ct = (warp - kCvtWarp0) * 32 + lane;
+        const int kc = (ct & 7) ^ ((ct >> 3) & 7);
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
             const int64_t irow = r0 + s * kTK + lane;
-            const double sv = (irow < r1) ? __ldg(srow + irow) : 0.0;   // issued before the wait
+            const float sv = (irow < r1) ? (float)__ldg(srow + irow) : 0.f;   // issued before the wait
+            float w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) w[u] = __shfl_sync(0xffffffffu, sv, 4 * kc + u);
             if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
                 atomicExch(err, 5);
                 break;
             }
             uint8_t* st = base + (size_t)slot * kStageAlloc;
-            split_tile(st, st + kOpBytes, sv, a0, k, ct);
-            if (!diag) split_tile(st + 2 * kOpBytes, st + 3 * kOpBytes, sv, b0, k, ct);
+            split_tile(st, st + kOpBytes, w, a0, k, ct);
+            if (!diag) split_tile(st + 2 * kOpBytes, st + 3 * kOpBytes, w, b0, k, ct);
             tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
