@@ -284,6 +284,14 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
     }
 }
 
+// Compensated (Kahan) FP32 accumulation: the running sum is s - c.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 // ---- streaming passes on the column-major FP32 factor FT (k x ldT) ------------
 // Reads are coalesced along rows; products are FP32 (round to nearest) and the
 // long sums over rows or columns are FP64.
@@ -387,7 +395,7 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j.  thread: columns 4 (tid >> 4)..+4,
+// CTA's rows, for a block of 64 columns j (FP32 products, compensated sums).  thread: columns 4 (tid >> 4)..+4,
 // U columns 2 (tid & 15)..+2.
 __global__ void __launch_bounds__(256)
 evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
@@ -399,7 +407,8 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
     const int64_t j0 = (int64_t)blockIdx.x * 64;
     const int64_t r0 = (int64_t)blockIdx.y * rows_per;
     const int64_t r1 = min(N, r0 + rows_per);
-    double acc64[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    float ks[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    float kc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
     for (int64_t i0 = r0; i0 < r1; i0 += 64) {
         __syncthreads();
         for (int e = tid; e < 64 * 64; e += 256) {
@@ -413,37 +422,32 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
             Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
         }
         __syncthreads();
-        float acc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
 #pragma unroll 8
         for (int ii = 0; ii < 64; ++ii) {
             const float w0 = Ws[ii][qc], w1 = Ws[ii][qc + 1];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const float f = Fs[jr + a][ii];
-                acc[a][0] = fmaf(f, w0, acc[a][0]);
-                acc[a][1] = fmaf(f, w1, acc[a][1]);
+                kahan_add(ks[a][0], kc[a][0], f * w0);
+                kahan_add(ks[a][1], kc[a][1], f * w1);
             }
-        }
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            acc64[a][0] += (double)acc[a][0];
-            acc64[a][1] += (double)acc[a][1];
         }
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int64_t j = j0 + jr + a;
         if (j >= k) continue;
+#pragma unroll
         for (int b = 0; b < 2; ++b) {
             const int q = qc + b;
-            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = acc64[a][b];
+            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] - (double)kc[a][b];
         }
     }
 }
 
 // Rayleigh-Ritz H and M partials over 256-row tiles: w_i = F_i (T1h + T1l)
 // (T1 as an FP32 hi/lo pair, k x 32), H += (w/sqrt(q))(w/sqrt(q))^T, M += u u^T.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 1)
 evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ T1hl,
               int m, const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
     __shared__ __align__(16) float Ts[2][32][32];   // hi, lo for a 32-row chunk of T1
@@ -453,9 +457,9 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
     const int64_t n_tiles = (N + 255) / 256;
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const int64_t i = t * 256 + tid;
-        float w[32];
+        float w[32], wc[32];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) w[q] = 0.f;
+        for (int q = 0; q < 32; ++q) w[q] = wc[q] = 0.f;
         for (int64_t j0 = 0; j0 < k; j0 += 32) {
             __syncthreads();
             for (int e = tid; e < 32 * 32; e += 256) {
@@ -474,10 +478,15 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
 #pragma unroll
                     for (int q4 = 0; q4 < 8; ++q4) {
                         const float4 a = th[q4], b = tl[q4];
-                        w[4 * q4 + 0] = fmaf(f, a.x, fmaf(f, b.x, w[4 * q4 + 0]));
-                        w[4 * q4 + 1] = fmaf(f, a.y, fmaf(f, b.y, w[4 * q4 + 1]));
-                        w[4 * q4 + 2] = fmaf(f, a.z, fmaf(f, b.z, w[4 * q4 + 2]));
-                        w[4 * q4 + 3] = fmaf(f, a.w, fmaf(f, b.w, w[4 * q4 + 3]));
+                        // hi products into the compensated sum, lo products into its correction
+                        kahan_add(w[4 * q4 + 0], wc[4 * q4 + 0], f * a.x);
+                        kahan_add(w[4 * q4 + 1], wc[4 * q4 + 1], f * a.y);
+                        kahan_add(w[4 * q4 + 2], wc[4 * q4 + 2], f * a.z);
+                        kahan_add(w[4 * q4 + 3], wc[4 * q4 + 3], f * a.w);
+                        wc[4 * q4 + 0] = fmaf(-f, b.x, wc[4 * q4 + 0]);
+                        wc[4 * q4 + 1] = fmaf(-f, b.y, wc[4 * q4 + 1]);
+                        wc[4 * q4 + 2] = fmaf(-f, b.z, wc[4 * q4 + 2]);
+                        wc[4 * q4 + 3] = fmaf(-f, b.w, wc[4 * q4 + 3]);
                     }
                 }
             }
@@ -485,15 +494,15 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
         __syncthreads();
         const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
 #pragma unroll
-        for (int q = 0; q < 32; ++q) Ws[tid][q] = (q < m) ? w[q] * sq : 0.f;
+        for (int q = 0; q < 32; ++q) Ws[tid][q] = (q < m) ? (w[q] - wc[q]) * sq : 0.f;
         __syncthreads();
 #pragma unroll
         for (int qq = 0; qq < 4; ++qq) {
             const int e = tid + 256 * qq;
             const int ja = e >> 5, jb = e & 31;
-            float hs = 0.f;
-            for (int rr = 0; rr < 256; ++rr) hs = fmaf(Ws[rr][ja], Ws[rr][jb], hs);
-            h64[qq] += (double)hs;
+            float hs = 0.f, hc = 0.f;
+            for (int rr = 0; rr < 256; ++rr) kahan_add(hs, hc, Ws[rr][ja] * Ws[rr][jb]);
+            h64[qq] += (double)hs - (double)hc;
         }
         __syncthreads();
         {
@@ -508,9 +517,9 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
         for (int qq = 0; qq < 4; ++qq) {
             const int e = tid + 256 * qq;
             const int ja = e >> 5, jb = e & 31;
-            float ms = 0.f;
-            for (int rr = 0; rr < 256; ++rr) ms = fmaf(Ws[rr][ja], Ws[rr][jb], ms);
-            m64[qq] += (double)ms;
+            float ms = 0.f, mc = 0.f;
+            for (int rr = 0; rr < 256; ++rr) kahan_add(ms, mc, Ws[rr][ja] * Ws[rr][jb]);
+            m64[qq] += (double)ms - (double)mc;
         }
     }
     double* out = partial + (int64_t)blockIdx.x * 2048;

@@ -54,6 +54,8 @@ struct Bars {
     uint64_t empty[kStages];
     uint64_t accf[kBufs];
     uint64_t acce[kBufs];
+    uint64_t kfull;     // K(R, S_i) tile landed
+    uint64_t kempty;    // epilogue done with the K tile
     uint64_t done;
     uint32_t tmem_base;
 };
@@ -72,8 +74,8 @@ struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
-update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F, int64_t ldF, int64_t N,
-                 const float* __restrict__ Kc, const float* __restrict__ minv_f, int b,
+update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmk,
+                 float* __restrict__ F, int64_t ldF, int64_t N, const float* __restrict__ minv_f, int b,
                  const uint8_t* __restrict__ bprep, const RoundView* st, double* __restrict__ dvec,
                  double* __restrict__ dblk, int* __restrict__ err) {
     if (st->done) return;
@@ -85,9 +87,10 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    float* mv = reinterpret_cast<float*>(base + (size_t)kStages * kStageBytes);   // kCols x kCols
-    float* kt = mv + kCols * kCols;              // kRows x (kCols + 1): K(R, S_i), then G
-    Bars* bar = reinterpret_cast<Bars*>(kt + kRows * (kCols + 1));
+    // K(R, S_i) tile: two 128 x 32 SWIZZLE_128B halves (TMA), then G in place
+    uint8_t* ktile = base + (size_t)kStages * kStageBytes;
+    float* mv = reinterpret_cast<float*>(ktile + 2 * kAOp);                      // kCols x kCols
+    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // L_i^{-1} (FP32) for the epilogue
@@ -105,6 +108,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
             tc::mbar_init(&bar->accf[t], 1);
             tc::mbar_init(&bar->acce[t], 128);
         }
+        tc::mbar_init(&bar->kfull, 1);
+        tc::mbar_init(&bar->kempty, 128);
         tc::mbar_init(&bar->done, 1);
         tc::mbar_fence_init();
     }
@@ -137,6 +142,18 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
                 }
             }
             if (!ok) atomicExch(err, 11);
+        } else if (lane == 1) {
+            // K(R, S_i) tiles, one per row block, single-buffered
+            int64_t it = 0;
+            for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x, ++it) {
+                if (!tc::mbar_wait(&bar->kempty, ((uint32_t)it & 1u) ^ 1u, kTimeoutNs)) {
+                    atomicExch(err, 16);
+                    break;
+                }
+                tc::mbar_arrive_expect_tx(&bar->kfull, 2 * kAOp);
+                tc::tma_load_2d(ktile, &tmk, 0, (int)(rb * kRows), &bar->kfull);
+                tc::tma_load_2d(ktile + kAOp, &tmk, 32, (int)(rb * kRows), &bar->kfull);
+            }
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -228,26 +245,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
         const int q = warp - 4;
         const int rloc = 32 * q + lane;
         int64_t g = 0;
+        int64_t kit = 0;
         bool ok = true;
         __shared__ double wsum[4];
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
-            // stage K(R, S_i) (contiguous 128 x 64 floats) into padded smem with
-            // coalesced loads; they complete while the block's MMAs run
             const int64_t row0 = rb * kRows;
-            {
-                const float4* src = reinterpret_cast<const float4*>(Kc + row0 * kCols);
-                const int64_t n4 = (min((int64_t)kRows, N - row0) * kCols) / 4;
-#pragma unroll 4
-                for (int e = rloc; e < kRows * kCols / 4; e += 128) {
-                    const float4 v = (e < n4) ? __ldg(src + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    const int rr = (4 * e) / kCols, cc = (4 * e) % kCols;
-                    float* dst = kt + rr * (kCols + 1) + cc;
-                    dst[0] = v.x;
-                    dst[1] = v.y;
-                    dst[2] = v.z;
-                    dst[3] = v.w;
-                }
-            }
             const int64_t i = row0 + rloc;
             const double d_old = (i < N) ? dvec[i] : 0.0;
             float acc[kCols];
@@ -276,14 +278,23 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");   // kt filled
+            if (ok && !tc::mbar_wait(&bar->kfull, (uint32_t)(kit & 1), kTimeoutNs)) {
+                atomicExch(err, 17);
+                ok = false;
+            }
             double nd = d_old;
-            float* krow = kt + rloc * (kCols + 1);
             if (ok && i < N) {
-                // T = K(i, S_i) - P  (K(:, S_i) precomputed by update_kcols_kernel)
+                // T = K(i, S_i) - P  (K(:, S_i) by update_kcols_kernel, TMA tile in smem)
 #pragma unroll
-                for (int c = 0; c < kCols; ++c) acc[c] = krow[c] - acc[c];
-                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc); G -> kt row
+                for (int c4 = 0; c4 < kCols / 4; ++c4) {
+                    const float4 kv = *reinterpret_cast<const float4*>(
+                        ktile + (c4 >> 3) * kAOp + tc::sw128_off((uint32_t)rloc, (uint32_t)(4 * (c4 & 7))));
+                    acc[4 * c4 + 0] = kv.x - acc[4 * c4 + 0];
+                    acc[4 * c4 + 1] = kv.y - acc[4 * c4 + 1];
+                    acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
+                    acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
+                }
+                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc); G -> own tile row
                 float sq = 0.f;
 #pragma unroll
                 for (int a = 0; a < kCols; ++a) {
@@ -292,23 +303,28 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ F
                         const float* ma = mv + a * kCols;
 #pragma unroll
                         for (int e = 0; e <= a; ++e) gsum = fmaf(acc[e], ma[e], gsum);
-                        krow[a] = gsum;
+                        *reinterpret_cast<float*>(ktile + (a >> 5) * kAOp +
+                                                  tc::sw128_off((uint32_t)rloc, (uint32_t)(a & 31))) = gsum;
                         sq = fmaf(gsum, gsum, sq);
                     }
                 }
                 nd = fmax(d_old - (double)sq, 0.0);
                 dvec[i] = nd;
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");   // G rows in kt
+            asm volatile("bar.sync 1, 128;" ::: "memory");   // G rows in the tile
             // coalesced store of the new columns: warp q writes rows q, q+4, ...
             if (ok) {
                 const int64_t nrows = min((int64_t)kRows, N - row0);
                 for (int rr = q; rr < nrows; rr += 4) {
                     float* frow = F + (row0 + rr) * ldF + r;
-                    const float* grow = kt + rr * (kCols + 1);
-                    for (int a = lane; a < nacc; a += 32) frow[a] = grow[a];
+                    for (int a = lane; a < nacc; a += 32)
+                        frow[a] = *reinterpret_cast<const float*>(
+                            ktile + (a >> 5) * kAOp + tc::sw128_off((uint32_t)rr, (uint32_t)(a & 31)));
                 }
             }
+            asm volatile("bar.sync 1, 128;" ::: "memory");   // tile consumed
+            tc::mbar_arrive(&bar->kempty);
+            ++kit;
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
@@ -422,8 +438,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + kCols * kCols * 4 + kRows * (kCols + 1) * 4 +
-                            sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + sizeof(Bars) + 1024;
 
 // Whether the tensor-core update can run for this factor layout.
 bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
@@ -461,6 +476,22 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     const RoundView* rv = static_cast<const RoundView*>(round_state);
     float* Kc = arena_get<float>(ctx, "utc.kc", (size_t)N * kCols, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
+    static thread_local const void* last_K = nullptr;
+    static thread_local int64_t last_KN = -1;
+    static thread_local CUtensorMap tmk;
+    if (Kc != last_K || N != last_KN) {
+        const cuuint64_t gdim[2] = {(cuuint64_t)kCols, (cuuint64_t)N};
+        const cuuint64_t gstride[1] = {(cuuint64_t)kCols * 4};
+        const cuuint32_t box[2] = {32, (cuuint32_t)kRows};
+        const cuuint32_t estr[2] = {1, 1};
+        CUresult cr = get_encode()(&tmk, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)Kc, gdim, gstride, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS)
+            return set_error(ctx, KEVD_ERR_CUDA, "update_tc: tensor map (K) encode failed (%d)", (int)cr);
+        last_K = Kc;
+        last_KN = N;
+    }
     {
         ProfScope ps(ctx, "rp_update_kcols", s);
         const size_t ksm = (size_t)(kRows + kCols) * (d + 1) * sizeof(float);
@@ -481,7 +512,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     const int grid = (int)std::min<int64_t>(nblk, ctx->num_sms);
     {
         ProfScope ps(ctx, "rp_update", s);
-        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, F, ldF, N, Kc, minv_f, b, bprep, rv, dvec, dblk,
+        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, tmk, F, ldF, N, minv_f, b, bprep, rv, dvec, dblk,
                                                           err);
         KEVD_LAUNCH(ctx);
     }
