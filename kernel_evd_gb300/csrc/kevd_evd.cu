@@ -761,7 +761,6 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     }
 
     // dense 1: shift, Cholesky A + sI = L L^T
-    ProfScope ps_dense(ctx, "dense_kxk", s);
     ev_trace_shift_kernel<<<1, 1024, 0, s>>>(A, k, trsh);
     KEVD_LAUNCH(ctx);
     KEVD_SOLVER(ctx, cusolverDnSetStream(ctx->solver, s));
