@@ -104,6 +104,19 @@ int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                    const double* scales, int32_t n_scales, double* sums,
                    void* stream);
 
+/* kevd_calibrate for callers that cannot allocate device memory (inside a CUDA
+ * graph capture or a stream callback, under a device-memory pool they do not
+ * own, or after an allocation freeze).  No reference counterpart.  Needs no
+ * context and allocates nothing: its scratch is a fixed device array of about
+ * 160 KB that every GPU loading the library keeps until exit.  Limits:
+ * n_scales <= 64 (KEVD_ERR_ARG beyond).  The first call on a device resolves
+ * the array's device address with that device current, so make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race.
+ * X: device; scales, sums: host. */
+int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d,
+                           const double* scales, int32_t n_scales,
+                           double* sums, void* stream);
+
 /* Host post-processing of ks_bandwidth.cu:612-642 in FP64:
  * logS[i] = log(2 sums[i]/NM + 1); slope[i-1] = centred difference at bw[i]
  * (n-2 values); idmax = first arg-max; eopt = bw[idmax+1];

@@ -65,6 +65,7 @@ SIGNATURES = {
     "kevd_hankel_rows": (C.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
     "kevd_kernel_block": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I64, _I64, _P, _I64, _I32, _P, _I64, _P]),
     "kevd_calibrate": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),
+    "kevd_calibrate_noalloc": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P]),
     "kevd_calibrate_select": (C.c_int, [_P, _P, _I32, _I64, _P, _P, _P, _P, _P]),
     "kevd_pair_median": (C.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P]),
     "kevd_rpchol": (C.c_int, [_P, _P, _I64, _I32, _D, C.POINTER(RpcholParams), _P, _I64, _P, _P, _P,

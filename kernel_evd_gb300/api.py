@@ -121,6 +121,18 @@ def calibrate(ctx: Context, X: torch.Tensor, scales) -> np.ndarray:
     return sums
 
 
+def calibrate_noalloc(X: torch.Tensor, scales) -> np.ndarray:
+    """calibrate() without a context or any device allocation (fixed device
+    scratch; at most 64 scales; concurrent calls on one GPU race)."""
+    _need_cuda(X, torch.float32, "X")
+    scales = np.ascontiguousarray(scales, dtype=np.float64)
+    sums = np.zeros(scales.size, dtype=np.float64)
+    N, d = X.shape
+    check(_lib.load().kevd_calibrate_noalloc(_ptr(X), N, d, _np_ptr(scales), scales.size, _np_ptr(sums),
+                                             _stream()))
+    return sums
+
+
 def select_bandwidth(bw, sums, NM: int) -> dict:
     """ks_bandwidth.cu:612-642: logS, centred slope, first arg-max, eopt, mdim."""
     lib = _lib.load()

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace kevd {
@@ -176,6 +177,91 @@ int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double*
     KEVD_LAUNCH(ctx);
     KEVD_CUDA(ctx, cudaMemcpyAsync(sums, out, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s));
     KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    return KEVD_OK;
+}
+
+// ---- calibration without allocation -------------------------------------
+// Some callers cannot allocate device memory at all: code running inside a
+// CUDA graph capture or another library's stream callback, processes whose
+// device memory is fully reserved by a pool they do not own, and hosts that
+// forbid allocation after start-up.  For them the pair-sum sweep has a variant
+// whose scratch (per-CTA FP64 partials, the device copy of the scales and the
+// reduced sums) lives in fixed file-scope device arrays instead of workspace
+// buffers.  Limits: at most kNaMaxScales scales per call and a grid of at most
+// kNaGrid CTAs (about 160 KB held by every GPU that loads the library, until
+// the process exits).  Each call overwrites every entry it reads, so no entry
+// has to start at zero; calls share the arrays, so calls that overlap on the
+// GPU (different streams, or several host threads) race.
+constexpr int kNaMaxScales = 64;
+constexpr int kNaGrid = 304;
+static __device__ __align__(256) double g_na_partial[kNaGrid * kNaMaxScales];
+static __device__ __align__(256) float g_na_scales[kNaMaxScales];
+static __device__ __align__(256) double g_na_sums[kNaMaxScales];
+
+struct NoAllocScratch {
+    double* partial = nullptr;
+    float* scales = nullptr;
+    double* sums = nullptr;
+};
+
+// Device addresses of the arrays, resolved once per device with that device
+// current (a host-side use of the symbols would be a host stand-in, not a
+// device address).
+static int noalloc_scratch(NoAllocScratch* out) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static bool ready[kMaxDevices] = {};
+    static NoAllocScratch table[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return KEVD_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ready[dev]) {
+        NoAllocScratch t;
+        if (cudaGetSymbolAddress((void**)&t.partial, g_na_partial) != cudaSuccess ||
+            cudaGetSymbolAddress((void**)&t.scales, g_na_scales) != cudaSuccess ||
+            cudaGetSymbolAddress((void**)&t.sums, g_na_sums) != cudaSuccess) {
+            cudaGetLastError();
+            return KEVD_ERR_CUDA;
+        }
+        table[dev] = t;
+        ready[dev] = true;
+    }
+    *out = table[dev];
+    return KEVD_OK;
+}
+
+int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales, int n_scales, double* sums,
+                          cudaStream_t s) {
+    if (!X || !scales || !sums || N < 1 || d < 1 || d > kCalMaxD || n_scales < 1 || n_scales > kNaMaxScales)
+        return KEVD_ERR_ARG;
+    for (int j = 0; j < n_scales; ++j)
+        if (!(scales[j] > 0.0)) return KEVD_ERR_ARG;
+    NoAllocScratch sc;
+    const int rc = noalloc_scratch(&sc);
+    if (rc != KEVD_OK) return rc;
+    float hc[kNaMaxScales];
+    for (int j = 0; j < n_scales; ++j) hc[j] = (float)(scales[j] * 1.4426950408889634);
+    const int64_t nt = (N + kCalTile - 1) / kCalTile;
+    const int64_t n_tiles = nt * (nt + 1) / 2;
+    const int grid = (int)std::min<int64_t>(n_tiles, kNaGrid);
+    const size_t smem = calib_smem(d);
+    if (cudaMemcpyAsync(sc.scales, hc, n_scales * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaFuncSetAttribute(calibrate_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return KEVD_ERR_CUDA;
+    }
+    calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, sc.scales, n_scales, n_tiles, sc.partial);
+    reduce_partials_kernel<<<1, kCalMaxScales, 0, s>>>(sc.partial, grid, n_scales, sc.sums);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(sums, sc.sums, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return KEVD_ERR_CUDA;
+    }
     return KEVD_OK;
 }
 

@@ -193,6 +193,11 @@ int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, const do
     return run_calibrate(ctx, X, N, d, scales, n_scales, sums, as_stream(stream));
 }
 
+int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d, const double* scales, int32_t n_scales,
+                           double* sums, void* stream) {
+    return run_calibrate_noalloc(X, N, d, scales, n_scales, sums, as_stream(stream));
+}
+
 int kevd_calibrate_select(const double* bw, const double* sums, int32_t n, int64_t NM,
                           double* logS, double* slope, int32_t* idmax, double* eopt,
                           double* mdim) {

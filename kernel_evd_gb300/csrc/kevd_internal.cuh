@@ -161,6 +161,8 @@ int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double 
                         const float* Xc = nullptr);
 int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
                   int n_scales, double* sums, cudaStream_t s);
+int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales, int n_scales, double* sums,
+                          cudaStream_t s);
 int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64_t* pi,
                     const int64_t* pl, int64_t n_pairs, double* median, cudaStream_t s);
 int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
