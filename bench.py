@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--kout", type=int, default=32)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--cpu-rows", type=int, default=40000, help="row sample of the CPU baseline")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     return ap.parse_args()
 
 
@@ -262,6 +263,19 @@ def main():
             np.linalg.norm(U_mixed, axis=0) * np.linalg.norm(U64h, axis=0))
         ang = np.arccos(np.clip(c, 0, 1))
         same = int(np.argmax(fac.piv != fac64.piv)) if np.any(fac.piv != fac64.piv) else int(fac.rank)
+        # precision of the mixed EVD alone: FP64 factor and EVD of the mixed run's own pivots
+        F64.zero_()
+        f64s = api.factor_from_pivots(ctx, Xd, scale, fac.piv, precision="fp64", F=F64[:, : fac.rank])
+        ev64s = api.bistochastic_evd(ctx, f64s, k_out=args.kout, U=U64)
+        lam_err_s = np.abs(lam_mixed[-top:] - ev64s.lam[-top:])
+        U64s = U64.cpu().numpy().astype(np.float64)
+        cs = np.abs(np.einsum("ij,ij->j", U_mixed, U64s)) / (
+            np.linalg.norm(U_mixed, axis=0) * np.linalg.norm(U64s, axis=0))
+        ang_s = np.arccos(np.clip(cs, 0, 1))
+        result["same_pivots_fp64"] = {"top_eig_abs_err_max": float(lam_err_s.max()),
+                                      "top_eig_abs_err_leading8": [float(x) for x in lam_err_s[::-1][:8]],
+                                      "eigvec_angle_max_rad": float(ang_s.max()),
+                                      "eigvec_angle_leading4_rad": [float(x) for x in ang_s[::-1][:4]]}
         result["fp64"] = {"seconds": fp64_ms / 1e3, "speedup_mixed_vs_fp64": fp64_ms / ms,
                           "trace_error": fac64.trace_error, "rank": fac64.rank,
                           "top_eig_abs_err_max": float(lam_err.max()),
@@ -303,7 +317,7 @@ def main():
         roofline = dict(roofline, kernel=dom)
     # --- CPU baseline on rank 0 (bounded sample)
     cpu = None
-    if rank == 0 and ws == 1:
+    if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import baseline
         n_s = min(args.cpu_rows, N)
         tb = baseline.timed_pipeline(X[:n_s], scale, args.k, args.b, args.kout)

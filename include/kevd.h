@@ -217,6 +217,16 @@ int kevd_factor_from_linv(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                           const double* Linv, int32_t precision, void* F,
                           int64_t ldF, void* stream);
 
+/* Nystrom factor of a given pivot set in FP64 arithmetic: F = K(:,S) L^{-T}
+ * with L L^T = K(S,S) (ks_arpclm.cu's factor for the accepted pivots,
+ * README_arpclm.md:21-47), written as double (KEVD_FP64) or rounded to float
+ * (KEVD_MIXED).  Used to compare a mixed-precision run against the FP64 EVD of
+ * the same pivots.  piv: host; F: device N x ldF. */
+int kevd_factor_from_pivots(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                            double scale, const int64_t* piv, int64_t r,
+                            int32_t precision, void* F, int64_t ldF,
+                            void* stream);
+
 /* Out-of-sample (Nystrom) eigenfunctions of new states Y (device, n x d):
  * Uy[j,:] = (K(y_j,S) Z') / (K(y_j,S) p1'), the pass-4 formula
  * (ks_kevd.cu:2246-2269) applied to new rows; the model (landmarks S, Z', p1')

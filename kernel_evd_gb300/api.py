@@ -252,6 +252,22 @@ def factor_from_linv(ctx: Context, X: torch.Tensor, scale: float, piv, Linv: np.
     return F
 
 
+def factor_from_pivots(ctx: Context, X: torch.Tensor, scale: float, piv, precision="fp64",
+                       F: torch.Tensor | None = None) -> torch.Tensor:
+    """F = K(:, S) L^{-T}, L L^T = K(S, S), in FP64 arithmetic for the given pivots."""
+    _need_cuda(X, torch.float32, "X")
+    N, d = X.shape
+    p = _prec(precision)
+    piv = np.ascontiguousarray(piv, dtype=np.int64)
+    r = piv.size
+    dt = torch.float64 if p == KEVD_FP64 else torch.float32
+    if F is None:
+        F = torch.empty((N, r), dtype=dt, device=X.device)
+    ctx._check(ctx.lib.kevd_factor_from_pivots(ctx.h, _ptr(X), N, d, float(scale), _np_ptr(piv), r, p, _ptr(F),
+                                               F.stride(0), _stream()))
+    return F
+
+
 # ---- stage 3 ---------------------------------------------------------------
 @dataclass
 class Eigendecomposition:

@@ -2,6 +2,7 @@
 // workspace management, and the host orchestration that is not a kernel.
 #include "kevd_internal.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <iterator>
 #include <cstdarg>
@@ -311,6 +312,56 @@ int kevd_factor_from_linv(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, d
         if (precision == KEVD_MIXED) {
             const int grid = (int)std::min<int64_t>((nr * r + 255) / 256, (int64_t)ctx->num_sms * 16);
             cast_d2f_kernel<<<grid, 256, 0, s>>>(Fp, nr, r, r, (float*)F + r0 * ldF, ldF);
+            KEVD_LAUNCH(ctx);
+        }
+    }
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    return KEVD_OK;
+}
+
+int kevd_factor_from_pivots(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, double scale,
+                            const int64_t* piv, int64_t r, int32_t precision, void* F, int64_t ldF,
+                            void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    if (!X || !piv || !F || N < 1 || r < 1 || r > N || ldF < r ||
+        (precision != KEVD_FP64 && precision != KEVD_MIXED))
+        return set_error(ctx, KEVD_ERR_ARG, "factor_from_pivots: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    int64_t rows = std::max<int64_t>(1, (256ll << 20) / (r * 8));
+    rows = std::min(rows, N);
+    int st = KEVD_OK;
+    int64_t* idx = arena_get<int64_t>(ctx, "fp.idx", r, &st);
+    double* L = arena_get<double>(ctx, "fp.L", (size_t)r * r, &st);
+    double* Kp = arena_get<double>(ctx, "fp.K", (size_t)rows * r, &st);
+    int* info = arena_get<int>(ctx, "fp.info", 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "factor_from_pivots: out of device memory");
+    KEVD_CUDA(ctx, cudaMemcpyAsync(idx, piv, r * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    // L L^T = K(S, S): row-major K(S,S) is its own column-major transpose (symmetric)
+    KEVD_TRY(launch_kernel_block(ctx, X, N, d, scale, idx, 0, r, idx, r, KEVD_FP64, L, r, s));
+    KEVD_SOLVER(ctx, cusolverDnSetStream(ctx->solver, s));
+    KEVD_BLAS(ctx, cublasSetStream(ctx->blas, s));
+    int lwork = 0;
+    KEVD_SOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)r, L, (int)r, &lwork));
+    double* work = arena_get<double>(ctx, "fp.work", (size_t)lwork + 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "factor_from_pivots: out of device memory");
+    KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)r, L, (int)r, work, lwork, info));
+    int hinfo = 0;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    if (hinfo != 0) return set_error(ctx, KEVD_ERR_POTRF, "factor_from_pivots: K(S,S) not positive definite (%d)", hinfo);
+    const double one = 1.0;
+    for (int64_t r0 = 0; r0 < N; r0 += rows) {
+        const int64_t nr = std::min(rows, N - r0);
+        KEVD_TRY(launch_kernel_block(ctx, X, N, d, scale, nullptr, r0, nr, idx, r, KEVD_FP64, Kp, r, s));
+        // (F panel)^T solves L Y = K(R,S)^T (column-major r x nr)
+        KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                   CUBLAS_DIAG_NON_UNIT, (int)r, (int)nr, &one, L, (int)r, Kp, (int)r));
+        if (precision == KEVD_FP64) {
+            KEVD_CUDA(ctx, cudaMemcpy2DAsync((double*)F + r0 * ldF, ldF * sizeof(double), Kp, r * sizeof(double),
+                                             r * sizeof(double), nr, cudaMemcpyDeviceToDevice, s));
+        } else {
+            const int grid = (int)std::min<int64_t>((nr * r + 255) / 256, (int64_t)ctx->num_sms * 16);
+            cast_d2f_kernel<<<grid, 256, 0, s>>>(Kp, nr, r, r, (float*)F + r0 * ldF, ldF);
             KEVD_LAUNCH(ctx);
         }
     }

@@ -1,11 +1,11 @@
 // Weighted Gram G = Y^T Y, Y = diag(s) F, of an FP32 factor on the tcgen05
 // tensor cores (the A and B Grams of the bistochastic EVD).
 //
-// Precision: 4xTF32.  Each element y is split as hi = rn_tf32(y) and
+// Precision: 3xTF32.  Each element y is split as hi = rn_tf32(y) and
 // lo = rn_tf32(y - hi) (both exact tf32 values, so every product is exact in
 // FP32 and the split error is unbiased, about 2^-23 |y|); a 128 x 128 output
-// tile accumulates lo_a lo_b^T + hi_a lo_b^T + lo_a hi_b^T + hi_a hi_b^T in
-// FP32 in Tensor Memory.  The tensor-core accumulator rounds each update
+// tile accumulates hi_a lo_b^T + lo_a hi_b^T + hi_a hi_b^T in FP32 in Tensor
+// Memory (the dropped lo_a lo_b^T is about 2^-24 relative and of random sign).  The tensor-core accumulator rounds each update
 // with a one-sided bias, so the FP32 partial is kept short: every 1024 rows it
 // is added into an FP64 tile in global memory and the long sum over N rows is
 // FP64 (the Gram accumulators of the reference are FP64,
@@ -220,8 +220,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                         const uint64_t dal = tc::desc_kmajor_sw128(alo + koff);
                         const uint64_t dbh = tc::desc_kmajor_sw128(bhi + koff);
                         const uint64_t dbl = tc::desc_kmajor_sw128(blo + koff);
-                        tc::mma_tf32(d, dal, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
-                        tc::mma_tf32(d, dah, dbl, idesc, 1u);
+                        tc::mma_tf32(d, dah, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
                         tc::mma_tf32(d, dal, dbh, idesc, 1u);
                         tc::mma_tf32(d, dah, dbh, idesc, 1u);
                     }

@@ -265,16 +265,16 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     continue;
                 }
                 tc::tc_fence_after();
-                float v[32];
+                float v[32], v2[32];
                 const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kCols);
-                tc::tmem_ld32(ta, v);
+                tc::tmem_ld32(ta, v);          // both halves in flight, one wait
+                tc::tmem_ld32(ta + 32, v2);
                 tc::tmem_wait_ld();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) acc[j] += v[j];
-                tc::tmem_ld32(ta + 32, v);
-                tc::tmem_wait_ld();
-#pragma unroll
-                for (int j = 0; j < 32; ++j) acc[32 + j] += v[j];
+                for (int j = 0; j < 32; ++j) {
+                    acc[j] += v[j];
+                    acc[32 + j] += v2[j];
+                }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
             }

@@ -104,3 +104,10 @@ def test_nystrom_reproduces_training_rows(ctx, fac):
     Uy = model(Xt[torch.from_numpy(idx).cuda()].contiguous()).cpu().numpy()
     U = e.U.cpu().numpy()[idx]
     np.testing.assert_allclose(Uy, U, rtol=0, atol=1e-5 * np.abs(U).max())
+
+
+def test_factor_from_pivots_matches_oracle(ctx, fac):
+    from kernel_evd_gb300 import api
+    X, r = fac
+    F = api.factor_from_pivots(ctx, torch.from_numpy(X).cuda(), SCALE, r["piv"][:200]).cpu().numpy()
+    np.testing.assert_allclose(F, r["F"][:, :200], rtol=0, atol=1e-9)

@@ -26,8 +26,8 @@ def test_gram_tc_fp32_factor(ctx, N, k, ld):
     R = _ref(Fb[:, :k], s)
     scale = np.sqrt(np.outer(np.diag(R), np.diag(R)))
     err = np.abs(G - R) / scale
-    # 4xTF32 products are exact; the tensor-core FP32 accumulator over 1024-row
-    # chunks limits the relative error (FP64 across chunks)
+    # 3xTF32 products (exact hi/lo pieces); the tensor-core FP32 accumulator over
+    # 1024-row chunks limits the relative error (FP64 across chunks)
     assert err.max() < 3e-5, err.max()
     np.testing.assert_allclose(G, G.T, rtol=0, atol=0)
 
