@@ -296,33 +296,34 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 // Reads are coalesced along rows; products are FP32 (round to nearest) and the
 // long sums over rows or columns are FP64.
 
-// c[j] = sum_i w_i FT[j][i]  (w == nullptr: ones).  One CTA per column.
-__global__ void __launch_bounds__(256)
-evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, const double* __restrict__ w,
-                  double* __restrict__ c) {
-    const int64_t j = blockIdx.x;
-    const float* col = FT + j * ldT;
+// Partial column sums c[j] = sum_i w_i FT[j][i] (w == nullptr: ones) over this
+// CTA's row range.  CTA = 16 warps = 16 columns; the weights of each 2048-row
+// chunk are staged once in shared memory for all 16 columns; each lane sums 64
+// products in FP32, chunks are added in FP64.
+__global__ void __launch_bounds__(512)
+evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ w,
+                  int64_t rows_per, double* __restrict__ partial) {
+    __shared__ float ws[2048];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t j = (int64_t)blockIdx.x * 16 + warp;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per;
+    const int64_t r1 = min(N, r0 + rows_per);
     double acc = 0.0;
-    float part = 0.f;
-    int cnt = 0;
-    for (int64_t i = threadIdx.x; i < N; i += 256) {
-        const float f = col[i];
-        part = w ? fmaf(f, (float)w[i], part) : part + f;
-        if (++cnt == 64) {
+    for (int64_t i0 = r0; i0 < r1; i0 += 2048) {
+        const int n = (int)min((int64_t)2048, r1 - i0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < n; t += 512) ws[t] = w ? (float)w[i0 + t] : 1.f;
+        __syncthreads();
+        if (j < k) {
+            const float* col = FT + j * ldT + i0;
+            float part = 0.f;
+            for (int t = lane; t < n; t += 32) part = fmaf(col[t], ws[t], part);
             acc += (double)part;
-            part = 0.f;
-            cnt = 0;
         }
     }
-    acc += (double)part;
-    __shared__ double red[256];
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) c[j] = red[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0 && j < k) partial[(int64_t)blockIdx.y * k + j] = acc;
 }
 
 // y_i = sum_j FT[j][i] v_j with v split into an FP32 hi/lo pair; FP64 every 32
@@ -372,17 +373,22 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
         }
         __syncthreads();
         if (i < N) {
-            const int64_t jn = min((int64_t)128, k - j0);
-            for (int jj = 0; jj < jn; ++jj) {
-                const float f = FT[(j0 + jj) * ldT + i];
-                const float4* zr = reinterpret_cast<const float4*>(Zs[jj]);
+            const int jn = (int)min((int64_t)128, k - j0);
+            for (int jj = 0; jj < jn; jj += 4) {
+                float f[4];
 #pragma unroll
-                for (int q4 = 0; q4 < 8; ++q4) {
-                    const float4 z = zr[q4];
-                    acc[4 * q4 + 0] = fmaf(f, z.x, acc[4 * q4 + 0]);
-                    acc[4 * q4 + 1] = fmaf(f, z.y, acc[4 * q4 + 1]);
-                    acc[4 * q4 + 2] = fmaf(f, z.z, acc[4 * q4 + 2]);
-                    acc[4 * q4 + 3] = fmaf(f, z.w, acc[4 * q4 + 3]);
+                for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4* zr = reinterpret_cast<const float4*>(Zs[jj + u]);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                        const float4 z = zr[q4];
+                        acc[4 * q4 + 0] = fmaf(f[u], z.x, acc[4 * q4 + 0]);
+                        acc[4 * q4 + 1] = fmaf(f[u], z.y, acc[4 * q4 + 1]);
+                        acc[4 * q4 + 2] = fmaf(f[u], z.z, acc[4 * q4 + 2]);
+                        acc[4 * q4 + 3] = fmaf(f[u], z.w, acc[4 * q4 + 3]);
+                    }
                 }
             }
         }
@@ -470,25 +476,32 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
             }
             __syncthreads();
             if (i < N) {
+                // 32 products per column in FP32 (hi and lo parts of T1), then one
+                // compensated add of the chunk sum
                 const int jn = (int)min((int64_t)32, k - j0);
-                for (int jj = 0; jj < jn; ++jj) {
-                    const float f = FT[(j0 + jj) * ldT + i];
-                    const float4* th = reinterpret_cast<const float4*>(Ts[0][jj]);
-                    const float4* tl = reinterpret_cast<const float4*>(Ts[1][jj]);
+                float part[32];
 #pragma unroll
-                    for (int q4 = 0; q4 < 8; ++q4) {
-                        const float4 a = th[q4], b = tl[q4];
-                        // hi products into the compensated sum, lo products into its correction
-                        kahan_add(w[4 * q4 + 0], wc[4 * q4 + 0], f * a.x);
-                        kahan_add(w[4 * q4 + 1], wc[4 * q4 + 1], f * a.y);
-                        kahan_add(w[4 * q4 + 2], wc[4 * q4 + 2], f * a.z);
-                        kahan_add(w[4 * q4 + 3], wc[4 * q4 + 3], f * a.w);
-                        wc[4 * q4 + 0] = fmaf(-f, b.x, wc[4 * q4 + 0]);
-                        wc[4 * q4 + 1] = fmaf(-f, b.y, wc[4 * q4 + 1]);
-                        wc[4 * q4 + 2] = fmaf(-f, b.z, wc[4 * q4 + 2]);
-                        wc[4 * q4 + 3] = fmaf(-f, b.w, wc[4 * q4 + 3]);
+                for (int q = 0; q < 32; ++q) part[q] = 0.f;
+                for (int jj = 0; jj < jn; jj += 4) {
+                    float f[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float4* th = reinterpret_cast<const float4*>(Ts[0][jj + u]);
+                        const float4* tl = reinterpret_cast<const float4*>(Ts[1][jj + u]);
+#pragma unroll
+                        for (int q4 = 0; q4 < 8; ++q4) {
+                            const float4 a = th[q4], b = tl[q4];
+                            part[4 * q4 + 0] = fmaf(f[u], a.x, fmaf(f[u], b.x, part[4 * q4 + 0]));
+                            part[4 * q4 + 1] = fmaf(f[u], a.y, fmaf(f[u], b.y, part[4 * q4 + 1]));
+                            part[4 * q4 + 2] = fmaf(f[u], a.z, fmaf(f[u], b.z, part[4 * q4 + 2]));
+                            part[4 * q4 + 3] = fmaf(f[u], a.w, fmaf(f[u], b.w, part[4 * q4 + 3]));
+                        }
                     }
                 }
+#pragma unroll
+                for (int q = 0; q < 32; ++q) kahan_add(w[q], wc[q], part[q]);
             }
         }
         __syncthreads();
@@ -567,14 +580,17 @@ __global__ void rr_rotate_kernel(float* __restrict__ U, int64_t N, int m, const 
     for (int e = threadIdx.x; e < m * m; e += blockDim.x) Cs[e] = C[e];
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        float u[32], v[32];
-        for (int j = 0; j < m; ++j) u[j] = U[i * m + j];
+        float u[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) u[j] = (j < m) ? U[i * m + j] : 0.f;
+#pragma unroll 1
         for (int j = 0; j < m; ++j) {
-            double s = 0.0;
-            for (int q = 0; q < m; ++q) s += (double)u[q] * Cs[j * m + q];
-            v[j] = (float)s;
+            float s = 0.f;
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                if (q < m) s = fmaf(u[q], (float)Cs[j * m + q], s);
+            U[i * m + j] = s;
         }
-        for (int j = 0; j < m; ++j) U[i * m + j] = v[j];
     }
 }
 
@@ -717,11 +733,20 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
         KEVD_CUDA(ctx, cudaFuncSetAttribute(evt_rowdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)std::max(vsm, (size_t)1024)));
         ProfScope ps(ctx, "ev_passes", s);
-        evt_colsum_kernel<<<(int)k, 256, 0, s>>>(FT, ldT, N, nullptr, c1);
+        const int ny = (int)std::min<int64_t>(16, std::max<int64_t>(1, N / 8192));
+        const int64_t rows_per = (N + ny - 1) / ny;
+        double* cpart = arena_get<double>(ctx, "ev.cpartT", (size_t)ny * k, &st);
+        if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+        const dim3 cgrid(ceil_div(k, 16), ny);
+        evt_colsum_kernel<<<cgrid, 512, 0, s>>>(FT, ldT, N, k, nullptr, rows_per, cpart);
+        KEVD_LAUNCH(ctx);
+        ev_sum_partials_kernel<<<ceil_div(k, 256), 256, 0, s>>>(cpart, ny, k, c1);
         KEVD_LAUNCH(ctx);
         evt_rowdot_kernel<<<ceil_div(N, 256), 256, vsm, s>>>(FT, ldT, N, k, c1, dtil, dinv, flags + 0);
         KEVD_LAUNCH(ctx);
-        evt_colsum_kernel<<<(int)k, 256, 0, s>>>(FT, ldT, N, dinv, cq);
+        evt_colsum_kernel<<<cgrid, 512, 0, s>>>(FT, ldT, N, k, dinv, rows_per, cpart);
+        KEVD_LAUNCH(ctx);
+        ev_sum_partials_kernel<<<ceil_div(k, 256), 256, 0, s>>>(cpart, ny, k, cq);
         KEVD_LAUNCH(ctx);
         evt_rowdot_kernel<<<ceil_div(N, 256), 256, vsm, s>>>(FT, ldT, N, k, cq, qtil, qinv, flags + 1);
         KEVD_LAUNCH(ctx);

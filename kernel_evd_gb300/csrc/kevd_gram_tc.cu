@@ -166,11 +166,14 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
         // ---------------- converters (128 threads, 8 chunks of 16 B per tile each)
         const int ct = (warp - kCvtWarp0) * 32 + lane;
         const int kc = (ct & 7) ^ ((ct >> 3) & 7);
+        // row weights one stage ahead of their use
+        float sv_next = (r0 + lane < r1) ? (float)__ldg(srow + r0 + lane) : 0.f;
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
-            const int64_t irow = r0 + s * kTK + lane;
-            const float sv = (irow < r1) ? (float)__ldg(srow + irow) : 0.f;   // issued before the wait
+            const float sv = sv_next;
+            const int64_t inext = r0 + (s + 1) * kTK + lane;
+            sv_next = (inext < r1) ? (float)__ldg(srow + inext) : 0.f;
             float w[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) w[u] = __shfl_sync(0xffffffffu, sv, 4 * kc + u);
