@@ -476,13 +476,13 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
             }
             __syncthreads();
             if (i < N) {
-                // 32 products per column in FP32 (hi and lo parts of T1), then one
-                // compensated add of the chunk sum
+                // 4 rows x (hi, lo) products per column in FP32, then one compensated
+                // add of that 8-term sum
                 const int jn = (int)min((int64_t)32, k - j0);
-                float part[32];
-#pragma unroll
-                for (int q = 0; q < 32; ++q) part[q] = 0.f;
                 for (int jj = 0; jj < jn; jj += 4) {
+                    float part[32];
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) part[q] = 0.f;
                     float f[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
@@ -499,9 +499,9 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
                             part[4 * q4 + 3] = fmaf(f[u], a.w, fmaf(f[u], b.w, part[4 * q4 + 3]));
                         }
                     }
-                }
 #pragma unroll
-                for (int q = 0; q < 32; ++q) kahan_add(w[q], wc[q], part[q]);
+                    for (int q = 0; q < 32; ++q) kahan_add(w[q], wc[q], part[q]);
+                }
             }
         }
         __syncthreads();

@@ -37,6 +37,7 @@ namespace {
 constexpr int kTT = 128;               // output tile edge
 constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
 constexpr int kStages = 3;
+constexpr int kPrefetch = 6;          // stages of F prefetched into L2 ahead of the ring
 constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
 constexpr int kStageBytes = 4 * kOpBytes;   // a_hi, a_lo, b_hi, b_lo
@@ -156,6 +157,11 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                 }
                 uint8_t* st = base + (size_t)slot * kStageAlloc;
                 const int x = (int)(r0 + s * kTK);
+                if (s + kPrefetch < n_stages) {
+                    const int xp = (int)(r0 + (s + kPrefetch) * kTK);
+                    tc::tma_prefetch_2d(&tmF, xp, (int)a0);
+                    if (!diag) tc::tma_prefetch_2d(&tmF, xp, (int)b0);
+                }
                 tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
                 tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
                 if (!diag) tc::tma_load_2d(st + 2 * kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);

@@ -74,6 +74,14 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
         : "memory");
 }
 
+// Prefetch the box at (x, y) of the tensor map into L2 (no shared memory, no
+// completion tracking): lowers the latency of a later tma_load_2d of that box.
+__device__ __forceinline__ void tma_prefetch_2d(const void* tmap, int x, int y) {
+    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"((uint64_t)tmap), "r"(x),
+                 "r"(y)
+                 : "memory");
+}
+
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* tmap, int x, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];" ::"r"(

@@ -10,10 +10,10 @@
 //
 // Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
 // lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
-// stage accumulates hi_a hi_b + hi_a lo_b + lo_a hi_b in a fresh TMEM partial
-// (12 MMA updates), and the epilogue sums the stage partials in FP32 registers
-// with round-to-nearest, so the tensor-core accumulator's rounding bias never
-// builds up over r.
+// stage accumulates hi_a hi_b + hi_a lo_b + lo_a hi_b; every two stages use a
+// fresh TMEM partial (24 MMA updates), and the epilogue sums the partials in
+// FP32 registers with round-to-nearest, so the tensor-core accumulator's
+// rounding bias never builds up over r.
 //
 // CTA (320 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
@@ -40,7 +40,9 @@ constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
 constexpr int kStages = 3;
+constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
 constexpr int kBufs = 8;            // TMEM partial buffers (8 x 64 = all 512 columns)
+constexpr int kPerPartial = 2;      // 32-column stages accumulated per TMEM partial
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
 constexpr int kStageBytes = 2 * kAOp + 2 * kBOp;   // a_hi, a_lo, b_hi, b_lo
@@ -136,6 +138,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         break;
                     }
                     uint8_t* stg = base + (size_t)slot * kStageBytes;
+                    {   // L2 prefetch kPrefetch stages ahead (possibly in the next row block)
+                        const int sp = s + kPrefetch;
+                        const int64_t rbp = rb + (int64_t)(sp / n_st) * gridDim.x;
+                        if (rbp < nblk) tc::tma_prefetch_2d(&tmap, (sp % n_st) * kKs, (int)(rbp * kRows));
+                    }
                     tc::mbar_arrive_expect_tx(&bar->tma_full[slot], kAOp + 2 * kBOp);
                     tc::tma_load_2d(stg, &tmap, s * kKs, (int)(rb * kRows), &bar->tma_full[slot]);
                     tc::bulk_load(stg + 2 * kAOp, bprep + (size_t)s * 2 * kBOp, 2 * kBOp, &bar->tma_full[slot]);
@@ -160,15 +167,17 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // ---------------- MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
-            int64_t g = 0;
+            int64_t g = 0, pg = 0;
             bool ok = true;
             for (int64_t rb = blockIdx.x; rb < nblk && ok; rb += gridDim.x) {
                 for (int s = 0; s < n_st; ++s, ++g) {
                     const int slot = (int)(g % kStages);
                     const uint32_t use = (uint32_t)(g / kStages);
-                    const int tb = (int)(g % kBufs);
-                    const uint32_t tuse = (uint32_t)(g / kBufs);
-                    if (!tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs) ||
+                    const int tb = (int)(pg % kBufs);
+                    const uint32_t tuse = (uint32_t)(pg / kBufs);
+                    const bool first = (s % kPerPartial) == 0;
+                    const bool last = (s % kPerPartial) == kPerPartial - 1 || s == n_st - 1;
+                    if ((first && !tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs)) ||
                         !tc::mbar_wait(&bar->cvt_full[slot], use & 1u, kTimeoutNs)) {
                         ok = false;
                         break;
@@ -185,12 +194,15 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         const uint64_t dal = tc::desc_kmajor_sw128(alo + ko);
                         const uint64_t dbh = tc::desc_kmajor_sw128(bhi + ko);
                         const uint64_t dbl = tc::desc_kmajor_sw128(blo + ko);
-                        tc::mma_tf32(dt, dal, dbh, idesc, j > 0 ? 1u : 0u);
+                        tc::mma_tf32(dt, dal, dbh, idesc, (j > 0 || !first) ? 1u : 0u);
                         tc::mma_tf32(dt, dah, dbl, idesc, 1u);
                         tc::mma_tf32(dt, dah, dbh, idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[slot]);
-                    tc::mma_commit(&bar->accf[tb]);
+                    if (last) {
+                        tc::mma_commit(&bar->accf[tb]);
+                        ++pg;
+                    }
                 }
             }
             if (!ok) atomicExch(err, 12);
@@ -244,6 +256,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // row blocks, so all four warps meet the same named barriers.
         const int q = warp - 4;
         const int rloc = 32 * q + lane;
+        const int n_part = (n_st + kPerPartial - 1) / kPerPartial;
         int64_t g = 0;
         int64_t kit = 0;
         bool ok = true;
@@ -255,7 +268,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             float acc[kCols];
 #pragma unroll
             for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
-            for (int s = 0; s < n_st; ++s, ++g) {
+            for (int s = 0; s < n_part; ++s, ++g) {
                 if (!ok) continue;
                 const int tb = (int)(g % kBufs);
                 const uint32_t use = (uint32_t)(g / kBufs);
