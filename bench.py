@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--cpu-rows", type=int, default=40000, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--cal-n", type=int, default=200_000, help="states in the calibration measurement (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the serving window (0: no serving phase)")
+    ap.add_argument("--fact-rate", type=float, default=20.0, help="factorization requests per second")
+    ap.add_argument("--query-rate", type=float, default=2000.0, help="query batches per second")
     return ap.parse_args()
 
 
@@ -129,6 +134,185 @@ class ClockSampler:
         reasons = sorted({names[j] for r in self.rows for j in range(4) if r[2 + j].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+def calibration_phase(ctx, Xd, args, sm_mhz):
+    """Fused bandwidth calibration at N = 200,000 (the first 200,000 states of
+    the trajectory), d = 64, 64 log-spaced eps in 2^-10..2^10 x the median
+    squared distance of a seeded 1e7-pair sample: every pair tile evaluated once
+    for all 64 eps.  Timed with CUDA events; the work is N(N-1)/2 x 64
+    exp evaluations, bound by the MUFU ex2 rate (16 per clock per SM, nominal,
+    at the sampled SM clock).  Precision: relative error of S(eps) against the
+    plain FP64 pass on the first 40,000 states, and the selected eps."""
+    import torch
+    from kernel_evd_gb300 import api
+    n = min(args.cal_n, Xd.shape[0])
+    Xs = Xd[:n].contiguous()
+    pi, pl = sample_pairs(n, 10_000_000, seed=0)
+    med = api.pair_median(ctx, Xs, pairs=(torch.from_numpy(pi).cuda(), torch.from_numpy(pl).cuda()))
+    eps = api.log_sweep(med, 64)
+    sc = 1.0 / eps
+    api.calibrate(ctx, Xs, sc)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    reps = 3
+    c0.record(stream)
+    for _ in range(reps):
+        sums = api.calibrate(ctx, Xs, sc)
+    c1.record(stream)
+    torch.cuda.synchronize()
+    t = c0.elapsed_time(c1) / reps / 1e3
+    pairs = n * (n - 1) / 2
+    sel = api.select_bandwidth(eps, sums, n)
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    peak = 16.0 * nsm * mhz * 1e6
+    # precision against the FP64 form on a row prefix
+    n64 = min(40_000, n)
+    X64 = Xd[:n64].contiguous()
+    s32 = api.calibrate(ctx, X64, sc)
+    t64 = time.time()
+    s64 = api.calibrate(ctx, X64, sc, precision="fp64")
+    t64 = time.time() - t64
+    mask = s64 > 1e-12 * s64.max()
+    rel = np.abs(s32[mask] - s64[mask]) / s64[mask]
+    sel32 = api.select_bandwidth(eps, s32, n64)
+    sel64 = api.select_bandwidth(eps, s64, n64)
+    return {"workload": f"N={n}, d={Xs.shape[1]}, 64 eps, all pairs", "seconds": t,
+            "pair_eps_per_s": pairs * 64 / t, "pairs": pairs, "median_sqdist_sampled": med,
+            "eopt": sel["eopt"], "mdim": sel["mdim"], "idmax": sel["idmax"],
+            "roofline": {"bound": "mufu_ex2", "achieved": pairs * 64 / t / 1e12, "peak": peak / 1e12,
+                         "unit": "Texp/s", "frac": pairs * 64 / t / peak,
+                         "note": f"nominal 16 ex2/clk/SM x {nsm} SMs x {mhz:.0f} MHz (sampled clock)"},
+            "vs_fp64": {"rows": n64, "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
+                        "scales_compared": int(mask.sum()), "same_selected_eps": sel32["idmax"] == sel64["idmax"],
+                        "fp64_pass_s": t64}}
+
+
+def serving_phase(ctx, X, Xd, scale, args):
+    """Serving loop under Poisson load: factorization requests (KS slices, N
+    log-uniform in [1e4, 1e6], rank uniform in [200, 2000], b = 64) at
+    ``fact_rate``/s and Nystrom query batches (1..4096 fresh states, size
+    log-uniform) at ``query_rate``/s against two resident k = 2000 landmark
+    sets, for ``serve_seconds``.  Latencies are measured by the server from
+    submission to completion; the eigenfunction error is against an FP64
+    Nystrom extension built on the same pivots."""
+    import queue
+    from kernel_evd_gb300 import api
+    from kernel_evd_gb300._lib import KEVD_FP64
+    import torch
+    N = X.shape[0]
+    kout = args.kout
+    rng_r = np.random.default_rng(7)
+    rng_q = np.random.default_rng(8)
+    pool_q = X[N - min(N // 20, 100_000):]            # fresh states, never a training row
+    base = [(0, min(1_000_000, N // 2)), (N // 2, min(300_000, N // 4))]
+    srv = api.Server(factor_workers=3, max_query_batch=16384, hbm_budget_bytes=160 << 30)
+    t0 = time.time()
+    models = []
+    for j, (o, n) in enumerate(base):
+        r = srv.wait(srv.submit_factorization(X[o:o + n], scale, k=2000, block=64, k_out=kout, seed=100 + j))
+        models.append(r.model_id)
+    base_s = time.time() - t0
+    T = args.serve_seconds
+    fa = np.cumsum(rng_r.exponential(1.0 / args.fact_rate, int(args.fact_rate * T * 2) + 16))
+    fa = fa[fa < T]
+    qa = np.cumsum(rng_q.exponential(1.0 / args.query_rate, int(args.query_rate * T * 2) + 64))
+    qa = qa[qa < T]
+    fn = np.exp(rng_r.uniform(np.log(1e4), np.log(min(1e6, N // 2)), fa.size)).astype(np.int64)
+    fk = np.minimum(rng_r.integers(200, 2001, fa.size), fn // 4)
+    fo = (rng_r.random(fa.size) * (N // 2 - fn)).astype(np.int64)
+    qs = np.exp(rng_q.uniform(0.0, np.log(4096.0), qa.size)).astype(np.int64).clip(1, 4096)
+    qo = (rng_q.random(qa.size) * (pool_q.shape[0] - qs)).astype(np.int64)
+    qm = rng_q.integers(0, len(models), qa.size)
+    done = queue.Queue()
+    keep = []                      # (model index, offset, size, out) of the first queries, for the error check
+    t_start = time.time() + 0.05
+
+    def fact_submitter():
+        for i in range(fa.size):
+            dt = t_start + fa[i] - time.time()
+            if dt > 0:
+                time.sleep(dt)
+            done.put(("f", srv.submit_factorization(X[fo[i]:fo[i] + fn[i]], scale, k=int(fk[i]), block=64,
+                                                    k_out=min(kout, int(fk[i])), seed=int(1000 + i))))
+
+    def query_submitter():
+        for i in range(qa.size):
+            dt = t_start + qa[i] - time.time()
+            if dt > 0:
+                time.sleep(dt)
+            rid, out = srv.submit_query(models[qm[i]], pool_q[qo[i]:qo[i] + qs[i]], kout)
+            if len(keep) < 200:
+                keep.append((int(qm[i]), int(qo[i]), int(qs[i]), out, rid))
+            done.put(("q", rid))
+
+    th = [threading.Thread(target=fact_submitter), threading.Thread(target=query_submitter)]
+    for t in th:
+        t.start()
+    n_wait = fa.size + qa.size
+    fact_ok = 0
+    states = 0
+    batch_rows = []
+    failed = {}
+    for _ in range(n_wait):
+        kind, rid = done.get()
+        try:
+            r = srv.wait(rid, timeout_s=600.0)
+        except api.KevdError as e:        # e.g. a slice whose rank stays below k_out
+            f = failed.setdefault(e.name, {"count": 0, "first": str(e)[:200]})
+            f["count"] += 1
+            continue
+        if kind == "f":
+            fact_ok += 1
+            srv.release_model(r.model_id)
+        else:
+            batch_rows.append(r.batch_rows)
+    for t in th:
+        t.join()
+    wall = time.time() - t_start
+    states = int(qs.sum())
+    sf, sq = srv.stats("factorization"), srv.stats("query")
+    mem = srv.memory()
+    # eigenfunction error of the resident mixed model 1 against an FP64 Nystrom
+    # extension on the same pivots (the mixed factorization is deterministic)
+    o, n = base[1]
+    Xs = Xd[o:o + n].contiguous()
+    fac_m = api.rpcholesky(ctx, Xs, scale, k_max=2000, block=64, seed=101, precision="mixed")
+    F64 = api.factor_from_pivots(ctx, Xs, scale, fac_m.piv, precision="fp64")
+    fac64 = api.Factorization(F=F64, piv=fac_m.piv, err=np.zeros(0), accepted=np.zeros(0, np.int32),
+                              rank=fac_m.rank, rounds=0, trace_error=0.0, precision=KEVD_FP64, scale=scale)
+    m64 = api.NystromModel(ctx, Xs, fac64, k_out=kout)
+    errs = []
+    for mi, qo_, qs_, out, rid in keep:
+        if mi != 1:
+            continue
+        ref = m64(torch.from_numpy(pool_q[qo_:qo_ + qs_]).cuda()).cpu().numpy().astype(np.float64)
+        errs.append((out.astype(np.float64), ref))
+    m64.close()
+    del F64, fac64
+    err = None
+    if errs:
+        U = np.concatenate([e[0] for e in errs])
+        R = np.concatenate([e[1] for e in errs])
+        sgn = np.sign(np.sum(U * R, axis=0))
+        sgn[sgn == 0] = 1.0
+        col = np.abs(U * sgn[None, :] - R).max(axis=0) / np.abs(R).max(axis=0)
+        err = {"rel_max_leading8": [float(x) for x in col[::-1][:8]], "rel_max_all": float(col.max()),
+               "states": int(U.shape[0])}
+    srv.close()
+    return {"window_s": T, "wall_s": wall, "base_models_s": base_s,
+            "factorization": {"arrival_rate_hz": args.fact_rate, "submitted": int(fa.size), "completed": fact_ok,
+                              "p50_s": sf["p50_s"], "p99_s": sf["p99_s"], "throughput_hz": fact_ok / wall},
+            "query": {"arrival_rate_hz": args.query_rate, "submitted": int(qa.size), "states": states,
+                      "p50_s": sq["p50_s"], "p99_s": sq["p99_s"], "states_per_s": states / wall,
+                      "mean_batch_states": float(np.mean(batch_rows)) if batch_rows else 0.0},
+            "peak_concurrent_factorizations": mem["peak_active"], "failed": failed,
+            "eigenfunction_err_vs_fp64_same_pivots": err,
+            "config": "KS slices of the benchmark trajectory; resident k=2000 landmark sets at N=1e6 and 3e5; "
+                      "3 factor workers, query batches up to 16384 states, 160 GiB admission budget"}
 
 
 def reference_arm(args, n_gpus):
@@ -325,6 +509,14 @@ def main():
         cpu = {"value": est, "unit": "s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"first {n_s} of {N} states, k={args.k}, b={args.b}: rows-proportional "
                          f"{tb['stream_s']:.2f} s x {N}/{n_s} + dense {tb['dense_s']:.2f} s"}
+    # --- fused calibration at N = 200,000, 64 eps
+    if args.cal_n > 0:
+        result["calibration"] = calibration_phase(ctx, Xd, args, (clocks or {}).get("sm_mhz"))
+    # --- serving loop under load (after the timed regions; frees the step's buffers first)
+    if args.serve_seconds > 0:
+        del F, U
+        torch.cuda.empty_cache()
+        result["serving"] = serving_phase(ctx, X, Xd, scale, args)
     # --- max over ranks
     val = ms / 1e3
     if dist is not None:

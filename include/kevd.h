@@ -104,6 +104,13 @@ int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                    const double* scales, int32_t n_scales, double* sums,
                    void* stream);
 
+/* The plain FP64 form of kevd_calibrate (FP64 distances from the FP32 states,
+ * FP64 exp): the precision reference for the fused pass, as the reference's
+ * FP64 programs are for its FP32 kernels.  Same arguments and limits. */
+int kevd_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
+                        const double* scales, int32_t n_scales, double* sums,
+                        void* stream);
+
 /* kevd_calibrate for callers that cannot allocate device memory (inside a CUDA
  * graph capture or a stream callback, under a device-memory pool they do not
  * own, or after an allocation freeze).  No reference counterpart.  Needs no
@@ -116,6 +123,25 @@ int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
 int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d,
                            const double* scales, int32_t n_scales,
                            double* sums, void* stream);
+
+/* Many calibrations of uneven size in one persistent launch (no reference
+ * counterpart: the reference calibrates one dataset per program run).  Every
+ * job's lower-triangle pair tiles are cut into work items of tiles_per_item
+ * tiles (0: chosen from the batch size) and placed in one device work queue; a
+ * persistent grid takes items with an atomic counter and a second kernel sums
+ * each job's item partials in item order (deterministic).  Per job: sums[j] as
+ * kevd_calibrate, n_scales <= 64, d <= 128.  X: device; scales, sums: host. */
+typedef struct {
+    const float* X;
+    int64_t N;
+    int32_t d;
+    int32_t n_scales;
+    const double* scales;
+    double* sums;
+} kevd_calib_job;
+int kevd_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs,
+                           int32_t n_jobs, int32_t tiles_per_item,
+                           void* stream);
 
 /* Host post-processing of ks_bandwidth.cu:612-642 in FP64:
  * logS[i] = log(2 sums[i]/NM + 1); slope[i-1] = centred difference at bw[i]
@@ -239,6 +265,80 @@ int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
 int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y,
                       int64_t n, float* Uy, void* stream);
 void kevd_model_destroy(kevd_model* model);
+
+/* ---- serving loop (no reference counterpart) ----------------------------
+ * The reference runs its three stages as batch programs.  The server keeps
+ * factorized models resident on one GPU and answers eigenfunction queries
+ * against them while new factorizations run:
+ *  - a factorization request (host X, N x d) is admitted when a worker is
+ *    free and its HBM footprint fits the budget left by running
+ *    factorizations and resident models; it runs block RPCholesky, the
+ *    bistochastic EVD and kevd_nystrom_prepare on its worker's own stream,
+ *    then frees everything except the model;
+ *  - query requests (host Y, n x d) for a model are batched: whatever is
+ *    queued for the model with the oldest pending query, up to
+ *    max_query_batch states, is evaluated in one kevd_nystrom_eval launch
+ *    (rows are evaluated independently, so a query's result does not depend
+ *    on the batch it joined).
+ * Y and out stay owned by the caller and must remain valid until
+ * kevd_server_wait has returned for that request. */
+typedef struct kevd_server kevd_server;
+
+typedef struct {
+    int32_t device;            /* CUDA device ordinal                         */
+    int32_t factor_workers;    /* concurrent factorizations, 1..16            */
+    int64_t max_query_batch;   /* states per query launch, >= 1              */
+    uint64_t hbm_budget_bytes; /* admission budget (bytes of device memory)   */
+    double batch_window_us;    /* batcher waits this long before taking a
+                                  batch, letting it fill (0: no wait)         */
+} kevd_server_config;
+
+typedef struct {
+    int32_t status;            /* kevd_status of the request                  */
+    int64_t model_id;          /* factorization: id of the resident model     */
+    double latency_s;          /* submit -> done                              */
+    double queue_s;            /* submit -> started                           */
+    int64_t batch_rows;        /* query: states in the launch(es) it joined   */
+    double trace_error;        /* factorization: tr(K - FF^T)/tr(K)           */
+    int64_t rank;              /* factorization: realised rank                */
+    char message[192];         /* failure description (empty on success)      */
+} kevd_request_info;
+
+int kevd_server_create(const kevd_server_config* cfg, kevd_server** server);
+/* Device bytes the server charges against its budget for a factorization of
+ * N x d states to rank k (X, F and its column-major copy, workspaces); -1 for
+ * invalid sizes.  A resident model is charged r (4 d + 8 (k_out + 1)) bytes. */
+int64_t kevd_factorization_footprint(int64_t N, int32_t d, int64_t k,
+                                     int32_t k_out, int32_t precision);
+/* Stops the workers after the requests already running; queued requests are
+ * dropped.  Frees every resident model. */
+void kevd_server_destroy(kevd_server* server);
+/* X is copied at submission.  KEVD_ERR_NOMEM when the footprint can never fit
+ * the budget. */
+int kevd_server_submit_factorization(kevd_server* server, const float* X,
+                                     int64_t N, int32_t d, double scale,
+                                     int64_t k, int32_t block, int32_t k_out,
+                                     uint64_t seed, int32_t precision,
+                                     int64_t* request_id);
+/* out: host, n x k_out float (row-major). */
+int kevd_server_submit_query(kevd_server* server, int64_t model_id,
+                             const float* Y, int64_t n, float* out,
+                             int64_t* request_id);
+/* Blocks until the request is done (KEVD_ERR_TIMEOUT after timeout_s, the
+ * request stays pending).  Once it returns KEVD_OK the id is retired. */
+int kevd_server_wait(kevd_server* server, int64_t request_id, double timeout_s,
+                     kevd_request_info* info);
+/* Frees a resident model; KEVD_ERR_ARG while queries for it are pending. */
+int kevd_server_release_model(kevd_server* server, int64_t model_id);
+/* Latency percentiles over finished requests of one type (0 factorization,
+ * 1 query), in seconds. */
+int kevd_server_stats(kevd_server* server, int32_t type, double* p50,
+                      double* p99, int64_t* count);
+/* Bytes charged against the budget, running factorizations, resident models,
+ * and the largest number of factorizations that ever ran at once. */
+int kevd_server_memory(kevd_server* server, int64_t* used_bytes,
+                       int32_t* active_factorizations, int32_t* models,
+                       int32_t* peak_active);
 
 #ifdef __cplusplus
 }

@@ -44,6 +44,22 @@ class EvdInfo(C.Structure):
     _fields_ = [("trace_A", C.c_double), ("shift", C.c_double)]
 
 
+class CalibJob(C.Structure):
+    _fields_ = [("X", C.c_void_p), ("N", C.c_int64), ("d", C.c_int32), ("n_scales", C.c_int32),
+                ("scales", C.c_void_p), ("sums", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("factor_workers", C.c_int32), ("max_query_batch", C.c_int64),
+                ("hbm_budget_bytes", C.c_uint64), ("batch_window_us", C.c_double)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("model_id", C.c_int64), ("latency_s", C.c_double),
+                ("queue_s", C.c_double), ("batch_rows", C.c_int64), ("trace_error", C.c_double),
+                ("rank", C.c_int64), ("message", C.c_char * 192)]
+
+
 class EvdDump(C.Structure):
     _fields_ = [(n, C.POINTER(C.c_double)) for n in ("c1", "dtil", "cq", "qtil", "A", "B", "W", "Z")]
 
@@ -65,6 +81,8 @@ SIGNATURES = {
     "kevd_hankel_rows": (C.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
     "kevd_kernel_block": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I64, _I64, _P, _I64, _I32, _P, _I64, _P]),
     "kevd_calibrate": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),
+    "kevd_calibrate_fp64": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),
+    "kevd_calibrate_batched": (C.c_int, [_P, C.POINTER(CalibJob), _I32, _I32, _P]),
     "kevd_calibrate_noalloc": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P]),
     "kevd_calibrate_select": (C.c_int, [_P, _P, _I32, _I64, _P, _P, _P, _P, _P]),
     "kevd_pair_median": (C.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P]),
@@ -80,6 +98,18 @@ SIGNATURES = {
                                        C.POINTER(_P), _P]),
     "kevd_nystrom_eval": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
     "kevd_model_destroy": (None, [_P]),
+    "kevd_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "kevd_server_destroy": (None, [_P]),
+    "kevd_factorization_footprint": (_I64, [_I64, C.c_int32, _I64, C.c_int32, C.c_int32]),
+    "kevd_server_submit_factorization": (C.c_int, [_P, _P, _I64, C.c_int32, C.c_double, _I64, C.c_int32,
+                                                   C.c_int32, C.c_uint64, C.c_int32, C.POINTER(_I64)]),
+    "kevd_server_submit_query": (C.c_int, [_P, _I64, _P, _I64, _P, C.POINTER(_I64)]),
+    "kevd_server_wait": (C.c_int, [_P, _I64, C.c_double, C.POINTER(RequestInfo)]),
+    "kevd_server_release_model": (C.c_int, [_P, _I64]),
+    "kevd_server_stats": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(_I64)]),
+    "kevd_server_memory": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -110,15 +110,36 @@ def kernel_block(ctx: Context, X: torch.Tensor, scale: float, cols: torch.Tensor
 
 
 # ---- stage 1 ---------------------------------------------------------------
-def calibrate(ctx: Context, X: torch.Tensor, scales) -> np.ndarray:
-    """sums[j] = sum_{i>l} exp(-scales[j] ||x_i - x_l||^2) (FP64, host)."""
+def calibrate(ctx: Context, X: torch.Tensor, scales, precision="mixed") -> np.ndarray:
+    """sums[j] = sum_{i>l} exp(-scales[j] ||x_i - x_l||^2) (FP64, host).
+
+    ``precision="mixed"``: the fused FP32-distance / exp2 pass;
+    ``"fp64"``: its plain FP64 form (FP64 distances and exp)."""
     _need_cuda(X, torch.float32, "X")
     scales = np.ascontiguousarray(scales, dtype=np.float64)
     sums = np.zeros(scales.size, dtype=np.float64)
     N, d = X.shape
-    ctx._check(ctx.lib.kevd_calibrate(ctx.h, _ptr(X), N, d, _np_ptr(scales), scales.size,
-                                      _np_ptr(sums), _stream()))
+    fn = ctx.lib.kevd_calibrate_fp64 if _prec(precision) == KEVD_FP64 else ctx.lib.kevd_calibrate
+    ctx._check(fn(ctx.h, _ptr(X), N, d, _np_ptr(scales), scales.size, _np_ptr(sums), _stream()))
     return sums
+
+
+def calibrate_batched(ctx: Context, Xs, scales_list, tiles_per_item: int = 0) -> list:
+    """calibrate() for many datasets (uneven N, d <= 128, <= 64 scales each) in
+    one persistent launch over a device work queue of pair-tile ranges."""
+    n = len(Xs)
+    jobs = (_lib.CalibJob * n)()
+    keep = []
+    outs = []
+    for q, (X, sc) in enumerate(zip(Xs, scales_list)):
+        _need_cuda(X, torch.float32, "X")
+        sc = np.ascontiguousarray(sc, dtype=np.float64)
+        out = np.zeros(sc.size, dtype=np.float64)
+        keep += [sc, out]
+        outs.append(out)
+        jobs[q] = _lib.CalibJob(X.data_ptr(), X.shape[0], X.shape[1], sc.size, sc.ctypes.data, out.ctypes.data)
+    ctx._check(ctx.lib.kevd_calibrate_batched(ctx.h, jobs, n, int(tiles_per_item), _stream()))
+    return outs
 
 
 def calibrate_noalloc(X: torch.Tensor, scales) -> np.ndarray:
@@ -348,6 +369,106 @@ class NystromModel:
         if getattr(self, "h", None):
             self.ctx.lib.kevd_model_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- serving loop ------------------------------------------------------------
+@dataclass
+class RequestResult:
+    status: int
+    model_id: int
+    latency_s: float
+    queue_s: float
+    batch_rows: int
+    trace_error: float
+    rank: int
+
+
+def factorization_footprint(N: int, d: int, k: int, k_out: int = 32, precision="mixed") -> int:
+    """Bytes the server charges against its HBM budget for one factorization."""
+    return int(_lib.load().kevd_factorization_footprint(N, d, k, k_out, _prec(precision)))
+
+
+def model_bytes(rank: int, d: int, k_out: int) -> int:
+    """Bytes a resident Nystrom model is charged (landmarks + [Z'|p1'])."""
+    return rank * (4 * d + 8 * (k_out + 1))
+
+
+class Server:
+    """Resident models on one GPU, factorizations admitted by HBM footprint,
+    Nystrom queries batched as they arrive (``kevd_server_*``).
+
+    ``submit_factorization`` copies X (host float32, N x d).  ``submit_query``
+    keeps a reference to Y (host float32, n x d) and writes into ``out``
+    (host float32, n x k_out) until ``wait`` returns for that request."""
+
+    def __init__(self, device: int = 0, factor_workers: int = 2, max_query_batch: int = 8192,
+                 hbm_budget_bytes: int = 200 << 30, batch_window_us: float = 0.0):
+        self.lib = _lib.load()
+        cfg = _lib.ServerConfig(device, factor_workers, max_query_batch, hbm_budget_bytes, batch_window_us)
+        h = C.c_void_p()
+        check(self.lib.kevd_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}   # request id -> host arrays the server still reads or writes
+
+    def submit_factorization(self, X: np.ndarray, scale: float, k: int, block: int = 64, k_out: int = 32,
+                             seed: int = 0, precision="mixed") -> int:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        rid = C.c_int64()
+        check(self.lib.kevd_server_submit_factorization(self.h, _np_ptr(X), X.shape[0], X.shape[1], float(scale),
+                                                        int(k), int(block), int(k_out), int(seed),
+                                                        _prec(precision), C.byref(rid)))
+        return rid.value
+
+    def submit_query(self, model_id: int, Y: np.ndarray, k_out: int) -> tuple[int, np.ndarray]:
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        out = np.empty((Y.shape[0], k_out), dtype=np.float32)
+        rid = C.c_int64()
+        check(self.lib.kevd_server_submit_query(self.h, int(model_id), _np_ptr(Y), Y.shape[0], _np_ptr(out),
+                                                C.byref(rid)))
+        self._keep[rid.value] = (Y, out)
+        return rid.value, out
+
+    def wait(self, rid: int, timeout_s: float = 600.0) -> RequestResult:
+        info = _lib.RequestInfo()
+        check(self.lib.kevd_server_wait(self.h, int(rid), float(timeout_s), C.byref(info)))
+        self._keep.pop(rid, None)
+        res = RequestResult(info.status, info.model_id, info.latency_s, info.queue_s, info.batch_rows,
+                            info.trace_error, info.rank)
+        if res.status != 0:
+            raise KevdError(res.status, f"request {rid} failed: {info.message.decode(errors='replace')}")
+        return res
+
+    def release_model(self, model_id: int):
+        check(self.lib.kevd_server_release_model(self.h, int(model_id)))
+
+    def stats(self, kind: str) -> dict:
+        p50, p99, n = C.c_double(), C.c_double(), C.c_int64()
+        check(self.lib.kevd_server_stats(self.h, {"factorization": 0, "query": 1}[kind], C.byref(p50),
+                                         C.byref(p99), C.byref(n)))
+        return {"p50_s": p50.value, "p99_s": p99.value, "count": n.value}
+
+    def memory(self) -> dict:
+        used, act, mods, peak = C.c_int64(), C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.lib.kevd_server_memory(self.h, C.byref(used), C.byref(act), C.byref(mods), C.byref(peak)))
+        return {"used_bytes": used.value, "active": act.value, "models": mods.value, "peak_active": peak.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kevd_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def __del__(self):
         try:

@@ -57,7 +57,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             objs.append(obj)
             jobs.append(ex.submit(_run, [nvcc, *flags, "-c", src, "-o", obj]))
         logs = [j.result() for j in jobs]
-    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcublas", "-lcusolver", "-lcudart"])
+    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcublas", "-lcusolver", "-lcudart", "-lpthread"])
     cc = shutil.which("gcc") or shutil.which("cc")
     _run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-o", KSGEN,
           os.path.join(CSRC, "host", "ksgen.c"), "-lm"])

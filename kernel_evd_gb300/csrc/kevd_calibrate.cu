@@ -138,6 +138,113 @@ __global__ void reduce_partials_kernel(const double* __restrict__ partial, int n
     out[j] = s;
 }
 
+// Plain FP64 form of the same pass (FP64 direct distances, FP64 exp): the
+// precision reference of the fused FP32 / exp2 kernel above.  Same tiles and
+// masking; 64 FP64 distances per thread, so one CTA per SM.
+__global__ void __launch_bounds__(256, 1)
+calibrate_tiles_fp64_kernel(const float* __restrict__ X, int64_t N, int d, const double* __restrict__ sc,
+                            int n_scales, int64_t n_tiles, double* __restrict__ partial) {
+    extern __shared__ float sm[];
+    const int dp = d + 1;
+    float* xi = sm;
+    float* xj = sm + kCalTile * dp;
+    double* cs = reinterpret_cast<double*>(xj + kCalTile * dp + 2);   // 8-byte aligned (dp*128*2 floats is even)
+    double* red = cs + kCalMaxScales;                                   // 8 warps x n_scales
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j = threadIdx.x; j < n_scales; j += blockDim.x) cs[j] = sc[j];
+    double acc = 0.0;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        int64_t ti, tj;
+        tri_tile(t, ti, tj);
+        __syncthreads();
+        load_rows(X, N, d, ti * kCalTile, xi);
+        load_rows(X, N, d, tj * kCalTile, xj);
+        __syncthreads();
+        double D[8][8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) D[a][b] = 0.0;
+        for (int k = 0; k < d; ++k) {
+            double vi[8], vj[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) vi[a] = (double)xi[(ty + 16 * a) * dp + k];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) vj[b] = (double)xj[(tx + 16 * b) * dp + k];
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const double u = vi[a] - vj[b];
+                    D[a][b] = fma(u, u, D[a][b]);
+                }
+        }
+        const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const int64_t gi = gi0 + 16 * a, gj = gj0 + 16 * b;
+                if (!(gi < N && gi > gj)) D[a][b] = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+            }
+        for (int j = 0; j < n_scales; ++j) {
+            const double c = -cs[j];
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) s += exp(D[a][b] * c);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) red[warp * kCalMaxScales + j] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < n_scales) {
+            double w = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) w += red[q * kCalMaxScales + threadIdx.x];
+            acc += w;
+        }
+    }
+    if (threadIdx.x < n_scales) partial[(int64_t)blockIdx.x * n_scales + threadIdx.x] = acc;
+}
+
+static size_t calib_smem_fp64(int d) {
+    return 2 * kCalTile * (size_t)(d + 1) * sizeof(float) + 16 + 9 * kCalMaxScales * sizeof(double);
+}
+
+int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales, int n_scales,
+                       double* sums, cudaStream_t s) {
+    if (!X || !scales || !sums || N < 1 || d < 1 || d > kCalMaxD || n_scales < 1 || n_scales > kCalMaxScales)
+        return set_error(ctx, KEVD_ERR_ARG, "calibrate_fp64: need N >= 1, 1 <= d <= %d, 1 <= n_scales <= %d",
+                         kCalMaxD, kCalMaxScales);
+    for (int j = 0; j < n_scales; ++j)
+        if (!(scales[j] > 0.0)) return set_error(ctx, KEVD_ERR_ARG, "calibrate_fp64: scales must be positive");
+    const int64_t nt = (N + kCalTile - 1) / kCalTile;
+    const int64_t n_tiles = nt * (nt + 1) / 2;
+    const int grid = (int)std::min<int64_t>(n_tiles, (int64_t)ctx->num_sms);
+    int st = KEVD_OK;
+    double* sc = arena_get<double>(ctx, "cal64.sc", kCalMaxScales, &st);
+    double* partial = arena_get<double>(ctx, "cal64.partial", (size_t)grid * n_scales, &st);
+    double* out = arena_get<double>(ctx, "cal64.out", kCalMaxScales, &st);
+    if (st != KEVD_OK) return st;
+    KEVD_CUDA(ctx, cudaMemcpyAsync(sc, scales, n_scales * sizeof(double), cudaMemcpyHostToDevice, s));
+    const size_t smem = calib_smem_fp64(d);
+    KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_tiles_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+    {
+        ProfScope ps(ctx, "calibrate_tiles_fp64", s);
+        calibrate_tiles_fp64_kernel<<<grid, 256, smem, s>>>(X, N, d, sc, n_scales, n_tiles, partial);
+        KEVD_LAUNCH(ctx);
+    }
+    reduce_partials_kernel<<<1, kCalMaxScales, 0, s>>>(partial, grid, n_scales, out);
+    KEVD_LAUNCH(ctx);
+    KEVD_CUDA(ctx, cudaMemcpyAsync(sums, out, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    return KEVD_OK;
+}
+
 static size_t calib_smem(int d) {
     return (2 * kCalTile * (size_t)(d + 1) + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
 }

@@ -194,6 +194,18 @@ int kevd_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, const do
     return run_calibrate(ctx, X, N, d, scales, n_scales, sums, as_stream(stream));
 }
 
+int kevd_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int32_t n_jobs, int32_t tiles_per_item,
+                           void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_calibrate_batched(ctx, jobs, n_jobs, tiles_per_item, as_stream(stream));
+}
+
+int kevd_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, const double* scales,
+                        int32_t n_scales, double* sums, void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_calibrate_fp64(ctx, X, N, d, scales, n_scales, sums, as_stream(stream));
+}
+
 int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d, const double* scales, int32_t n_scales,
                            double* sums, void* stream) {
     return run_calibrate_noalloc(X, N, d, scales, n_scales, sums, as_stream(stream));
@@ -369,6 +381,14 @@ int kevd_factor_from_pivots(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
     return KEVD_OK;
 }
 
+__global__ void landmark_gather_kernel(const float* __restrict__ X, const int64_t* __restrict__ idx, int64_t r, int d,
+                                       float* __restrict__ xs) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < r * d; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = e / d;
+        xs[e] = X[idx[q] * d + (e - q * d)];
+    }
+}
+
 int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, double scale,
                          const void* F, int32_t precision, int64_t ldF, const int64_t* piv,
                          int64_t r, int32_t k_out, kevd_model** model, void* stream) {
@@ -421,16 +441,14 @@ int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, do
             rc = set_error(ctx, KEVD_ERR_CUDA, "nystrom_prepare: trsm failed");
             break;
         }
-        // landmark rows
-        std::vector<int64_t> hp(piv, piv + r);
-        for (int64_t q = 0; q < r; ++q) {
-            if (cudaMemcpyAsync(m->m.xs + q * d, X + hp[q] * d, d * sizeof(float),
-                                cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
-                rc = set_error(ctx, KEVD_ERR_CUDA, "nystrom_prepare: landmark copy failed");
-                break;
-            }
+        // landmark rows X[piv]
+        landmark_gather_kernel<<<(unsigned)std::min<int64_t>((r * d + 255) / 256, (int64_t)ctx->num_sms * 8), 256, 0,
+                                 s>>>(X, idx, r, d, m->m.xs);
+        ++ctx->launches;
+        if (cudaGetLastError() != cudaSuccess) {
+            rc = set_error(ctx, KEVD_ERR_CUDA, "nystrom_prepare: landmark gather failed");
+            break;
         }
-        if (rc != KEVD_OK) break;
         if (cudaStreamSynchronize(s) != cudaSuccess) rc = set_error(ctx, KEVD_ERR_CUDA, "nystrom_prepare: sync");
     } while (0);
     if (rc != KEVD_OK) {
@@ -441,14 +459,93 @@ int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, do
     return KEVD_OK;
 }
 
-__global__ void nystrom_ratio_kernel(const double* __restrict__ P, int64_t n, int k_out,
-                                     float* __restrict__ Uy) {
-    // P: n x (k_out + 1) column-major = [K Z' | K p1']
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k_out;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e / k_out, j = e - i * k_out;
-        Uy[e] = (float)(P[(int64_t)j * n + i] / P[(int64_t)k_out * n + i]);
+// Fused out-of-sample evaluation.  One CTA serves 32 query rows: for each
+// chunk of 32 landmarks it forms K(y, s_j) from FP32 direct differences summed
+// over the feature index in increasing order and an FP32 exp (relative error
+// about 1e-7 in K, far below the FP32 output's), and accumulates
+// P[row][c] = sum_j K(y, s_j) [Z'|p1'][j][c] in FP64 with j ascending in one
+// register per output: [Z'|p1'] = L^{-T}[Z|c1] has large entries of both
+// signs, so the sum stays FP64.  No thread ever combines two query rows, so a
+// row's result is bit-identical whatever batch it is evaluated in and wherever
+// it sits in the batch.
+constexpr int kNyRows = 32;
+constexpr int kNyLm = 32;
+constexpr int kNyMaxOut = 9;   // ceil(32 * 65 / 256) outputs per thread
+
+__global__ void __launch_bounds__(256) nystrom_eval_kernel(const float* __restrict__ Y, int64_t n,
+                                                           const float* __restrict__ xs, const double* __restrict__ zp,
+                                                           int64_t r, int d, int k_out, double scale,
+                                                           float* __restrict__ Uy) {
+    extern __shared__ __align__(16) unsigned char ny_smem[];
+    const int dp = d + 1, kc = k_out + 1;
+    double* kv = reinterpret_cast<double*>(ny_smem);     // 32 x 33
+    double* zc = kv + kNyRows * (kNyLm + 1);             // 32 landmarks x kc
+    float* ys = reinterpret_cast<float*>(zc + kNyLm * kc);  // 32 x dp
+    float* xc = ys + kNyRows * dp;                       // 32 x dp
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const float fscale = (float)scale;
+    const int64_t row0 = (int64_t)blockIdx.x * kNyRows;
+    for (int e = threadIdx.x; e < kNyRows * d; e += 256) {
+        const int rr = e / d, kk = e - rr * d;
+        ys[rr * dp + kk] = (row0 + rr < n) ? Y[(row0 + rr) * d + kk] : 0.f;
     }
+    double acc[kNyMaxOut];
+#pragma unroll
+    for (int q = 0; q < kNyMaxOut; ++q) acc[q] = 0.0;
+    const int n_out = kNyRows * kc;
+    for (int64_t j0 = 0; j0 < r; j0 += kNyLm) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kNyLm * d; e += 256) {
+            const int jj = e / d, kk = e - jj * d;
+            xc[jj * dp + kk] = (j0 + jj < r) ? xs[(j0 + jj) * d + kk] : 0.f;
+        }
+        for (int e = threadIdx.x; e < kNyLm * kc; e += 256) {
+            const int jj = e / kc, c = e - jj * kc;
+            zc[jj * kc + c] = (j0 + jj < r) ? zp[(int64_t)c * r + j0 + jj] : 0.0;
+        }
+        __syncthreads();
+        // K(row ty + 8i, landmark tx)
+        float dist[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int kk = 0; kk < d; ++kk) {
+            const float c = xc[tx * dp + kk];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float t = ys[(ty + 8 * i) * dp + kk] - c;
+                dist[i] = fmaf(t, t, dist[i]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            kv[(ty + 8 * i) * (kNyLm + 1) + tx] = (j0 + tx < r) ? (double)expf(-fscale * dist[i]) : 0.0;
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kNyMaxOut; ++q) {
+            const int o = threadIdx.x + 256 * q;
+            if (o < n_out) {
+                const int rr = o / kc, c = o - rr * kc;
+                double a = acc[q];
+#pragma unroll 8
+                for (int jj = 0; jj < kNyLm; ++jj) a += kv[rr * (kNyLm + 1) + jj] * zc[jj * kc + c];
+                acc[q] = a;
+            }
+        }
+    }
+    __syncthreads();
+    double* P = kv;   // reuse: 32 x kc doubles fit in kv + zc
+#pragma unroll
+    for (int q = 0; q < kNyMaxOut; ++q) {
+        const int o = threadIdx.x + 256 * q;
+        if (o < n_out) P[o] = acc[q];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kNyRows * k_out; e += 256) {
+        const int rr = e / k_out, c = e - rr * k_out;
+        if (row0 + rr < n) Uy[(row0 + rr) * k_out + c] = (float)(P[rr * kc + c] / P[rr * kc + k_out]);
+    }
+}
+
+static size_t nystrom_smem(int d, int k_out) {
+    return (size_t)kNyRows * (kNyLm + 1) * 8 + (size_t)kNyLm * (k_out + 1) * 8 + 2 * (size_t)kNyRows * (d + 1) * 4;
 }
 
 int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y, int64_t n, float* Uy,
@@ -457,22 +554,17 @@ int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y, in
     if (!model || !Y || !Uy || n < 0) return set_error(ctx, KEVD_ERR_ARG, "nystrom_eval: bad arguments");
     if (n == 0) return KEVD_OK;
     const Model& m = model->m;
+    const int64_t n_blocks = (n + kNyRows - 1) / kNyRows;
+    const size_t smem = nystrom_smem(m.d, m.k_out);
+    if (smem > 227 * 1024 || n_blocks > (int64_t)INT32_MAX)
+        return set_error(ctx, KEVD_ERR_ARG, "nystrom_eval: unsupported size (d=%d, n=%lld)", m.d, (long long)n);
     cudaStream_t s = as_stream(stream);
-    int st = KEVD_OK;
-    double* Kys = arena_get<double>(ctx, "ny.K", (size_t)n * m.r, &st);
-    double* P = arena_get<double>(ctx, "ny.P", (size_t)n * (m.k_out + 1), &st);
-    if (st != KEVD_OK) return set_error(ctx, st, "nystrom_eval: out of device memory");
-    KEVD_TRY(launch_kernel_block(ctx, Y, n, m.d, m.scale, nullptr, 0, n, nullptr, m.r, KEVD_FP64, Kys,
-                                 m.r, s, m.xs));
-    // P (n x (k_out+1), col-major) = Kys (n x r, row-major) * zp (r x (k_out+1), col-major)
-    KEVD_BLAS(ctx, cublasSetStream(ctx->blas, s));
-    const double one = 1.0, zero = 0.0;
-    KEVD_BLAS(ctx, cublasDgemm(ctx->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, m.k_out + 1, (int)m.r, &one,
-                               Kys, (int)m.r, m.zp, (int)m.r, &zero, P, (int)n));
-    const int grid = (int)std::min<int64_t>((n * m.k_out + 255) / 256, (int64_t)ctx->num_sms * 8);
-    nystrom_ratio_kernel<<<grid, 256, 0, s>>>(P, n, m.k_out, Uy);
+    if (smem > 48 * 1024)
+        KEVD_CUDA(ctx, cudaFuncSetAttribute(nystrom_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+    nystrom_eval_kernel<<<(unsigned)n_blocks, 256, smem, s>>>(Y, n, m.xs, m.zp, m.r, m.d, m.k_out,
+                                                                         m.scale, Uy);
     KEVD_LAUNCH(ctx);
-    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
     return KEVD_OK;
 }
 

@@ -293,17 +293,37 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 }
 
 // ---- streaming passes on the column-major FP32 factor FT (k x ldT) ------------
-// Reads are coalesced along rows; products are FP32 (round to nearest) and the
-// long sums over rows or columns are FP64.
+// Reads are coalesced along rows.  The bistochastic scaling vectors are FP64
+// quantities: FP64 multipliers are carried as FP32 (hi, lo) pairs, each product
+// x * hi keeps its exact rounding error (fma), and short sums are double-FP32
+// pairs (two-sum), flushed into FP64.  The result is FP64-accurate (about
+// 1e-14 relative) while the arithmetic stays on the FP32 pipe, so the passes
+// remain HBM-bound.
+
+// (s, c) += x exactly up to the rounding of c: s + c is the running sum.
+__device__ __forceinline__ void df_add(float& s, float& c, float x) {
+    const float t = s + x;
+    const float z = t - s;
+    c += (s - (t - z)) + (x - z);
+    s = t;
+}
+
+// (s, c) += x * (wh + wl), with the product error of x * wh kept.
+__device__ __forceinline__ void df_fma(float& s, float& c, float x, float wh, float wl) {
+    const float p = __fmul_rn(x, wh);   // never contracted into the following add
+    const float pe = fmaf(x, wh, -p);
+    df_add(s, c, p);
+    c = fmaf(x, wl, c + pe);
+}
 
 // Partial column sums c[j] = sum_i w_i FT[j][i] (w == nullptr: ones) over this
-// CTA's row range.  CTA = 16 warps = 16 columns; the weights of each 2048-row
-// chunk are staged once in shared memory for all 16 columns; each lane sums 64
-// products in FP32, chunks are added in FP64.
+// CTA's row range.  CTA = 16 warps = 16 columns; the (hi, lo) weights of each
+// 2048-row chunk are staged once in shared memory for all 16 columns; each lane
+// sums 64 products as a double-FP32 pair, chunks are added in FP64.
 __global__ void __launch_bounds__(512)
 evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ w,
                   int64_t rows_per, double* __restrict__ partial) {
-    __shared__ float ws[2048];
+    __shared__ float wsh[2048], wsl[2048];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t j = (int64_t)blockIdx.x * 16 + warp;
     const int64_t r0 = (int64_t)blockIdx.y * rows_per;
@@ -312,13 +332,18 @@ evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     for (int64_t i0 = r0; i0 < r1; i0 += 2048) {
         const int n = (int)min((int64_t)2048, r1 - i0);
         __syncthreads();
-        for (int t = threadIdx.x; t < n; t += 512) ws[t] = w ? (float)w[i0 + t] : 1.f;
+        for (int t = threadIdx.x; t < n; t += 512) {
+            const double x = w ? w[i0 + t] : 1.0;
+            const float h = (float)x;
+            wsh[t] = h;
+            wsl[t] = (float)(x - (double)h);
+        }
         __syncthreads();
         if (j < k) {
             const float* col = FT + j * ldT + i0;
-            float part = 0.f;
-            for (int t = lane; t < n; t += 32) part = fmaf(col[t], ws[t], part);
-            acc += (double)part;
+            float ps = 0.f, pc = 0.f;
+            for (int t = lane; t < n; t += 32) df_fma(ps, pc, col[t], wsh[t], wsl[t]);
+            acc += (double)ps + (double)pc;
         }
     }
 #pragma unroll
@@ -326,8 +351,8 @@ evt_colsum_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     if (lane == 0 && j < k) partial[(int64_t)blockIdx.y * k + j] = acc;
 }
 
-// y_i = sum_j FT[j][i] v_j with v split into an FP32 hi/lo pair; FP64 every 32
-// terms; yinv = 1/y; bad |= (y <= 0).
+// y_i = sum_j FT[j][i] v_j with v as an FP32 (hi, lo) pair; double-FP32 sums
+// of 32 terms, FP64 across them; yinv = 1/y; bad |= (y <= 0).
 __global__ void __launch_bounds__(256)
 evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ v,
                   double* __restrict__ y, double* __restrict__ yinv, int* __restrict__ bad) {
@@ -342,13 +367,10 @@ evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     if (i >= N) return;
     double acc = 0.0;
     for (int64_t j0 = 0; j0 < k; j0 += 32) {
-        float part = 0.f;
+        float ps = 0.f, pc = 0.f;
         const int64_t j1 = min(k, j0 + 32);
-        for (int64_t j = j0; j < j1; ++j) {
-            const float f = FT[j * ldT + i];
-            part = fmaf(f, vhl[2 * j], fmaf(f, vhl[2 * j + 1], part));
-        }
-        acc += (double)part;
+        for (int64_t j = j0; j < j1; ++j) df_fma(ps, pc, FT[j * ldT + i], vhl[2 * j], vhl[2 * j + 1]);
+        acc += (double)ps + (double)pc;
     }
     y[i] = acc;
     yinv[i] = 1.0 / acc;
@@ -401,13 +423,15 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j (FP32 products, compensated sums).  thread: columns 4 (tid >> 4)..+4,
+// CTA's rows, for a block of 64 columns j (the FP64 weights U dinv as (hi, lo)
+// pairs, double-FP32 sums per CTA row range).  thread: columns 4 (tid >> 4)..+4,
 // U columns 2 (tid & 15)..+2.
 __global__ void __launch_bounds__(256)
 evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
               const double* __restrict__ dinv, int64_t rows_per, double* __restrict__ partial) {
     __shared__ float Fs[64][65];
     __shared__ __align__(16) float Ws[64][32];
+    __shared__ __align__(16) float Wl[64][32];
     const int tid = threadIdx.x;
     const int jr = 4 * (tid >> 4), qc = 2 * (tid & 15);
     const int64_t j0 = (int64_t)blockIdx.x * 64;
@@ -425,17 +449,21 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
         for (int e = tid; e < 64 * 32; e += 256) {
             const int ii = e >> 5, q = e & 31;
             const int64_t i = i0 + ii;
-            Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
+            const double x = (i < r1 && q < m) ? (double)U[i * m + q] * dinv[i] : 0.0;
+            const float h = (float)x;
+            Ws[ii][q] = h;
+            Wl[ii][q] = (float)(x - (double)h);
         }
         __syncthreads();
 #pragma unroll 8
         for (int ii = 0; ii < 64; ++ii) {
             const float w0 = Ws[ii][qc], w1 = Ws[ii][qc + 1];
+            const float l0 = Wl[ii][qc], l1 = Wl[ii][qc + 1];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const float f = Fs[jr + a][ii];
-                kahan_add(ks[a][0], kc[a][0], f * w0);
-                kahan_add(ks[a][1], kc[a][1], f * w1);
+                df_fma(ks[a][0], kc[a][0], f, w0, l0);
+                df_fma(ks[a][1], kc[a][1], f, w1, l1);
             }
         }
     }
@@ -446,7 +474,7 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
             const int q = qc + b;
-            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] - (double)kc[a][b];
+            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] + (double)kc[a][b];
         }
     }
 }
@@ -700,6 +728,78 @@ static int d2h(kevd_ctx* ctx, double* host, const double* dev, size_t n, cudaStr
     return KEVD_OK;
 }
 
+// Element-wise copies between the FP64 and FP32 k x k workspaces (column-major).
+__global__ void ev_d2f_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+__global__ void ev_f2d_kernel(const float* __restrict__ a, double* __restrict__ b, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
+// Leading eigenpairs of the FP64 matrix W (k x k) for an FP32 factor: an FP32
+// divide-and-conquer eigensolve of W rounded to FP32 gives the whole spectrum
+// (FP32-accurate) and the leading m-dimensional subspace; Rayleigh-Ritz on the
+// FP64 W over that subspace (two Cholesky-QR passes, then H = V^T W V and an
+// m x m FP64 eigensolve) gives the leading eigenpairs in FP64.  On return
+// lam[0..k) holds the spectrum (ascending; the top m entries from the FP64
+// Rayleigh-Ritz step) and V (k x m, column-major) the refined eigenvectors,
+// ascending.  flag receives the solver info (non-zero: failure).
+static int top_eigs_fp32_rr(kevd_ctx* ctx, const double* W, int64_t k, int m, double* lam, double* V, int* flag,
+                            cudaStream_t s) {
+    int st = KEVD_OK;
+    float* Wf = arena_get<float>(ctx, "ev.Wf", (size_t)k * k, &st);
+    float* lamf = arena_get<float>(ctx, "ev.lamf", k, &st);
+    double* Y = arena_get<double>(ctx, "ev.rrY", (size_t)k * m, &st);
+    double* H = arena_get<double>(ctx, "ev.rrH", (size_t)m * m, &st);
+    double* mu = arena_get<double>(ctx, "ev.rrmu", m, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+    const int grid = ctx->num_sms * 4;
+    ev_d2f_kernel<<<grid, 256, 0, s>>>(W, Wf, k * k);
+    KEVD_LAUNCH(ctx);
+    int lw = 0, lw2 = 0, lw3 = 0;
+    KEVD_SOLVER(ctx, cusolverDnSsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                 (int)k, Wf, (int)k, lamf, &lw));
+    KEVD_SOLVER(ctx, cusolverDnDsyevd_bufferSize(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m,
+                                                 H, m, mu, &lw2));
+    KEVD_SOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->solver, CUBLAS_FILL_MODE_UPPER, m, H, m, &lw3));
+    float* wf = arena_get<float>(ctx, "ev.swork", (size_t)lw + 1, &st);
+    double* wd = arena_get<double>(ctx, "ev.rrwork", (size_t)std::max(lw2, lw3) + 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+    {
+        ProfScope p3(ctx, "dense_syevd", s);
+        KEVD_SOLVER(ctx, cusolverDnSsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, (int)k, Wf,
+                                          (int)k, lamf, wf, lw, flag));
+    }
+    ProfScope pr(ctx, "dense_rr", s);
+    ev_f2d_kernel<<<grid, 256, 0, s>>>(lamf, lam, k);
+    KEVD_LAUNCH(ctx);
+    ev_f2d_kernel<<<grid, 256, 0, s>>>(Wf + (k - m) * k, V, k * m);
+    KEVD_LAUNCH(ctx);
+    const double one = 1.0, zero = 0.0;
+    // two Cholesky-QR passes: V <- V R^{-1}, R^T R = V^T V
+    for (int pass = 0; pass < 2; ++pass) {
+        KEVD_BLAS(ctx, cublasDsyrk(ctx->blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, m, (int)k, &one, V, (int)k,
+                                   &zero, H, m));
+        KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_UPPER, m, H, m, wd, lw3, flag + 1));
+        KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                                   CUBLAS_DIAG_NON_UNIT, (int)k, m, &one, H, m, V, (int)k));
+    }
+    // H = V^T W V, eigenpairs ascending; V <- V Q
+    KEVD_BLAS(ctx, cublasDsymm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, (int)k, m, &one, W, (int)k, V,
+                               (int)k, &zero, Y, (int)k));
+    KEVD_BLAS(ctx, cublasDgemm(ctx->blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, (int)k, &one, V, (int)k, Y, (int)k, &zero,
+                               H, m));
+    KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, H, m, mu,
+                                      wd, lw2, flag + 2));
+    KEVD_BLAS(ctx, cublasDgemm(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)k, m, m, &one, V, (int)k, H, m, &zero, Y,
+                               (int)k));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(V, Y, (size_t)k * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    KEVD_CUDA(ctx, cudaMemcpyAsync(lam + (k - m), mu, (size_t)m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return KEVD_OK;
+}
+
 template <typename T>
 static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF, int k_out,
                     double* lam_h, float* U, kevd_evd_info* info, kevd_evd_dump* dump,
@@ -817,14 +917,33 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     ev_symmetrize_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(W, k);
     KEVD_LAUNCH(ctx);
     if (dump) KEVD_TRY(d2h(ctx, dump->W, W, (size_t)k * k, s));
-    {
-        ProfScope p3(ctx, "dense_syevd", s);
-        KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                          (int)k, W, (int)k, lam, work, lwork2, flags + 3));
+    if (sizeof(T) == 4) {
+        // FP32 factor: FP32 eigensolve + FP64 Rayleigh-Ritz of the leading subspace
+        const int m = (int)std::min<int64_t>(k, k_out + 16);
+        double* V = arena_get<double>(ctx, "ev.rrV", (size_t)k * m, &st);
+        int* rrflag = arena_get<int>(ctx, "ev.rrflag", 3, &st);
+        if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+        KEVD_CUDA(ctx, cudaMemsetAsync(rrflag, 0, 3 * sizeof(int), s));
+        KEVD_TRY(top_eigs_fp32_rr(ctx, W, k, m, lam, V, rrflag, s));
+        int hrr[3];
+        KEVD_CUDA(ctx, cudaMemcpyAsync(hrr, rrflag, sizeof(hrr), cudaMemcpyDeviceToHost, s));
+        KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+        if (hrr[0] != 0 || hrr[1] != 0 || hrr[2] != 0)
+            return set_error(ctx, KEVD_ERR_SYEVD, "bistochastic_evd: eigensolve failed, info %d/%d/%d", hrr[0],
+                             hrr[1], hrr[2]);
+        // Z = L^{-T} V[:, m-k_out:]
+        KEVD_CUDA(ctx, cudaMemcpyAsync(Z, V + (size_t)(m - k_out) * k, (size_t)k * k_out * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, s));
+    } else {
+        {
+            ProfScope p3(ctx, "dense_syevd", s);
+            KEVD_SOLVER(ctx, cusolverDnDsyevd(ctx->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                              (int)k, W, (int)k, lam, work, lwork2, flags + 3));
+        }
+        // Z = L^{-T} V[:, k-k_out:]
+        KEVD_CUDA(ctx, cudaMemcpyAsync(Z, W + (k - k_out) * k, (size_t)k * k_out * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, s));
     }
-    // Z = L^{-T} V[:, k-k_out:]
-    KEVD_CUDA(ctx, cudaMemcpyAsync(Z, W + (k - k_out) * k, (size_t)k * k_out * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, s));
     KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
                                CUBLAS_DIAG_NON_UNIT, (int)k, k_out, &one, A, (int)k, Z, (int)k));
     // pass 4: U = Dtil^{-1} F Z

@@ -12,16 +12,22 @@
 // ks_kevd.cu:1152-1158).  The relative error of a Gram entry is about 1e-5;
 // eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
 //
-// CTA roles (416 threads):
+// CTA roles (320 threads):
 //   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
 //               lanes 32q..32q+31 = tile rows)
-//   warps 4-11  converters: coalesced float4 loads of 32 rows x 128 columns
-//               of F for the a and b column blocks, row scaling, tf32 split,
-//               transposed stores into K-major SW128 operand tiles
-//   warp 12     TMEM allocation and the single MMA-issuing thread
-// A 3-stage shared-memory ring (64 KB per stage: a_hi, a_lo, b_hi, b_lo)
-// and a double-buffered TMEM accumulator (2 x 128 columns) are handed over
-// with mbarriers; every wait is bounded and sets an error flag on timeout.
+//   warps 4-7   converters: thread m owns row m of both operand tiles (factor
+//               columns a0+m and b0+m, 32 rows of F each): row scaling and the
+//               tf32 split; the a operand goes to Tensor Memory (tcgen05.st,
+//               hi and lo columns per stage), the b operand stays in shared
+//               memory (hi in place, lo beside it)
+//   warp 8      TMA producer
+//   warp 9      TMEM allocation and the single MMA-issuing thread (A from
+//               Tensor Memory, B from shared memory)
+// A 3-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
+// double-buffered TMEM accumulator (2 x 128 columns) are handed over with
+// mbarriers; every wait is bounded and sets an error flag on timeout.
+// Keeping the a operand out of shared memory removes its split stores and the
+// MMA's a-operand reads (about 80 KB of shared-memory traffic per stage).
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
@@ -37,7 +43,9 @@ namespace {
 constexpr int kTT = 128;               // output tile edge
 constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
 constexpr int kStages = 3;
-constexpr int kPrefetch = 6;          // stages of F prefetched into L2 ahead of the ring
+constexpr int kPrefetch = 0;          // stages of F prefetched into L2 ahead of the ring (0: off;
+                                      // at N = 2M, k = 2000 a 6-stage prefetch cost 1.8x: it
+                                      // broke the L2 sharing of panels between CTAs)
 constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
 constexpr int kStageBytes = 4 * kOpBytes;   // a_hi, a_lo, b_hi, b_lo
@@ -47,7 +55,9 @@ constexpr int kCvtWarps = 4;
 constexpr int kProdWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kThreads = 10 * 32;
-constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kTmemCols = 512;       // accumulators [0,256), a-operand slots [256,448)
+constexpr uint32_t kTmemA = 256;
+constexpr uint32_t kTmemASlot = 64;       // hi columns [0,32), lo [32,64)
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
@@ -79,27 +89,37 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
 // 16-byte chunk holds 4 consecutive rows k of one column m.
 constexpr int kStageAlloc = 4 * kOpBytes + 1024;   // keeps every stage 1024-aligned
 
-// Thread ct handles the 16-byte chunks ct + 128 q (q < 8) of a tile: row
-// m = (ct + 128 q) / 8 and logical K chunk kc = (ct & 7) ^ ((ct >> 3) & 7),
-// the same for every q, so it needs the weights of rows 4 kc .. 4 kc + 3 only.
-__device__ __forceinline__ void split_tile(uint8_t* hi, uint8_t* lo, const float (&w)[4], int64_t a0, int64_t k,
-                                           int ct) {
+// Row m of a K-major SW128 tile: its 8 16-byte chunks (K = 4c .. 4c+3).
+__device__ __forceinline__ void load_row(const uint8_t* tile, int m, float (&x)[32]) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;
-        const uint32_t m = off >> 7;                                   // tile column
-        float4 v = *reinterpret_cast<float4*>(hi + off);
-        const bool colok = (a0 + (int64_t)m) < k;
-        float x[4] = {v.x, v.y, v.z, v.w}, h[4], l[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float y = colok ? x[u] * w[u] : 0.f;
-            h[u] = tc::tf32_rn(y);
-            l[u] = tc::tf32_rn(y - h[u]);
-        }
-        *reinterpret_cast<float4*>(hi + off) = make_float4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<float4*>(lo + off) = make_float4(l[0], l[1], l[2], l[3]);
+    for (int c = 0; c < 8; ++c) {
+        const float4 v = *reinterpret_cast<const float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c));
+        x[4 * c] = v.x;
+        x[4 * c + 1] = v.y;
+        x[4 * c + 2] = v.z;
+        x[4 * c + 3] = v.w;
     }
+}
+
+__device__ __forceinline__ void store_row(uint8_t* tile, int m, const float (&x)[32]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        *reinterpret_cast<float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c)) =
+            make_float4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
+}
+
+// y = w * x (zero for factor columns >= k), hi = rn_tf32(y), lo = rn_tf32(y - hi)
+__device__ __forceinline__ void scale_split(float (&y)[32], float (&h)[32], const float (&w)[32], bool colok) {
+#pragma unroll
+    for (int u = 0; u < 32; ++u) {
+        y[u] = colok ? y[u] * w[u] : 0.f;
+        h[u] = tc::tf32_rn(y[u]);
+    }
+}
+
+__device__ __forceinline__ void lo_part(const float (&y)[32], float (&h)[32]) {
+#pragma unroll
+    for (int u = 0; u < 32; ++u) h[u] = tc::tf32_rn(y[u] - h[u]);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -157,7 +177,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                 }
                 uint8_t* st = base + (size_t)slot * kStageAlloc;
                 const int x = (int)(r0 + s * kTK);
-                if (s + kPrefetch < n_stages) {
+                if (kPrefetch > 0 && s + kPrefetch < n_stages) {
                     const int xp = (int)(r0 + (s + kPrefetch) * kTK);
                     tc::tma_prefetch_2d(&tmF, xp, (int)a0);
                     if (!diag) tc::tma_prefetch_2d(&tmF, xp, (int)b0);
@@ -169,9 +189,10 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
         }
         __syncwarp();
     } else if (warp >= kCvtWarp0 && warp < kCvtWarp0 + kCvtWarps) {
-        // ---------------- converters (128 threads, 8 chunks of 16 B per tile each)
-        const int ct = (warp - kCvtWarp0) * 32 + lane;
-        const int kc = (ct & 7) ^ ((ct >> 3) & 7);
+        // ---------------- converters: thread m owns row m of the a and b tiles
+        const int m = (warp - kCvtWarp0) * 32 + lane;
+        const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);   // this warp's TMEM lanes
+        const bool aok = (a0 + m) < k, bok = (b0 + m) < k;
         // row weights one stage ahead of their use
         float sv_next = (r0 + lane < r1) ? (float)__ldg(srow + r0 + lane) : 0.f;
         for (int64_t s = 0; s < n_stages; ++s) {
@@ -180,17 +201,36 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
             const float sv = sv_next;
             const int64_t inext = r0 + (s + 1) * kTK + lane;
             sv_next = (inext < r1) ? (float)__ldg(srow + inext) : 0.f;
-            float w[4];
+            float w[32];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) w[u] = __shfl_sync(0xffffffffu, sv, 4 * kc + u);
+            for (int u = 0; u < 32; ++u) w[u] = __shfl_sync(0xffffffffu, sv, u);
             if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
                 atomicExch(err, 5);
                 break;
             }
             uint8_t* st = base + (size_t)slot * kStageAlloc;
-            split_tile(st, st + kOpBytes, w, a0, k, ct);
-            if (!diag) split_tile(st + 2 * kOpBytes, st + 3 * kOpBytes, w, b0, k, ct);
+            float y[32], h[32];
+            // a operand -> Tensor Memory
+            const uint32_t ta = tlane + kTmemA + (uint32_t)slot * kTmemASlot;
+            load_row(st, m, y);
+            scale_split(y, h, w, aok);
+            tc::tmem_st32(ta, h);
+            if (diag) store_row(st, m, h);
+            lo_part(y, h);
+            tc::tmem_st32(ta + 32, h);
+            if (diag) {
+                store_row(st + kOpBytes, m, h);   // b = a: hi in place, lo beside it
+            } else {
+                uint8_t* bt = st + 2 * kOpBytes;
+                load_row(bt, m, y);
+                scale_split(y, h, w, bok);
+                store_row(bt, m, h);
+                lo_part(y, h);
+                store_row(st + 3 * kOpBytes, m, h);
+            }
+            tc::tmem_wait_st();
             tc::fence_async_smem();
+            tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }
@@ -219,19 +259,17 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                     }
                     tc::tc_fence_after();
                     uint8_t* st = base + (size_t)slot * kStageAlloc;
-                    const uint32_t ahi = tc::smem_u32(st), alo = tc::smem_u32(st + kOpBytes);
-                    const uint32_t bhi = diag ? ahi : tc::smem_u32(st + 2 * kOpBytes);
-                    const uint32_t blo = diag ? alo : tc::smem_u32(st + 3 * kOpBytes);
+                    const uint32_t ahi = tbase + kTmemA + (uint32_t)slot * kTmemASlot, alo = ahi + 32;
+                    const uint32_t bhi = diag ? tc::smem_u32(st) : tc::smem_u32(st + 2 * kOpBytes);
+                    const uint32_t blo = diag ? tc::smem_u32(st + kOpBytes) : tc::smem_u32(st + 3 * kOpBytes);
 #pragma unroll
                     for (int j = 0; j < kTK / 8; ++j) {
-                        const uint32_t koff = (uint32_t)(j * 32);   // 8 tf32 = 32 bytes
-                        const uint64_t dah = tc::desc_kmajor_sw128(ahi + koff);
-                        const uint64_t dal = tc::desc_kmajor_sw128(alo + koff);
+                        const uint32_t koff = (uint32_t)(j * 32);   // 8 tf32 = 32 bytes = 8 TMEM columns
                         const uint64_t dbh = tc::desc_kmajor_sw128(bhi + koff);
                         const uint64_t dbl = tc::desc_kmajor_sw128(blo + koff);
-                        tc::mma_tf32(d, dah, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
-                        tc::mma_tf32(d, dal, dbh, idesc, 1u);
-                        tc::mma_tf32(d, dah, dbh, idesc, 1u);
+                        tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
+                        tc::mma_tf32_tmem_a(d, alo + 8 * j, dbh, idesc, 1u);
+                        tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbh, idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[slot]);
                 }
@@ -294,17 +332,17 @@ __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    // resolved once per process (thread-safe static initialisation)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            cudaGetLastError();
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 

@@ -30,6 +30,11 @@ class Arena {
     ~Arena() { release(); }
     void* get(const std::string& name, size_t bytes, int* status);
     void release();
+    size_t total() const {
+        size_t t = 0;
+        for (const auto& kv : bufs_) t += kv.second.n;
+        return t;
+    }
 
   private:
     struct Buf {
@@ -159,6 +164,10 @@ int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double 
                         const int64_t* rows, int64_t row0, int64_t nrows, const int64_t* cols,
                         int64_t ncols, int precision, void* out, int64_t ld, cudaStream_t s,
                         const float* Xc = nullptr);
+int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs, int tiles_per_item,
+                          cudaStream_t s);
+int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales, int n_scales,
+                       double* sums, cudaStream_t s);
 int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
                   int n_scales, double* sums, cudaStream_t s);
 int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales, int n_scales, double* sums,

@@ -18,12 +18,17 @@
 // CTA (320 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
 //              and the pre-split S_i tiles (bulk copy)
-//   warp 1     TMEM allocation and the single MMA-issuing thread
-//   warps 2,3,8,9  converters: in-place hi / separate lo of the F tile, columns
-//              >= r zeroed
+//   warp 1     TMEM allocation and the single MMA-issuing thread (A from
+//              Tensor Memory, B from shared memory)
+//   warps 2,3,8,9  converters: thread m owns row m of the F tile (its TMEM lane
+//              quarter is warp % 4), zeroes columns >= r and writes the hi and
+//              lo parts into the stage's Tensor Memory a-slot (tcgen05.st)
 //   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
-// Ring of 3 shared-memory stages and 8 TMEM partial buffers of 64 columns,
-// handed over with mbarriers; every wait is bounded (error flag on timeout).
+// Ring of 4 stages (shared-memory tiles + Tensor Memory a-slots of 64 columns)
+// and 4 TMEM partial buffers of 64 columns, handed over with mbarriers; every
+// wait is bounded (error flag on timeout).  The F tile never goes back to
+// shared memory split, so per stage the shared-memory traffic is the TMA write,
+// one read by the converters and the MMA's B reads.
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
@@ -39,13 +44,15 @@ namespace {
 constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
-constexpr int kStages = 3;
+constexpr int kStages = 4;
 constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
-constexpr int kBufs = 8;            // TMEM partial buffers (8 x 64 = all 512 columns)
+constexpr int kBufs = 4;            // TMEM partial buffers, columns [0, 256)
 constexpr int kPerPartial = 2;      // 32-column stages accumulated per TMEM partial
+constexpr uint32_t kTmemA = kBufs * 64;   // a-slots: columns [256, 512), 64 per stage (hi 32, lo 32)
+constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
-constexpr int kStageBytes = 2 * kAOp + 2 * kBOp;   // a_hi, a_lo, b_hi, b_lo
+constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
 constexpr int kThreads = 320;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = 128;
@@ -63,7 +70,6 @@ struct Bars {
 };
 
 __device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || w == 8 || w == 9; }
-__device__ __forceinline__ int cvt_index(int w) { return w < 4 ? w - 2 : w - 6; }
 
 struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
     int64_t rank;
@@ -116,7 +122,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         tc::mbar_fence_init();
     }
     if (warp == 1) {
-        tc::tmem_alloc(&bar->tmem_base, kBufs * kCols);
+        tc::tmem_alloc(&bar->tmem_base, kTmemCols);
         tc::tmem_relinquish();
     }
     tc::tc_fence_before();
@@ -145,7 +151,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     }
                     tc::mbar_arrive_expect_tx(&bar->tma_full[slot], kAOp + 2 * kBOp);
                     tc::tma_load_2d(stg, &tmap, s * kKs, (int)(rb * kRows), &bar->tma_full[slot]);
-                    tc::bulk_load(stg + 2 * kAOp, bprep + (size_t)s * 2 * kBOp, 2 * kBOp, &bar->tma_full[slot]);
+                    tc::bulk_load(stg + kAOp, bprep + (size_t)s * 2 * kBOp, 2 * kBOp, &bar->tma_full[slot]);
                 }
             }
             if (!ok) atomicExch(err, 11);
@@ -184,19 +190,17 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     }
                     tc::tc_fence_after();
                     uint8_t* stg = base + (size_t)slot * kStageBytes;
-                    const uint32_t ahi = tc::smem_u32(stg), alo = tc::smem_u32(stg + kAOp);
-                    const uint32_t bhi = tc::smem_u32(stg + 2 * kAOp), blo = tc::smem_u32(stg + 2 * kAOp + kBOp);
+                    const uint32_t ahi = tbase + kTmemA + (uint32_t)slot * 64u, alo = ahi + 32u;
+                    const uint32_t bhi = tc::smem_u32(stg + kAOp), blo = tc::smem_u32(stg + kAOp + kBOp);
                     const uint32_t dt = tbase + (uint32_t)(tb * kCols);
 #pragma unroll
                     for (int j = 0; j < kKs / 8; ++j) {
-                        const uint32_t ko = (uint32_t)(j * 32);
-                        const uint64_t dah = tc::desc_kmajor_sw128(ahi + ko);
-                        const uint64_t dal = tc::desc_kmajor_sw128(alo + ko);
+                        const uint32_t ko = (uint32_t)(j * 32);   // 8 tf32: 32 bytes of B, 8 TMEM columns of A
                         const uint64_t dbh = tc::desc_kmajor_sw128(bhi + ko);
                         const uint64_t dbl = tc::desc_kmajor_sw128(blo + ko);
-                        tc::mma_tf32(dt, dal, dbh, idesc, (j > 0 || !first) ? 1u : 0u);
-                        tc::mma_tf32(dt, dah, dbl, idesc, 1u);
-                        tc::mma_tf32(dt, dah, dbh, idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh, idesc, (j > 0 || !first) ? 1u : 0u);
+                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbl, idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh, idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[slot]);
                     if (last) {
@@ -211,8 +215,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         }
         __syncwarp();
     } else if (is_cvt_warp(warp)) {
-        // ---------------- converters: 128 threads, 8 float4 each per stage
-        const int ct = cvt_index(warp) * 32 + lane;
+        // ---------------- converters: thread m owns row m of the F tile
+        const int m = 32 * (warp & 3) + lane;
+        const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
         int64_t g = 0;
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
             bool ok = true;
@@ -224,27 +229,26 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     ok = false;
                     break;
                 }
-                uint8_t* stg = base + (size_t)slot * kStageBytes;
+                const uint8_t* stg = base + (size_t)slot * kStageBytes;
                 const int64_t cbase = (int64_t)s * kKs;
+                float h[32], l[32];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const uint32_t off = (uint32_t)(ct + 128 * q) * 16u;   // 16-byte chunk
-                    const uint32_t row = off >> 7;
-                    const uint32_t chunk = ((off >> 4) & 7u) ^ (row & 7u);  // logical K chunk
-                    float4 a = *reinterpret_cast<float4*>(stg + off);
-                    float v[4] = {a.x, a.y, a.z, a.w};
-                    float h[4], l[4];
+                for (int c = 0; c < 8; ++c) {
+                    const float4 a =
+                        *reinterpret_cast<const float4*>(stg + tc::sw128_off((uint32_t)m, (uint32_t)(4 * c)));
+                    const float v[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        const int64_t col = cbase + 4 * chunk + u;
-                        const float x = (col < r) ? v[u] : 0.f;
-                        h[u] = tc::tf32_rn(x);
-                        l[u] = tc::tf32_rn(x - h[u]);
+                        const float x = (cbase + 4 * c + u < r) ? v[u] : 0.f;
+                        h[4 * c + u] = tc::tf32_rn(x);
+                        l[4 * c + u] = tc::tf32_rn(x - h[4 * c + u]);
                     }
-                    *reinterpret_cast<float4*>(stg + off) = make_float4(h[0], h[1], h[2], h[3]);
-                    *reinterpret_cast<float4*>(stg + kAOp + off) = make_float4(l[0], l[1], l[2], l[3]);
                 }
-                tc::fence_async_smem();
+                const uint32_t ta = tlane + kTmemA + (uint32_t)slot * 64u;
+                tc::tmem_st32(ta, h);
+                tc::tmem_st32(ta + 32u, l);
+                tc::tmem_wait_st();
+                tc::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&bar->cvt_full[slot]);
             }
@@ -350,7 +354,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 1) tc::tmem_dealloc(tbase, kBufs * kCols);
+    if (warp == 1) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
 // K(:, S_i) for the round, FP32 from direct differences: Kc[i][c], 64 columns
@@ -435,17 +439,17 @@ __global__ void update_prep_kernel(const float* __restrict__ F, int64_t ldF, con
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    // resolved once per process (thread-safe static initialisation)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            cudaGetLastError();
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 

@@ -59,3 +59,21 @@ def test_select_is_host_only_and_matches_oracle(lib):
 def test_null_context_is_an_argument_error(lib):
     lib.kevd_calibrate.restype = ctypes.c_int
     assert lib.kevd_calibrate(None, None, 0, 0, None, 0, None, None) == 1
+
+
+def test_server_arguments_and_footprint_without_gpu(lib):
+    from kernel_evd_gb300 import _lib
+    L = _lib.load()
+    cfg = _lib.ServerConfig(0, 0, 4096, 1 << 30, 0.0)            # no factor worker
+    h = ctypes.c_void_p()
+    assert L.kevd_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert L.kevd_server_create(None, ctypes.byref(h)) == 1
+    cfg = _lib.ServerConfig(0, 2, 0, 1 << 30, 0.0)               # empty query batch
+    assert L.kevd_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    # footprint: F and its transposed copy dominate; FP64 factors cost more
+    N, d, k = 2_000_000, 64, 2000
+    fm = L.kevd_factorization_footprint(N, d, k, 32, 1)
+    f64 = L.kevd_factorization_footprint(N, d, k, 32, 0)
+    assert 2 * 4 * N * k < fm < 3 * 4 * N * k and f64 > fm + 2 * 4 * N * k
+    assert L.kevd_factorization_footprint(0, d, k, 32, 1) == -1
+    assert L.kevd_factorization_footprint(N, d, k, 32, 7) == -1

@@ -57,6 +57,17 @@ def test_calibrate_matches_oracle(ctx, states, N):
     np.testing.assert_array_less(T[~mask], 1e-25 * N * N + 1e-300)
 
 
+@pytest.mark.parametrize("N", [2, 129, 1000])
+def test_calibrate_fp64_matches_oracle(ctx, states, N):
+    from kernel_evd_gb300 import api
+    Xn = np.ascontiguousarray(states[:N])
+    eps = calibrate.log_sweep(100.0, 64)
+    T = api.calibrate(ctx, torch.from_numpy(Xn).cuda(), 1.0 / eps, precision="fp64")
+    ref = calibrate.pair_sums(Xn.astype(np.float64), 1.0 / eps)
+    # FP64 distances from the same FP32 states, FP64 exp: summation order only
+    np.testing.assert_allclose(T, ref, rtol=1e-12, atol=1e-300)
+
+
 def test_calibrate_reference_sweep_hankel(ctx):
     from kernel_evd_gb300 import api
     rng = np.random.default_rng(3)
@@ -102,3 +113,23 @@ def test_pair_median_exact_and_sampled(ctx, states):
     D = ((Xn[pi].astype(np.float64) - Xn[pl].astype(np.float64)) ** 2).sum(1)
     refs = np.sort(D)[(D.size - 1) // 2]
     assert abs(ms - refs) <= 2e-6 * refs
+
+
+def test_calibrate_batched_matches_single(ctx):
+    """Uneven datasets (N, d) in one persistent launch: each job's sums equal the
+    single-dataset pass up to FP64 summation order, for any work-item size."""
+    from kernel_evd_gb300 import api
+    shapes = [(1, 64), (2, 32), (129, 128), (700, 64), (3000, 32), (1500, 128)]
+    Xs, scs = [], []
+    for q, (n, m) in enumerate(shapes):
+        Xn = ks.seeded_mode(max(n, 2), M=m, seed=q, warm_time=50.0)[:n].astype(np.float32)
+        Xs.append(torch.from_numpy(np.ascontiguousarray(Xn)).cuda())
+        scs.append(1.0 / calibrate.log_sweep(10.0 * m, 41 if q % 2 else 64))
+    single = [api.calibrate(ctx, X, sc) for X, sc in zip(Xs, scs)]
+    for tpi in (0, 1, 7):
+        batched = api.calibrate_batched(ctx, Xs, scs, tiles_per_item=tpi)
+        for q in range(len(shapes)):
+            np.testing.assert_allclose(batched[q], single[q], rtol=1e-12, atol=1e-300, err_msg=f"job {q} tpi {tpi}")
+    ref = calibrate.pair_sums(Xs[4].cpu().numpy().astype(np.float64), scs[4])
+    mask = ref > 1e-30
+    np.testing.assert_allclose(batched[4][mask], ref[mask], rtol=1e-4)
