@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=40000, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--cal-n", type=int, default=200_000, help="states in the calibration measurement (0: skip)")
+    ap.add_argument("--c4-datasets", type=int, default=48, help="datasets in the batched phase (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the serving window (0: no serving phase)")
     ap.add_argument("--fact-rate", type=float, default=20.0, help="factorization requests per second")
@@ -189,6 +190,99 @@ def calibration_phase(ctx, Xd, args, sm_mhz):
             "vs_fp64": {"rows": n64, "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
                         "scales_compared": int(mask.sum()), "same_selected_eps": sel32["idmax"] == sel64["idmax"],
                         "fp64_pass_s": t64}}
+
+
+def batched_phase(ctx, args):
+    """48 uneven datasets through one batched pipeline: KS with L in {16, 22, 36},
+    d in {32, 64, 128} gridpoints, N log-uniform in [1e4, 4e5], rank k uniform in
+    [100, 1000] (dataset i draws from default_rng(1000 + i), seed i), b = 32.
+    Per dataset: median squared distance of a seeded 1e7-pair sample, 41
+    log-spaced eps in 2^-10..2^10 x median, max-slope eps; then block RPCholesky
+    (mixed) and the bistochastic EVD, top 16.  The 48 calibrations are one
+    persistent launch over a device work queue (item size autotuned); the 48
+    factorisations are one captured CUDA graph; the EVDs run back to back.
+    Each dataset is checked against the plain FP64 EVD on the same pivots."""
+    import concurrent.futures as cf
+    import torch
+    from kernel_evd_gb300 import api, autotune, datagen
+    n_sets = args.c4_datasets
+    specs = []
+    for i in range(n_sets):
+        rng = np.random.default_rng(1000 + i)
+        L = float(rng.choice([16.0, 22.0, 36.0]))
+        m = int(rng.choice([32, 64, 128]))
+        n = int(np.exp(rng.uniform(np.log(1e4), np.log(4e5))))
+        k = int(rng.integers(100, 1001))
+        specs.append((L, m, n, k, i))
+    t0 = time.time()
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        data = list(ex.map(lambda sp: datagen.seeded_states(sp[2], L=sp[0], M=sp[1], seed=sp[4], warm_time=1000.0,
+                                                             dt=0.25), specs))
+    gen_s = time.time() - t0
+    Xs = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).cuda() for x in data]
+    torch.cuda.synchronize()
+    timings = {}
+    t0 = time.time()
+    meds = []
+    for X in Xs:
+        pi, pl = sample_pairs(X.shape[0], 10_000_000, seed=0)
+        meds.append(api.pair_median(ctx, X, pairs=(torch.from_numpy(pi).cuda(), torch.from_numpy(pl).cuda())))
+    timings["median_s"] = time.time() - t0
+    eps_list = [api.log_sweep(md, 41) for md in meds]
+    scales = [1.0 / e for e in eps_list]
+    tune_c = autotune.tune_calibration_items(ctx, Xs, scales)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    sums = api.calibrate_batched(ctx, Xs, scales, tiles_per_item=tune_c["tiles_per_item"])
+    timings["calibration_s"] = time.time() - t0
+    eopt = [api.select_bandwidth(eps_list[q], sums[q], Xs[q].shape[0])["eopt"] for q in range(n_sets)]
+    ks_ = [min(sp[3], sp[2] // 2) for sp in specs]
+    torch.cuda.synchronize()
+    t0 = time.time()
+    facs = api.rpcholesky_batched(ctx, Xs, [1.0 / e for e in eopt], ks_, 32, seeds=list(range(n_sets)),
+                                  use_graph=True)
+    timings["rpcholesky_graph_s"] = time.time() - t0
+    t0 = time.time()
+    evs = []
+    failed = 0
+    for f in facs:
+        try:
+            evs.append(api.bistochastic_evd(ctx, f.factor, k_out=16))
+        except api.KevdError:
+            evs.append(None)
+            failed += 1
+    torch.cuda.synchronize()
+    timings["evd_s"] = time.time() - t0
+    total = sum(timings.values())
+    pairs_eps = float(sum(X.shape[0] * (X.shape[0] - 1) / 2 * 41 for X in Xs))
+    # FP64 on the same pivots, per dataset
+    t0 = time.time()
+    errs = []
+    singular = []   # datasets whose pivot set is numerically singular in FP64 (rank reached before k)
+    for q, (f, ev) in enumerate(zip(facs, evs)):
+        if ev is None:
+            continue
+        try:
+            F64 = api.factor_from_pivots(ctx, Xs[q], f.scale, f.piv, precision="fp64")
+            ev64 = api.bistochastic_evd(ctx, F64, k_out=16)
+        except api.KevdError:
+            singular.append(q)
+            continue
+        errs.append(float(np.abs(ev.lam[-16:] - ev64.lam[-16:]).max()))
+        del F64
+    check_s = time.time() - t0
+    return {"datasets": n_sets, "seconds": total, "stages": timings, "datagen_s": gen_s,
+            "calibration_pair_eps_per_s": pairs_eps / timings["calibration_s"],
+            "autotune": {"calibration_tiles_per_item": tune_c["tiles_per_item"], "calibration_ms": tune_c["ms"]},
+            "ranks": [int(f.rank) for f in facs], "trace_error_max": float(max(f.trace_error for f in facs)),
+            "evd_failed": failed, "top16_eig_err_vs_fp64_same_pivots_max": float(max(errs)) if errs else None,
+            "top16_eig_err_median": float(np.median(errs)) if errs else None, "fp64_check_s": check_s,
+            "fp64_checked": len(errs),
+            "fp64_pivots_singular": {"count": len(singular),
+                                     "trace_error_min": float(min(facs[q].trace_error for q in singular))
+                                     if singular else None},
+            "config": "KS L in {16,22,36}, d in {32,64,128}, N log-uniform [1e4,4e5], k uniform [100,1000], b=32, "
+                      "seeds 0..47, 41 eps each; calibration = one persistent launch, factorisations = one CUDA graph"}
 
 
 def serving_phase(ctx, X, Xd, scale, args):
@@ -510,13 +604,24 @@ def main():
                "sample": f"first {n_s} of {N} states, k={args.k}, b={args.b}: rows-proportional "
                          f"{tb['stream_s']:.2f} s x {N}/{n_s} + dense {tb['dense_s']:.2f} s"}
     # --- fused calibration at N = 200,000, 64 eps
+    def phase(name, fn, *a):
+        """An extra measurement block: a failure is recorded, the headline line still prints."""
+        try:
+            result[name] = fn(*a)
+        except Exception as e:  # noqa: BLE001
+            result[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+        torch.cuda.synchronize()
+
     if args.cal_n > 0:
-        result["calibration"] = calibration_phase(ctx, Xd, args, (clocks or {}).get("sm_mhz"))
+        phase("calibration", calibration_phase, ctx, Xd, args, (clocks or {}).get("sm_mhz"))
     # --- serving loop under load (after the timed regions; frees the step's buffers first)
-    if args.serve_seconds > 0:
-        del F, U
+    del F, U
+    torch.cuda.empty_cache()
+    if args.c4_datasets > 0:
+        phase("batched", batched_phase, ctx, args)
         torch.cuda.empty_cache()
-        result["serving"] = serving_phase(ctx, X, Xd, scale, args)
+    if args.serve_seconds > 0:
+        phase("serving", serving_phase, ctx, X, Xd, scale, args)
     # --- max over ranks
     val = ms / 1e3
     if dist is not None:

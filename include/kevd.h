@@ -189,6 +189,32 @@ int kevd_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                 int64_t ldF, int64_t* piv, double* err, int32_t* accepted,
                 kevd_rpchol_result* result, void* stream);
 
+/* Many mixed-precision factorisations at once (no reference counterpart).
+ * Each job has its own X (device), FP32 factor F (device, N x ldF) and seed;
+ * piv (host, k_max entries) receives the pivots and result the rank, rounds
+ * and trace error.  use_graph != 0: the round loops of all jobs are captured
+ * as parallel branches of one CUDA graph (forked from stream, joined back)
+ * and launched once; every job runs max_rounds rounds on the device (kernels
+ * return at once after the stop).  use_graph == 0: the same work is issued on
+ * one stream per job. */
+typedef struct {
+    const float* X;
+    int64_t N;
+    int32_t d;
+    int32_t block;
+    double scale;
+    void* F;
+    int64_t ldF;
+    int64_t k_max;
+    int32_t max_rounds;
+    int32_t pad;
+    uint64_t seed;
+    int64_t* piv;
+    kevd_rpchol_result result;
+} kevd_rpchol_job;
+int kevd_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int32_t n_jobs,
+                        int32_t use_graph, void* stream);
+
 /* The reference's /linv output: L^{-1} (r x r, column-major, lower, zeros
  * stored) with L = F(S,:) (ks_arpclm.cu:1055-1095).  F: device; piv: host;
  * Linv: host. */

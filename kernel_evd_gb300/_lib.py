@@ -9,7 +9,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libkevd.so")
+LIB_PATH = os.environ.get("KEVD_LIB") or os.path.join(HERE, "lib", "libkevd.so")
 
 KEVD_FP64 = 0
 KEVD_MIXED = 1
@@ -42,6 +42,13 @@ class RpcholResult(C.Structure):
 
 class EvdInfo(C.Structure):
     _fields_ = [("trace_A", C.c_double), ("shift", C.c_double)]
+
+
+class RpcholJob(C.Structure):
+    _fields_ = [("X", C.c_void_p), ("N", C.c_int64), ("d", C.c_int32), ("block", C.c_int32),
+                ("scale", C.c_double), ("F", C.c_void_p), ("ldF", C.c_int64), ("k_max", C.c_int64),
+                ("max_rounds", C.c_int32), ("pad", C.c_int32), ("seed", C.c_uint64), ("piv", C.c_void_p),
+                ("result", RpcholResult)]
 
 
 class CalibJob(C.Structure):
@@ -83,6 +90,7 @@ SIGNATURES = {
     "kevd_calibrate": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),
     "kevd_calibrate_fp64": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),
     "kevd_calibrate_batched": (C.c_int, [_P, C.POINTER(CalibJob), _I32, _I32, _P]),
+    "kevd_rpchol_batched": (C.c_int, [_P, C.POINTER(RpcholJob), _I32, _I32, _P]),
     "kevd_calibrate_noalloc": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P]),
     "kevd_calibrate_select": (C.c_int, [_P, _P, _I32, _I64, _P, _P, _P, _P, _P]),
     "kevd_pair_median": (C.c_int, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P]),

@@ -273,6 +273,39 @@ def factor_from_linv(ctx: Context, X: torch.Tensor, scale: float, piv, Linv: np.
     return F
 
 
+def rpcholesky_batched(ctx: Context, Xs, scales, k_max, block=32, seeds=None, max_rounds=None,
+                       use_graph: bool = True) -> list:
+    """Mixed-precision block RPCholesky of many datasets at once
+    (``kevd_rpchol_batched``): with ``use_graph`` every job's round loop is a
+    branch of one captured CUDA graph launched once.  Returns one
+    Factorization per job (FP32 factor)."""
+    n = len(Xs)
+    k_max = list(k_max) if hasattr(k_max, "__len__") else [int(k_max)] * n
+    block = list(block) if hasattr(block, "__len__") else [int(block)] * n
+    seeds = list(seeds) if seeds is not None else [1234 + q for q in range(n)]
+    jobs = (_lib.RpcholJob * n)()
+    Fs, pivs, mr = [], [], []
+    for q, X in enumerate(Xs):
+        _need_cuda(X, torch.float32, "X")
+        N, d = X.shape
+        F = torch.empty((N, k_max[q]), dtype=torch.float32, device=X.device)
+        piv = np.zeros(k_max[q], dtype=np.int64)
+        rounds = max_rounds[q] if max_rounds is not None else max(1, 4 * ((k_max[q] + block[q] - 1) // block[q]) + 8)
+        Fs.append(F)
+        pivs.append(piv)
+        mr.append(rounds)
+        jobs[q] = _lib.RpcholJob(X.data_ptr(), N, d, block[q], float(scales[q]), F.data_ptr(), k_max[q], k_max[q],
+                                 rounds, 0, int(seeds[q]), piv.ctypes.data, _lib.RpcholResult())
+    ctx._check(ctx.lib.kevd_rpchol_batched(ctx.h, jobs, n, 1 if use_graph else 0, _stream()))
+    out = []
+    for q in range(n):
+        r = jobs[q].result
+        out.append(Factorization(F=Fs[q], piv=pivs[q][: r.rank].copy(), err=np.zeros(0), accepted=np.zeros(0, np.int32),
+                                 rank=int(r.rank), rounds=int(r.rounds), trace_error=float(r.trace_error),
+                                 precision=KEVD_MIXED, scale=float(scales[q])))
+    return out
+
+
 def factor_from_pivots(ctx: Context, X: torch.Tensor, scale: float, piv, precision="fp64",
                        F: torch.Tensor | None = None) -> torch.Tensor:
     """F = K(:, S) L^{-T}, L L^T = K(S, S), in FP64 arithmetic for the given pivots."""

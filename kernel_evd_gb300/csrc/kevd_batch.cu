@@ -224,8 +224,7 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     KEVD_CUDA(ctx, cudaMemcpyAsync(dc, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemsetAsync(counter, 0, sizeof(int), s));
     const size_t smem = queue_smem(dmax);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_queue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_queue_kernel), (int)smem));
     const int per_sm = smem * 2 <= (size_t)220 * 1024 ? 2 : 1;   // persistent: every CTA resident
     {
         ProfScope ps(ctx, "calibrate_queue", s);

@@ -231,8 +231,7 @@ int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const do
     if (st != KEVD_OK) return st;
     KEVD_CUDA(ctx, cudaMemcpyAsync(sc, scales, n_scales * sizeof(double), cudaMemcpyHostToDevice, s));
     const size_t smem = calib_smem_fp64(d);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_tiles_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_tiles_fp64_kernel), (int)smem));
     {
         ProfScope ps(ctx, "calibrate_tiles_fp64", s);
         calibrate_tiles_fp64_kernel<<<grid, 256, smem, s>>>(X, N, d, sc, n_scales, n_tiles, partial);
@@ -273,8 +272,7 @@ int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double*
     KEVD_CUDA(ctx, cudaMemcpyAsync(c2, hc.data(), n_scales * sizeof(float),
                                    cudaMemcpyHostToDevice, s));
     const size_t smem = calib_smem(d);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(calibrate_tiles_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_tiles_kernel), (int)smem));
     {
         ProfScope ps(ctx, "calibrate_tiles", s);
         calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, c2, n_scales, n_tiles, partial);
@@ -356,7 +354,7 @@ int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales
     const int grid = (int)std::min<int64_t>(n_tiles, kNaGrid);
     const size_t smem = calib_smem(d);
     if (cudaMemcpyAsync(sc.scales, hc, n_scales * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaFuncSetAttribute(calibrate_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        raise_smem_limit(reinterpret_cast<const void*>(&calibrate_tiles_kernel), (int)smem) !=
             cudaSuccess) {
         cudaGetLastError();
         return KEVD_ERR_CUDA;
@@ -459,8 +457,7 @@ int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64
     unsigned* hist = arena_get<unsigned>(ctx, "med.hist", kHistBins, &st);
     if (st != KEVD_OK) return st;
     const size_t smem = 2 * kCalTile * (size_t)(d + 1) * sizeof(float) + kHistBins * sizeof(unsigned);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(median_tiles_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&median_tiles_kernel), (int)smem));
     const int shifts[3] = {20, 8, 0};
     const unsigned masks[3] = {0xfffu, 0xfffu, 0xffu};
     unsigned prefix = 0;

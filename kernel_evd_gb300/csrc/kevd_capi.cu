@@ -2,6 +2,9 @@
 // workspace management, and the host orchestration that is not a kernel.
 #include "kevd_internal.cuh"
 
+#include <map>
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <iterator>
@@ -41,6 +44,20 @@ void* Arena::get(const std::string& name, size_t bytes, int* status) {
     }
     b.n = want;
     return b.p;
+}
+
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = limit[{dev, func}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
 }
 
 void Arena::release() {
@@ -240,6 +257,11 @@ int kevd_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, double scal
     KEVD_CHECK_CTX(ctx);
     return run_rpchol(ctx, X, N, d, scale, params, F, ldF, piv, err, accepted, result,
                       as_stream(stream));
+}
+
+int kevd_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int32_t n_jobs, int32_t use_graph, void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_rpchol_batched(ctx, jobs, n_jobs, use_graph, as_stream(stream));
 }
 
 int kevd_linv_from_factor(kevd_ctx* ctx, const void* F, int32_t precision, int64_t ldF,
@@ -560,8 +582,7 @@ int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y, in
         return set_error(ctx, KEVD_ERR_ARG, "nystrom_eval: unsupported size (d=%d, n=%lld)", m.d, (long long)n);
     cudaStream_t s = as_stream(stream);
     if (smem > 48 * 1024)
-        KEVD_CUDA(ctx, cudaFuncSetAttribute(nystrom_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
+        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&nystrom_eval_kernel), (int)smem));
     nystrom_eval_kernel<<<(unsigned)n_blocks, 256, smem, s>>>(Y, n, m.xs, m.zp, m.r, m.d, m.k_out,
                                                                          m.scale, Uy);
     KEVD_LAUNCH(ctx);

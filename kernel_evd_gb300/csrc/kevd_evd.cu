@@ -423,15 +423,14 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j (the FP64 weights U dinv as (hi, lo)
-// pairs, double-FP32 sums per CTA row range).  thread: columns 4 (tid >> 4)..+4,
+// CTA's rows, for a block of 64 columns j (FP32 products, round to nearest:
+// their errors are unbiased and average out in H; Kahan sums per CTA row range).  thread: columns 4 (tid >> 4)..+4,
 // U columns 2 (tid & 15)..+2.
 __global__ void __launch_bounds__(256)
 evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
               const double* __restrict__ dinv, int64_t rows_per, double* __restrict__ partial) {
     __shared__ float Fs[64][65];
     __shared__ __align__(16) float Ws[64][32];
-    __shared__ __align__(16) float Wl[64][32];
     const int tid = threadIdx.x;
     const int jr = 4 * (tid >> 4), qc = 2 * (tid & 15);
     const int64_t j0 = (int64_t)blockIdx.x * 64;
@@ -449,21 +448,17 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
         for (int e = tid; e < 64 * 32; e += 256) {
             const int ii = e >> 5, q = e & 31;
             const int64_t i = i0 + ii;
-            const double x = (i < r1 && q < m) ? (double)U[i * m + q] * dinv[i] : 0.0;
-            const float h = (float)x;
-            Ws[ii][q] = h;
-            Wl[ii][q] = (float)(x - (double)h);
+            Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
         }
         __syncthreads();
 #pragma unroll 8
         for (int ii = 0; ii < 64; ++ii) {
             const float w0 = Ws[ii][qc], w1 = Ws[ii][qc + 1];
-            const float l0 = Wl[ii][qc], l1 = Wl[ii][qc + 1];
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const float f = Fs[jr + a][ii];
-                df_fma(ks[a][0], kc[a][0], f, w0, l0);
-                df_fma(ks[a][1], kc[a][1], f, w1, l1);
+                kahan_add(ks[a][0], kc[a][0], f * w0);
+                kahan_add(ks[a][1], kc[a][1], f * w1);
             }
         }
     }
@@ -474,7 +469,7 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
             const int q = qc + b;
-            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] + (double)kc[a][b];
+            if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] - (double)kc[a][b];
         }
     }
 }
@@ -692,8 +687,7 @@ template <typename T>
 static int rowdot(kevd_ctx* ctx, const T* F, int64_t ldF, int64_t N, int64_t k, const double* v,
                   double* y, double* yinv, int* bad, cudaStream_t s) {
     const size_t smem = (size_t)k * sizeof(double);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(ev_rowdot_kernel<T>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&ev_rowdot_kernel<T>), (int)smem));
     const int grid = (int)std::min<int64_t>((N + 7) / 8, (int64_t)ctx->num_sms * 8);
     ProfScope ps(ctx, "ev_rowdot", s);
     ev_rowdot_kernel<T><<<grid, 256, smem, s>>>(F, ldF, N, k, v, y, yinv, bad);
@@ -830,8 +824,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     if (sizeof(T) == 4) {
         KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, s));
         const size_t vsm = (size_t)2 * k * sizeof(float);
-        KEVD_CUDA(ctx, cudaFuncSetAttribute(evt_rowdot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)std::max(vsm, (size_t)1024)));
+        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&evt_rowdot_kernel), (int)std::max(vsm, (size_t)1024)));
         ProfScope ps(ctx, "ev_passes", s);
         const int ny = (int)std::min<int64_t>(16, std::max<int64_t>(1, N / 8192));
         const int64_t rows_per = (N + ny - 1) / ny;

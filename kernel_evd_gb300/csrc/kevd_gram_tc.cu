@@ -400,16 +400,21 @@ int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t 
     }
     const int nt = ceil_div(k, kTT);
     const int n_tiles = nt * (nt + 1) / 2;
-    int n_split = std::max(1, ctx->num_sms / n_tiles);
-    n_split = (int)std::min<int64_t>(n_split, std::max<int64_t>(1, N / 4096));
+    // Row chunks: CTA (tile, chunk) has blockIdx = chunk * n_tiles + tile, so the
+    // hardware issues CTAs chunk by chunk and the CTAs that share a column panel
+    // stream the same rows at about the same time (the chunk's rows, about
+    // 64k x k x 4 bytes, stay in L2 while its tiles run).  At least 8 waves of
+    // CTAs keep the tail short.
+    int64_t n_split64 = std::max<int64_t>((N + 65535) / 65536, ((int64_t)ctx->num_sms * 8 + n_tiles - 1) / n_tiles);
+    n_split64 = std::min<int64_t>(n_split64, std::max<int64_t>(1, N / 1024));
+    const int n_split = (int)std::max<int64_t>(1, n_split64);
     const int64_t rows_per = ((N + n_split - 1) / n_split + kTK - 1) / kTK * kTK;
     int rc = KEVD_OK;
     double* partial = arena_get<double>(ctx, "tc.gpart", (size_t)n_split * n_tiles * kTT * kTT, &rc);
     int* err = arena_get<int>(ctx, "tc.err", 1, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
     KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)kSmemBytes));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel), (int)kSmemBytes));
     {
         ProfScope ps(ctx, "gram_tc", st);
         gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, s, N, k, n_tiles, rows_per, partial,

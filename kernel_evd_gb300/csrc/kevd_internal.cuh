@@ -164,6 +164,13 @@ int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double 
                         const int64_t* rows, int64_t row0, int64_t nrows, const int64_t* cols,
                         int64_t ncols, int precision, void* out, int64_t ld, cudaStream_t s,
                         const float* Xc = nullptr);
+// Raise (never lower) a kernel's dynamic shared-memory limit.  The attribute
+// belongs to the kernel, not to the calling thread: a call sized for a small
+// problem must not cut the limit that another thread's larger launch of the
+// same kernel relies on.
+cudaError_t raise_smem_limit(const void* func, size_t bytes);
+
+int run_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int n_jobs, int use_graph, cudaStream_t s);
 int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs, int tiles_per_item,
                           cudaStream_t s);
 int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales, int n_scales,

@@ -24,6 +24,7 @@
 #include "kevd_rng.cuh"
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace kevd {
@@ -46,6 +47,15 @@ struct RoundState {
     int32_t rounds;  // rounds executed
     int32_t pad;
     double total;    // sum of d after the last update
+};
+
+// Host side of a capture-safe factorisation: no host read inside the round
+// loop (all max_rounds rounds are enqueued; the kernels return at once after
+// the stop), results copied to these pinned buffers at the end.
+struct RpcholDeferred {
+    RoundState* state_h;
+    int* tcerr_h;
+    int64_t* piv_h;
 };
 
 __global__ void rp_init_kernel(double* __restrict__ d, double* __restrict__ dblk, int64_t N,
@@ -504,7 +514,8 @@ static size_t update_smem(int d) {
 template <typename T>
 static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
                        const kevd_rpchol_params* p, T* F, int64_t ldF, int64_t* piv_h,
-                       double* err_h, int32_t* hm_h, kevd_rpchol_result* res, cudaStream_t s) {
+                       double* err_h, int32_t* hm_h, kevd_rpchol_result* res, cudaStream_t s,
+                       RpcholDeferred* defer = nullptr) {
     const int b = p->block;
     const int64_t nblk = (N + kRowBlock - 1) / kRowBlock;
     const int n_split = (int)((p->k_max + kColChunk - 1) / kColChunk);
@@ -534,11 +545,9 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     KEVD_LAUNCH(ctx);
 
     const size_t fsm = (size_t)b * b * sizeof(double);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(rp_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)std::max(fsm, (size_t)1024)));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_factor_kernel), (int)std::max(fsm, (size_t)1024)));
     const size_t usm = update_smem<T>(d);
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(rp_update_kernel<T>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usm));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_update_kernel<T>), (int)usm));
     int* done_h = static_cast<int*>(ctx->pinned);
     // FP32 factors take the tensor-core residual update when the layout allows TMA
     const bool use_tc = sizeof(T) == 4 && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d, b);
@@ -575,7 +584,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                                                            minv_f, b, rs, dvec, dblk);
             KEVD_LAUNCH(ctx);
         }
-        if ((round & 3) == 3) {
+        if (!defer && (round & 3) == 3) {
             KEVD_CUDA(ctx, cudaMemcpyAsync(done_h, &rs->done, sizeof(int), cudaMemcpyDeviceToHost, s));
             KEVD_CUDA(ctx, cudaStreamSynchronize(s));
             if (*done_h) break;
@@ -586,6 +595,13 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                                                   0, p->seed, unif, props, rs, p->k_max,
                                                   std::min(round, p->max_rounds), p->err_target, err);
     KEVD_LAUNCH(ctx);
+    if (defer) {
+        // capture-safe: results go to pinned host memory, read after the stream completes
+        KEVD_CUDA(ctx, cudaMemcpyAsync(defer->state_h, rs, sizeof(RoundState), cudaMemcpyDeviceToHost, s));
+        KEVD_CUDA(ctx, cudaMemcpyAsync(defer->tcerr_h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        KEVD_CUDA(ctx, cudaMemcpyAsync(defer->piv_h, piv, p->k_max * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        return KEVD_OK;
+    }
     RoundState hs;
     int herr = 0;
     KEVD_CUDA(ctx, cudaMemcpyAsync(&hs, rs, sizeof(RoundState), cudaMemcpyDeviceToHost, s));
@@ -619,6 +635,140 @@ int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
     if (p->precision == KEVD_MIXED)
         return rpchol_impl<float>(ctx, X, N, d, scale, p, (float*)F, ldF, piv, err, accepted, res, s);
     return set_error(ctx, KEVD_ERR_ARG, "rpchol: unknown precision %d", p->precision);
+}
+
+// Many factorisations at once.  Each job gets its own workspace context and
+// stream; with use_graph the whole set of round loops is captured as parallel
+// branches of one CUDA graph (fork from the caller's stream, join back) and
+// launched once, so the GPU overlaps the jobs' small launches without a host
+// thread per job.  Without use_graph the same work is issued directly on the
+// per-job streams.
+int run_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int n_jobs, int use_graph, cudaStream_t s) {
+    if (!jobs || n_jobs < 1 || n_jobs > 1024) return set_error(ctx, KEVD_ERR_ARG, "rpchol_batched: 1..1024 jobs");
+    for (int q = 0; q < n_jobs; ++q) {
+        const kevd_rpchol_job& j = jobs[q];
+        if (!j.X || !j.F || !j.piv || j.N < 1 || j.d < 1 || j.d > 128 || j.block < 1 || j.block > kMaxBlock ||
+            j.k_max < 1 || j.ldF < j.k_max || j.max_rounds < 1 || !(j.scale > 0.0))
+            return set_error(ctx, KEVD_ERR_ARG, "rpchol_batched: bad job %d", q);
+    }
+    struct Slot {
+        kevd_ctx* c = nullptr;
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        RoundState* state_h = nullptr;
+        int* tcerr_h = nullptr;
+        int64_t* piv_h = nullptr;
+    };
+    std::vector<Slot> sl(n_jobs);
+    int rc = KEVD_OK;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (fork) cudaEventDestroy(fork);
+        for (auto& x : sl) {
+            if (x.ev) cudaEventDestroy(x.ev);
+            if (x.st) cudaStreamDestroy(x.st);
+            if (x.state_h) cudaFreeHost(x.state_h);
+            if (x.tcerr_h) cudaFreeHost(x.tcerr_h);
+            if (x.piv_h) cudaFreeHost(x.piv_h);
+            if (x.c) {
+                x.c->arena.release();
+                delete x.c;
+            }
+        }
+    };
+    for (int q = 0; q < n_jobs && rc == KEVD_OK; ++q) {
+        Slot& x = sl[q];
+        x.c = new kevd_ctx();
+        x.c->device = ctx->device;
+        x.c->num_sms = ctx->num_sms;
+        if (cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&x.ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaMallocHost(&x.state_h, sizeof(RoundState)) != cudaSuccess ||
+            cudaMallocHost(&x.tcerr_h, sizeof(int)) != cudaSuccess ||
+            cudaMallocHost(&x.piv_h, jobs[q].k_max * sizeof(int64_t)) != cudaSuccess)
+            rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: stream / pinned buffer setup failed");
+    }
+    if (rc == KEVD_OK && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
+        rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: event setup failed");
+    // the capture runs on a stream of its own (the caller's stream may be the
+    // legacy default stream, which cannot be captured); it is ordered after the
+    // caller's work and the graph is launched on the caller's stream
+    cudaStream_t cs = nullptr;
+    if (rc == KEVD_OK && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+        rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: capture stream setup failed");
+    auto enqueue_all = [&](int rounds_override, cudaStream_t root) -> int {
+        if (cudaEventRecord(fork, root) != cudaSuccess) return set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: fork");
+        for (int q = 0; q < n_jobs; ++q) {
+            const kevd_rpchol_job& j = jobs[q];
+            Slot& x = sl[q];
+            if (cudaStreamWaitEvent(x.st, fork, 0) != cudaSuccess)
+                return set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: fork wait");
+            kevd_rpchol_params p;
+            std::memset(&p, 0, sizeof(p));
+            p.k_max = j.k_max;
+            p.block = j.block;
+            p.max_rounds = rounds_override > 0 ? rounds_override : j.max_rounds;
+            p.tol = 1e-10;
+            p.seed = j.seed;
+            p.precision = KEVD_MIXED;
+            RpcholDeferred df{x.state_h, x.tcerr_h, x.piv_h};
+            const int r = rpchol_impl<float>(x.c, j.X, j.N, j.d, j.scale, &p, (float*)j.F, j.ldF, nullptr, nullptr,
+                                             nullptr, nullptr, x.st, &df);
+            ctx->launches += x.c->launches;
+            x.c->launches = 0;
+            if (r != KEVD_OK) return set_error(ctx, r, "rpchol_batched: job %d: %s", q, x.c->last_error.c_str());
+            if (cudaEventRecord(x.ev, x.st) != cudaSuccess || cudaStreamWaitEvent(root, x.ev, 0) != cudaSuccess)
+                return set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: join");
+        }
+        return KEVD_OK;
+    };
+    if (rc == KEVD_OK) {
+        if (use_graph) {
+            // one uncaptured round per job allocates every workspace buffer (their
+            // sizes do not depend on the round count), so nothing is allocated
+            // inside the capture; the captured run starts again from rp_init
+            rc = enqueue_all(1, s);
+            if (rc == KEVD_OK && cudaStreamSynchronize(s) != cudaSuccess)
+                rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: workspace pass failed");
+            if (rc == KEVD_OK) {
+                if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                    rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: begin capture");
+                } else {
+                    rc = enqueue_all(0, cs);
+                    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+                    if (rc == KEVD_OK && ce != cudaSuccess)
+                        rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: end capture: %s", cudaGetErrorString(ce));
+                }
+            }
+            if (rc == KEVD_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+                rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: graph instantiate");
+            if (rc == KEVD_OK && cudaGraphLaunch(exec, s) != cudaSuccess)
+                rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: graph launch");
+        } else {
+            rc = enqueue_all(0, s);
+        }
+    }
+    if (rc == KEVD_OK && cudaStreamSynchronize(s) != cudaSuccess)
+        rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc == KEVD_OK) {
+        for (int q = 0; q < n_jobs; ++q) {
+            const Slot& x = sl[q];
+            kevd_rpchol_job& j = jobs[q];
+            if (*x.tcerr_h != 0 && rc == KEVD_OK)
+                rc = set_error(ctx, KEVD_ERR_TIMEOUT, "rpchol_batched: job %d tensor-core pipeline timed out", q);
+            j.result.rank = x.state_h->rank;
+            j.result.rounds = x.state_h->rounds;
+            j.result.trace_error = x.state_h->total / (double)j.N;
+            std::memcpy(j.piv, x.piv_h, (size_t)x.state_h->rank * sizeof(int64_t));
+        }
+    }
+    cleanup();
+    if (cs) cudaStreamDestroy(cs);
+    return rc;
 }
 
 // Gather rows idx of F (first ncols columns) into a column-major FP64 n x ncols

@@ -44,11 +44,23 @@ namespace {
 constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
-constexpr int kStages = 4;
+// Pipeline shape (tuning parameters; Tensor Memory holds kBufs partial buffers
+// and kStages a-slots of 64 columns each, 512 columns in all)
+#ifndef KEVD_UPD_STAGES
+#define KEVD_UPD_STAGES 4
+#endif
+#ifndef KEVD_UPD_BUFS
+#define KEVD_UPD_BUFS 4
+#endif
+#ifndef KEVD_UPD_PER_PARTIAL
+#define KEVD_UPD_PER_PARTIAL 2
+#endif
+constexpr int kStages = KEVD_UPD_STAGES;
 constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
-constexpr int kBufs = 4;            // TMEM partial buffers, columns [0, 256)
-constexpr int kPerPartial = 2;      // 32-column stages accumulated per TMEM partial
-constexpr uint32_t kTmemA = kBufs * 64;   // a-slots: columns [256, 512), 64 per stage (hi 32, lo 32)
+constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of 64 columns
+constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulated per TMEM partial
+constexpr uint32_t kTmemA = kBufs * 64;   // a-slots after the partials, 64 per stage (hi 32, lo 32)
+static_assert(kBufs * 64 + kStages * 64 <= 512, "Tensor Memory holds 512 columns");
 constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
@@ -56,6 +68,7 @@ constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
 constexpr int kThreads = 320;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = 128;
+constexpr int kMaxDF = 64;          // K(R, S_i) is formed in the update kernel for d <= kMaxDF
 
 struct Bars {
     uint64_t tma_full[kStages];
@@ -85,7 +98,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmk,
                  float* __restrict__ F, int64_t ldF, int64_t N, const float* __restrict__ minv_f, int b,
                  const uint8_t* __restrict__ bprep, const RoundView* st, double* __restrict__ dvec,
-                 double* __restrict__ dblk, int* __restrict__ err) {
+                 double* __restrict__ dblk, int* __restrict__ err, const float* __restrict__ X, int d, float scale,
+                 const int64_t* __restrict__ sacc, int fuse_k) {
     if (st->done) return;
     const int nacc = st->nacc;
     if (nacc == 0) return;
@@ -98,7 +112,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
     // K(R, S_i) tile: two 128 x 32 SWIZZLE_128B halves (TMA), then G in place
     uint8_t* ktile = base + (size_t)kStages * kStageBytes;
     float* mv = reinterpret_cast<float*>(ktile + 2 * kAOp);                      // kCols x kCols
-    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
+    float* xs = mv + kCols * kCols;                                              // S_i rows, kCols x kMaxDF
+    Bars* bar = reinterpret_cast<Bars*>(xs + kCols * kMaxDF);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // L_i^{-1} (FP32) for the epilogue
@@ -106,6 +121,12 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         const int a = e / kCols, q = e - a * kCols;
         mv[e] = (a < nacc && q < nacc) ? minv_f[a * b + q] : 0.f;
     }
+    // the accepted points, for K(R, S_i) in the epilogue
+    if (fuse_k)
+        for (int e = threadIdx.x; e < kCols * kMaxDF; e += kThreads) {
+            const int q = e / kMaxDF, kk = e - q * kMaxDF;
+            xs[e] = (q < nacc && kk < d) ? X[sacc[q] * d + kk] : 0.f;
+        }
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             tc::mbar_init(&bar->tma_full[s], 1);
@@ -155,7 +176,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
             }
             if (!ok) atomicExch(err, 11);
-        } else if (lane == 1) {
+        } else if (lane == 1 && !fuse_k) {
             // K(R, S_i) tiles, one per row block, single-buffered
             int64_t it = 0;
             for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x, ++it) {
@@ -269,6 +290,29 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             const int64_t row0 = rb * kRows;
             const int64_t i = row0 + rloc;
             const double d_old = (i < N) ? dvec[i] : 0.0;
+            if (fuse_k) {
+                // K(i, S_i) from FP32 direct distances (the order and exp of
+                // update_kcols_kernel) into this thread's row of the K tile,
+                // while the MMAs of this row block run
+                float x[kMaxDF];
+#pragma unroll
+                for (int kk = 0; kk < kMaxDF; ++kk) x[kk] = (i < N && kk < d) ? __ldg(X + i * d + kk) : 0.f;
+#pragma unroll 1
+                for (int qq = 0; qq < kCols; ++qq) {
+                    const float* sq = xs + qq * kMaxDF;
+                    float dd = 0.f;
+#pragma unroll
+                    for (int kk = 0; kk < kMaxDF; ++kk) {
+                        if (kk < d) {
+                            const float t = x[kk] - sq[kk];
+                            dd = fmaf(t, t, dd);
+                        }
+                    }
+                    *reinterpret_cast<float*>(ktile + (qq >> 5) * kAOp +
+                                              tc::sw128_off((uint32_t)rloc, (uint32_t)(qq & 31))) =
+                        (qq < nacc) ? expf(-scale * dd) : 0.f;
+                }
+            }
             float acc[kCols];
 #pragma unroll
             for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
@@ -295,7 +339,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
             }
-            if (ok && !tc::mbar_wait(&bar->kfull, (uint32_t)(kit & 1), kTimeoutNs)) {
+            if (ok && !fuse_k && !tc::mbar_wait(&bar->kfull, (uint32_t)(kit & 1), kTimeoutNs)) {
                 atomicExch(err, 17);
                 ok = false;
             }
@@ -340,7 +384,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
             }
             asm volatile("bar.sync 1, 128;" ::: "memory");   // tile consumed
-            tc::mbar_arrive(&bar->kempty);
+            if (!fuse_k) tc::mbar_arrive(&bar->kempty);
             ++kit;
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
@@ -455,7 +499,9 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem =
+    (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + kCols * kMaxDF * 4 + sizeof(Bars) + 1024;
+static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 
 // Whether the tensor-core update can run for this factor layout.
 bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
@@ -491,29 +537,34 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
     const RoundView* rv = static_cast<const RoundView*>(round_state);
-    float* Kc = arena_get<float>(ctx, "utc.kc", (size_t)N * kCols, &rc);
-    if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
+    // K(R, S_i): formed in the update kernel's epilogue for d <= kMaxDF, else by
+    // update_kcols_kernel into an N x 64 buffer that the update kernel loads by TMA
+    const int fuse_k = d <= kMaxDF ? 1 : 0;
+    float* Kc = nullptr;
     static thread_local const void* last_K = nullptr;
     static thread_local int64_t last_KN = -1;
     static thread_local CUtensorMap tmk;
-    if (Kc != last_K || N != last_KN) {
-        const cuuint64_t gdim[2] = {(cuuint64_t)kCols, (cuuint64_t)N};
-        const cuuint64_t gstride[1] = {(cuuint64_t)kCols * 4};
-        const cuuint32_t box[2] = {32, (cuuint32_t)kRows};
-        const cuuint32_t estr[2] = {1, 1};
-        CUresult cr = get_encode()(&tmk, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)Kc, gdim, gstride, box, estr,
-                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (cr != CUDA_SUCCESS)
-            return set_error(ctx, KEVD_ERR_CUDA, "update_tc: tensor map (K) encode failed (%d)", (int)cr);
-        last_K = Kc;
-        last_KN = N;
+    if (!fuse_k) {
+        Kc = arena_get<float>(ctx, "utc.kc", (size_t)N * kCols, &rc);
+        if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
+        if (Kc != last_K || N != last_KN) {
+            const cuuint64_t gdim[2] = {(cuuint64_t)kCols, (cuuint64_t)N};
+            const cuuint64_t gstride[1] = {(cuuint64_t)kCols * 4};
+            const cuuint32_t box[2] = {32, (cuuint32_t)kRows};
+            const cuuint32_t estr[2] = {1, 1};
+            CUresult cr = get_encode()(&tmk, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)Kc, gdim, gstride, box, estr,
+                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (cr != CUDA_SUCCESS)
+                return set_error(ctx, KEVD_ERR_CUDA, "update_tc: tensor map (K) encode failed (%d)", (int)cr);
+            last_K = Kc;
+            last_KN = N;
+        }
     }
-    {
+    if (!fuse_k) {
         ProfScope ps(ctx, "rp_update_kcols", s);
         const size_t ksm = (size_t)(kRows + kCols) * (d + 1) * sizeof(float);
-        KEVD_CUDA(ctx, cudaFuncSetAttribute(update_kcols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)ksm));
+        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
         update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
         KEVD_LAUNCH(ctx);
     }
@@ -523,14 +574,13 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
             F, ldF, sacc, rv, n_stages_max, bprep);
         KEVD_LAUNCH(ctx);
     }
-    KEVD_CUDA(ctx, cudaFuncSetAttribute(update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)kUpdSmem));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_tc_kernel), (int)kUpdSmem));
     const int64_t nblk = (N + kRows - 1) / kRows;
     const int grid = (int)std::min<int64_t>(nblk, ctx->num_sms);
     {
         ProfScope ps(ctx, "rp_update", s);
         update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, tmk, F, ldF, N, minv_f, b, bprep, rv, dvec, dblk,
-                                                          err);
+                                                          err, X, d, (float)scale, sacc, fuse_k);
         KEVD_LAUNCH(ctx);
     }
     return KEVD_OK;

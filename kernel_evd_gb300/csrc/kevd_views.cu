@@ -99,16 +99,12 @@ int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double 
     size_t smem = 2 * 32 * (size_t)(d + 1) * sizeof(float);
     if (precision == KEVD_FP64) {
         if (smem > 48 * 1024)
-            KEVD_CUDA(ctx, cudaFuncSetAttribute(kernel_block_kernel<double>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem));
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&kernel_block_kernel<double>), (int)smem));
         kernel_block_kernel<double><<<grid, dim3(32, 8), smem, s>>>(
             X, Xc, d, scale, rows, row0, nrows, cols, ncols, (double*)out, ld);
     } else {
         if (smem > 48 * 1024)
-            KEVD_CUDA(ctx, cudaFuncSetAttribute(kernel_block_kernel<float>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem));
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&kernel_block_kernel<float>), (int)smem));
         kernel_block_kernel<float><<<grid, dim3(32, 8), smem, s>>>(
             X, Xc, d, scale, rows, row0, nrows, cols, ncols, (float*)out, ld);
     }

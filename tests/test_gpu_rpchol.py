@@ -114,3 +114,42 @@ def test_bad_arguments(ctx, states):
     with pytest.raises(KevdError):
         api.rpcholesky(ctx, X, SCALE, k_max=10, block=4, precision="fp64",
                        F=torch.empty((100, 5), dtype=torch.float64, device="cuda"))
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batched_factorisations_match_single(ctx, use_graph):
+    """Uneven jobs (N, d, k, b) in one call, with and without the captured
+    graph: each job equals the single-job factorisation (same pivots, same
+    trace error, same factor columns)."""
+    from kernel_evd_gb300 import api
+    shapes = [(3000, 64, 256, 32), (1200, 32, 100, 16), (5000, 128, 320, 64), (800, 64, 64, 32)]
+    Xs, scales = [], []
+    for q, (n, m, k, b) in enumerate(shapes):
+        Xn = ks.seeded_mode(n, M=m, seed=10 + q, warm_time=60.0).astype(np.float32)
+        Xs.append(torch.from_numpy(Xn).cuda())
+        scales.append(1.0 / (0.5 * m))
+    ks_ = [s[2] for s in shapes]
+    bs = [s[3] for s in shapes]
+    got = api.rpcholesky_batched(ctx, Xs, scales, ks_, bs, seeds=[7, 8, 9, 10], use_graph=use_graph)
+    for q in range(len(shapes)):
+        ref = api.rpcholesky(ctx, Xs[q], scales[q], k_max=ks_[q], block=bs[q], seed=7 + q, precision="mixed")
+        assert got[q].rank == ref.rank
+        np.testing.assert_array_equal(got[q].piv, ref.piv)
+        assert got[q].trace_error == ref.trace_error
+        np.testing.assert_array_equal(got[q].factor.cpu().numpy(), ref.factor.cpu().numpy())
+
+
+def test_autotuner_picks_a_candidate_and_caches(ctx, tmp_path, monkeypatch):
+    from kernel_evd_gb300 import autotune
+    monkeypatch.setenv("KEVD_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_loaded", False)
+    monkeypatch.setattr(autotune, "_cache", {})
+    X = torch.from_numpy(ks.seeded_mode(6000, warm_time=60.0).astype(np.float32)).cuda()
+    r1 = autotune.tune_block(ctx, X, 1.0 / 30.0, 300, candidates=(16, 32, 64), probe_rows=6000, probe_k=192)
+    assert r1["block"] in (16, 32, 64) and not r1["cached"] and len(r1["ms_per_column"]) == 3
+    r2 = autotune.tune_block(ctx, X, 1.0 / 30.0, 300, candidates=(16, 32, 64))
+    assert r2["cached"] and r2["block"] == r1["block"]
+    assert (tmp_path / "tune.json").exists()
+    c = autotune.tune_calibration_items(ctx, [X[:3000], X[3000:4500]], [1.0 / np.geomspace(1, 300, 41)] * 2,
+                                        candidates=(0, 4, 64))
+    assert c["tiles_per_item"] in (0, 4, 64)
