@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--k", type=int, default=2000)
-    ap.add_argument("--b", type=int, default=64)
+    ap.add_argument("--b", type=int, default=64, help="RPCholesky block size (0: the autotuner's choice)")
     ap.add_argument("--kout", type=int, default=32)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--cpu-rows", type=int, default=40000, help="row sample of the CPU baseline")
@@ -196,7 +196,7 @@ def batched_phase(ctx, args):
     """48 uneven datasets through one batched pipeline: KS with L in {16, 22, 36},
     d in {32, 64, 128} gridpoints, N log-uniform in [1e4, 4e5], rank k uniform in
     [100, 1000] (dataset i draws from default_rng(1000 + i), seed i), b = 32.
-    Per dataset: median squared distance of a seeded 1e7-pair sample, 41
+    Per dataset: median squared distance of a seeded 1e6-pair sample, 41
     log-spaced eps in 2^-10..2^10 x median, max-slope eps; then block RPCholesky
     (mixed) and the bistochastic EVD, top 16.  The 48 calibrations are one
     persistent launch over a device work queue (item size autotuned); the 48
@@ -225,7 +225,7 @@ def batched_phase(ctx, args):
     t0 = time.time()
     meds = []
     for X in Xs:
-        pi, pl = sample_pairs(X.shape[0], 10_000_000, seed=0)
+        pi, pl = sample_pairs(X.shape[0], 1_000_000, seed=0)
         meds.append(api.pair_median(ctx, X, pairs=(torch.from_numpy(pi).cuda(), torch.from_numpy(pl).cuda())))
     timings["median_s"] = time.time() - t0
     eps_list = [api.log_sweep(md, 41) for md in meds]
@@ -245,11 +245,14 @@ def batched_phase(ctx, args):
     t0 = time.time()
     evs = []
     failed = 0
+    status = []
     for f in facs:
         try:
             evs.append(api.bistochastic_evd(ctx, f.factor, k_out=16))
-        except api.KevdError:
+            status.append("ok")
+        except api.KevdError as e:
             evs.append(None)
+            status.append(e.name)
             failed += 1
     torch.cuda.synchronize()
     timings["evd_s"] = time.time() - t0
@@ -274,7 +277,10 @@ def batched_phase(ctx, args):
     return {"datasets": n_sets, "seconds": total, "stages": timings, "datagen_s": gen_s,
             "calibration_pair_eps_per_s": pairs_eps / timings["calibration_s"],
             "autotune": {"calibration_tiles_per_item": tune_c["tiles_per_item"], "calibration_ms": tune_c["ms"]},
-            "ranks": [int(f.rank) for f in facs], "trace_error_max": float(max(f.trace_error for f in facs)),
+            "per_dataset": [{"L": sp[0], "d": sp[1], "N": sp[2], "k": ks_[q], "eps": float(eopt[q]),
+                             "rank": int(facs[q].rank), "trace_error": float(facs[q].trace_error),
+                             "evd": status[q]} for q, sp in enumerate(specs)],
+            "trace_error_max": float(max(f.trace_error for f in facs)),
             "evd_failed": failed, "top16_eig_err_vs_fp64_same_pivots_max": float(max(errs)) if errs else None,
             "top16_eig_err_median": float(np.median(errs)) if errs else None, "fp64_check_s": check_s,
             "fp64_checked": len(errs),
@@ -469,6 +475,12 @@ def main():
     Xd = Xh.cuda()
     eps, med, n_cal = calibrate_eps(ctx, Xd, N)
     scale = 1.0 / eps
+    # block size: the autotuner times b in {16, 32, 64} on this data (a 131,072-row
+    # prefix to rank 512); --b 0 runs the step with its choice
+    from kernel_evd_gb300 import autotune
+    tuned = autotune.tune_block(ctx, Xd, scale, args.k, candidates=(16, 32, 64))
+    if args.b == 0:
+        args.b = int(tuned["block"])
     F = torch.empty((N, args.k), dtype=torch.float32, device="cuda")
     U = torch.empty((N, args.kout), dtype=torch.float32, device="cuda")
 
@@ -638,6 +650,8 @@ def main():
                 "config": {"workload": f"block RPCholesky + bistochastic EVD, N={N}, d={d}, k={args.k}, "
                                        f"b={args.b}, top {args.kout}, mixed precision",
                            "eps": eps, "median_sqdist": med, "calibration_rows": n_cal,
+                           "block_autotune": {"chosen": int(tuned["block"]),
+                                              "ms_per_column": tuned["ms_per_column"]},
                            "l2": "inputs larger than L2 (X 512 MB, F 16 GB)",
                            "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"},
                 "rank": int(fac.rank), "rounds": int(fac.rounds), "trace_error": fac.trace_error,

@@ -70,8 +70,8 @@ __device__ __forceinline__ void stage_rows(const float* __restrict__ X, int64_t 
 }
 
 __global__ void __launch_bounds__(256, 2)
-calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict__ items, int n_items,
-                       const float* __restrict__ c2all, int dmax, int* __restrict__ counter,
+calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict__ items, int item_base,
+                       int n_items, const float* __restrict__ c2all, int dmax, int* __restrict__ counter,
                        double* __restrict__ partial) {
     extern __shared__ float sm[];
     float* xi = sm;
@@ -85,8 +85,8 @@ calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict_
         __syncthreads();
         if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
         __syncthreads();
-        const int it = cur;
-        if (it >= n_items) break;
+        if (cur >= n_items) break;
+        const int it = item_base + cur;
         const Item item = items[it];
         const JobDesc jb = jobs[item.job];
         const int d = jb.d, dp = d + 1, ns = jb.n_scales;
@@ -189,7 +189,17 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     // item size: about 16 items per SM over the whole batch unless given
     int64_t per = tiles_per_item > 0 ? tiles_per_item
                                      : std::max<int64_t>(1, total_tiles / ((int64_t)ctx->num_sms * 16));
-    for (int q = 0; q < n_jobs; ++q) {
+    // jobs grouped by feature-dimension class (d <= 32, <= 64, <= 128): one
+    // persistent launch per class, shared memory sized for that class, so small-d
+    // datasets keep two CTAs per SM
+    const int cls_d[3] = {32, 64, 128};
+    std::vector<int> order;
+    for (int c = 0; c < 3; ++c)
+        for (int q = 0; q < n_jobs; ++q)
+            if ((c == 0 ? 0 : cls_d[c - 1]) < jobs[q].d && jobs[q].d <= cls_d[c]) order.push_back(q);
+    int cls_begin[4] = {0, 0, 0, 0};
+    for (int oi = 0; oi < n_jobs; ++oi) {
+        const int q = order[oi];
         const kevd_calib_job& j = jobs[q];
         const int64_t nt = (j.N + kTile - 1) / kTile;
         const int64_t tiles = nt * (nt + 1) / 2;
@@ -208,6 +218,8 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
         for (int64_t t0 = 0; t0 < tiles; t0 += per) hi.push_back(Item{q, 0, t0, std::min(tiles, t0 + per)});
         d.n_items = (int32_t)hi.size() - d.item0;
         d.pad = 0;
+        const int c = j.d <= 32 ? 0 : (j.d <= 64 ? 1 : 2);
+        for (int cc = c + 1; cc < 4; ++cc) cls_begin[cc] = (int)hi.size();
     }
     if (hi.size() > (size_t)INT32_MAX / 2) return set_error(ctx, KEVD_ERR_ARG, "calibrate_batched: too many items");
     const int n_items = (int)hi.size();
@@ -215,20 +227,23 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     JobDesc* dj = arena_get<JobDesc>(ctx, "cb.jobs", n_jobs, &st);
     Item* di = arena_get<Item>(ctx, "cb.items", n_items, &st);
     float* dc = arena_get<float>(ctx, "cb.c2", hc.size(), &st);
-    int* counter = arena_get<int>(ctx, "cb.counter", 1, &st);
+    int* counter = arena_get<int>(ctx, "cb.counter", 3, &st);
     double* partial = arena_get<double>(ctx, "cb.partial", (size_t)n_items * kMaxScalesB, &st);
     double* out = arena_get<double>(ctx, "cb.out", (size_t)n_jobs * kMaxScalesB, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "calibrate_batched: out of device memory");
     KEVD_CUDA(ctx, cudaMemcpyAsync(dj, hj.data(), hj.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemcpyAsync(di, hi.data(), hi.size() * sizeof(Item), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemcpyAsync(dc, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    KEVD_CUDA(ctx, cudaMemsetAsync(counter, 0, sizeof(int), s));
-    const size_t smem = queue_smem(dmax);
-    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_queue_kernel), (int)smem));
-    const int per_sm = smem * 2 <= (size_t)220 * 1024 ? 2 : 1;   // persistent: every CTA resident
-    {
+    KEVD_CUDA(ctx, cudaMemsetAsync(counter, 0, 3 * sizeof(int), s));
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_queue_kernel), (int)queue_smem(dmax)));
+    for (int c = 0; c < 3; ++c) {
+        const int b0 = cls_begin[c], b1 = c < 2 ? cls_begin[c + 1] : n_items;
+        if (b1 <= b0) continue;
+        const int dcls = std::min(dmax, cls_d[c]);
+        const size_t smem = queue_smem(dcls);
+        const int per_sm = smem * 2 <= (size_t)220 * 1024 ? 2 : 1;   // persistent: every CTA resident
         ProfScope ps(ctx, "calibrate_queue", s);
-        calibrate_queue_kernel<<<ctx->num_sms * per_sm, 256, smem, s>>>(dj, di, n_items, dc, dmax, counter,
+        calibrate_queue_kernel<<<ctx->num_sms * per_sm, 256, smem, s>>>(dj, di, b0, b1 - b0, dc, dcls, counter + c,
                                                                          partial);
         KEVD_LAUNCH(ctx);
     }

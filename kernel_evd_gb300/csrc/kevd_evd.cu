@@ -369,7 +369,15 @@ evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     for (int64_t j0 = 0; j0 < k; j0 += 32) {
         float ps = 0.f, pc = 0.f;
         const int64_t j1 = min(k, j0 + 32);
-        for (int64_t j = j0; j < j1; ++j) df_fma(ps, pc, FT[j * ldT + i], vhl[2 * j], vhl[2 * j + 1]);
+        int64_t j = j0;
+        for (; j + 8 <= j1; j += 8) {   // eight loads in flight, then the compensated sums in order
+            float f[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) f[u] = FT[(j + u) * ldT + i];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) df_fma(ps, pc, f[u], vhl[2 * (j + u)], vhl[2 * (j + u) + 1]);
+        }
+        for (; j < j1; ++j) df_fma(ps, pc, FT[j * ldT + i], vhl[2 * j], vhl[2 * j + 1]);
         acc += (double)ps + (double)pc;
     }
     y[i] = acc;
@@ -423,8 +431,9 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j (FP32 products, round to nearest:
-// their errors are unbiased and average out in H; Kahan sums per CTA row range).  thread: columns 4 (tid >> 4)..+4,
+// CTA's rows, for a block of 64 columns j (FP32 products and 8-row FP32
+// partials, round to nearest: their errors are unbiased and average out in H;
+// the partials are added with compensation over the CTA's row range).  thread: columns 4 (tid >> 4)..+4,
 // U columns 2 (tid & 15)..+2.
 __global__ void __launch_bounds__(256)
 evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
@@ -451,14 +460,24 @@ evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
             Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
         }
         __syncthreads();
-#pragma unroll 8
-        for (int ii = 0; ii < 64; ++ii) {
-            const float w0 = Ws[ii][qc], w1 = Ws[ii][qc + 1];
+        // 8-row FP32 partials (fma chains), each added with compensation
+#pragma unroll 1
+        for (int i8 = 0; i8 < 64; i8 += 8) {
+            float p[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float w0 = Ws[i8 + u][qc], w1 = Ws[i8 + u][qc + 1];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const float f = Fs[jr + a][i8 + u];
+                    p[a][0] = fmaf(f, w0, p[a][0]);
+                    p[a][1] = fmaf(f, w1, p[a][1]);
+                }
+            }
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-                const float f = Fs[jr + a][ii];
-                kahan_add(ks[a][0], kc[a][0], f * w0);
-                kahan_add(ks[a][1], kc[a][1], f * w1);
+                kahan_add(ks[a][0], kc[a][0], p[a][0]);
+                kahan_add(ks[a][1], kc[a][1], p[a][1]);
             }
         }
     }
@@ -502,13 +521,19 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
                 // 4 rows x (hi, lo) products per column in FP32, then one compensated
                 // add of that 8-term sum
                 const int jn = (int)min((int64_t)32, k - j0);
+                float fn[4];   // the next 4-row group, loaded one step ahead
+#pragma unroll
+                for (int u = 0; u < 4; ++u) fn[u] = (u < jn) ? FT[(j0 + u) * ldT + i] : 0.f;
                 for (int jj = 0; jj < jn; jj += 4) {
                     float part[32];
 #pragma unroll
                     for (int q = 0; q < 32; ++q) part[q] = 0.f;
                     float f[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
+                    for (int u = 0; u < 4; ++u) {
+                        f[u] = fn[u];
+                        fn[u] = (jj + 4 + u < jn) ? FT[(j0 + jj + 4 + u) * ldT + i] : 0.f;
+                    }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const float4* th = reinterpret_cast<const float4*>(Ts[0][jj + u]);

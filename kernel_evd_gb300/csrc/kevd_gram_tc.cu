@@ -23,7 +23,7 @@
 //   warp 8      TMA producer
 //   warp 9      TMEM allocation and the single MMA-issuing thread (A from
 //               Tensor Memory, B from shared memory)
-// A 3-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
+// A 4-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
 // double-buffered TMEM accumulator (2 x 128 columns) are handed over with
 // mbarriers; every wait is bounded and sets an error flag on timeout.
 // Keeping the a operand out of shared memory removes its split stores and the
@@ -42,22 +42,23 @@ namespace {
 
 constexpr int kTT = 128;               // output tile edge
 constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
-constexpr int kStages = 3;
+constexpr int kStages = 4;
 constexpr int kPrefetch = 0;          // stages of F prefetched into L2 ahead of the ring (0: off;
                                       // at N = 2M, k = 2000 a 6-stage prefetch cost 1.8x: it
                                       // broke the L2 sharing of panels between CTAs)
 constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
-constexpr int kStageBytes = 4 * kOpBytes;   // a_hi, a_lo, b_hi, b_lo
+constexpr int kStageBytes = 3 * kOpBytes;   // a (raw), b hi, b lo
 constexpr int kEpiWarps = 4;        // warps 0-3
 constexpr int kCvtWarp0 = 4;        // warps 4-7
 constexpr int kCvtWarps = 4;
 constexpr int kProdWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kThreads = 10 * 32;
-constexpr uint32_t kTmemCols = 512;       // accumulators [0,256), a-operand slots [256,448)
+constexpr uint32_t kTmemCols = 512;       // accumulators [0,256), a-operand slots [256,512)
 constexpr uint32_t kTmemA = 256;
 constexpr uint32_t kTmemASlot = 64;       // hi columns [0,32), lo [32,64)
+static_assert(kTmemA + kStages * kTmemASlot <= kTmemCols, "Tensor Memory holds 512 columns");
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
@@ -70,7 +71,8 @@ struct Barriers {
     uint32_t tmem_base;
 };
 
-constexpr size_t kSmemBytes = (size_t)kStages * (4 * kOpBytes + 1024) + sizeof(Barriers) + 1024;
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
+static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 
 __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
     int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -81,13 +83,15 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
 }
 
 // Per stage (32 rows of F = 32 columns of FT):
-//   [a_hi 16 KB][a_lo 16 KB][b_hi 16 KB][b_lo 16 KB]
+//   [a 16 KB][b hi 16 KB][b lo 16 KB]
 // The TMA writes the raw FT boxes (128 factor columns x 32 rows, K-major,
-// SWIZZLE_128B) into the hi slots; the
-// converters overwrite hi in place with rn_tf32(y) and write lo = rn_tf32(y - hi),
-// y = s_i * F[i][c].  Element (m, k) of a slot sits at sw128_off(m, k), so a
-// 16-byte chunk holds 4 consecutive rows k of one column m.
-constexpr int kStageAlloc = 4 * kOpBytes + 1024;   // keeps every stage 1024-aligned
+// SWIZZLE_128B) into the a and b tiles.  With y = s_i * F[i][c], the converters
+// write rn_tf32(y) and rn_tf32(y - hi) of the a tile into the stage's Tensor
+// Memory a-slot, and overwrite the b tile in place with its hi part, its lo part
+// going to the b-lo tile (on a diagonal tile b = a: the a tile itself becomes b
+// hi).  Element (m, k) of a tile sits at sw128_off(m, k), so a 16-byte chunk
+// holds 4 consecutive rows k of one column m.
+constexpr int kStageAlloc = kStageBytes;   // a multiple of 1024: every stage stays 1024-aligned
 
 // Row m of a K-major SW128 tile: its 8 16-byte chunks (K = 4c .. 4c+3).
 __device__ __forceinline__ void load_row(const uint8_t* tile, int m, float (&x)[32]) {
@@ -184,7 +188,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                 }
                 tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
                 tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
-                if (!diag) tc::tma_load_2d(st + 2 * kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
+                if (!diag) tc::tma_load_2d(st + kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
             }
         }
         __syncwarp();
@@ -219,14 +223,14 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
             lo_part(y, h);
             tc::tmem_st32(ta + 32, h);
             if (diag) {
-                store_row(st + kOpBytes, m, h);   // b = a: hi in place, lo beside it
+                store_row(st + 2 * kOpBytes, m, h);   // b = a: hi in place in the a tile, lo in the b-lo tile
             } else {
-                uint8_t* bt = st + 2 * kOpBytes;
+                uint8_t* bt = st + kOpBytes;
                 load_row(bt, m, y);
                 scale_split(y, h, w, bok);
                 store_row(bt, m, h);
                 lo_part(y, h);
-                store_row(st + 3 * kOpBytes, m, h);
+                store_row(st + 2 * kOpBytes, m, h);
             }
             tc::tmem_wait_st();
             tc::fence_async_smem();
@@ -260,8 +264,8 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                     tc::tc_fence_after();
                     uint8_t* st = base + (size_t)slot * kStageAlloc;
                     const uint32_t ahi = tbase + kTmemA + (uint32_t)slot * kTmemASlot, alo = ahi + 32;
-                    const uint32_t bhi = diag ? tc::smem_u32(st) : tc::smem_u32(st + 2 * kOpBytes);
-                    const uint32_t blo = diag ? tc::smem_u32(st + kOpBytes) : tc::smem_u32(st + 3 * kOpBytes);
+                    const uint32_t bhi = diag ? tc::smem_u32(st) : tc::smem_u32(st + kOpBytes);
+                    const uint32_t blo = tc::smem_u32(st + 2 * kOpBytes);
 #pragma unroll
                     for (int j = 0; j < kTK / 8; ++j) {
                         const uint32_t koff = (uint32_t)(j * 32);   // 8 tf32 = 32 bytes = 8 TMEM columns

@@ -68,7 +68,6 @@ constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
 constexpr int kThreads = 320;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = 128;
-constexpr int kMaxDF = 64;          // K(R, S_i) is formed in the update kernel for d <= kMaxDF
 
 struct Bars {
     uint64_t tma_full[kStages];
@@ -98,8 +97,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmk,
                  float* __restrict__ F, int64_t ldF, int64_t N, const float* __restrict__ minv_f, int b,
                  const uint8_t* __restrict__ bprep, const RoundView* st, double* __restrict__ dvec,
-                 double* __restrict__ dblk, int* __restrict__ err, const float* __restrict__ X, int d, float scale,
-                 const int64_t* __restrict__ sacc, int fuse_k) {
+                 double* __restrict__ dblk, int* __restrict__ err) {
     if (st->done) return;
     const int nacc = st->nacc;
     if (nacc == 0) return;
@@ -112,8 +110,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
     // K(R, S_i) tile: two 128 x 32 SWIZZLE_128B halves (TMA), then G in place
     uint8_t* ktile = base + (size_t)kStages * kStageBytes;
     float* mv = reinterpret_cast<float*>(ktile + 2 * kAOp);                      // kCols x kCols
-    float* xs = mv + kCols * kCols;                                              // S_i rows, kCols x kMaxDF
-    Bars* bar = reinterpret_cast<Bars*>(xs + kCols * kMaxDF);
+    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // L_i^{-1} (FP32) for the epilogue
@@ -121,12 +118,6 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         const int a = e / kCols, q = e - a * kCols;
         mv[e] = (a < nacc && q < nacc) ? minv_f[a * b + q] : 0.f;
     }
-    // the accepted points, for K(R, S_i) in the epilogue
-    if (fuse_k)
-        for (int e = threadIdx.x; e < kCols * kMaxDF; e += kThreads) {
-            const int q = e / kMaxDF, kk = e - q * kMaxDF;
-            xs[e] = (q < nacc && kk < d) ? X[sacc[q] * d + kk] : 0.f;
-        }
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             tc::mbar_init(&bar->tma_full[s], 1);
@@ -176,7 +167,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
             }
             if (!ok) atomicExch(err, 11);
-        } else if (lane == 1 && !fuse_k) {
+        } else if (lane == 1) {
             // K(R, S_i) tiles, one per row block, single-buffered
             int64_t it = 0;
             for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x, ++it) {
@@ -290,29 +281,6 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             const int64_t row0 = rb * kRows;
             const int64_t i = row0 + rloc;
             const double d_old = (i < N) ? dvec[i] : 0.0;
-            if (fuse_k) {
-                // K(i, S_i) from FP32 direct distances (the order and exp of
-                // update_kcols_kernel) into this thread's row of the K tile,
-                // while the MMAs of this row block run
-                float x[kMaxDF];
-#pragma unroll
-                for (int kk = 0; kk < kMaxDF; ++kk) x[kk] = (i < N && kk < d) ? __ldg(X + i * d + kk) : 0.f;
-#pragma unroll 1
-                for (int qq = 0; qq < kCols; ++qq) {
-                    const float* sq = xs + qq * kMaxDF;
-                    float dd = 0.f;
-#pragma unroll
-                    for (int kk = 0; kk < kMaxDF; ++kk) {
-                        if (kk < d) {
-                            const float t = x[kk] - sq[kk];
-                            dd = fmaf(t, t, dd);
-                        }
-                    }
-                    *reinterpret_cast<float*>(ktile + (qq >> 5) * kAOp +
-                                              tc::sw128_off((uint32_t)rloc, (uint32_t)(qq & 31))) =
-                        (qq < nacc) ? expf(-scale * dd) : 0.f;
-                }
-            }
             float acc[kCols];
 #pragma unroll
             for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
@@ -339,7 +307,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
             }
-            if (ok && !fuse_k && !tc::mbar_wait(&bar->kfull, (uint32_t)(kit & 1), kTimeoutNs)) {
+            if (ok && !tc::mbar_wait(&bar->kfull, (uint32_t)(kit & 1), kTimeoutNs)) {
                 atomicExch(err, 17);
                 ok = false;
             }
@@ -384,7 +352,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
             }
             asm volatile("bar.sync 1, 128;" ::: "memory");   // tile consumed
-            if (!fuse_k) tc::mbar_arrive(&bar->kempty);
+            tc::mbar_arrive(&bar->kempty);
             ++kit;
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
@@ -499,8 +467,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem =
-    (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + kCols * kMaxDF * 4 + sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + sizeof(Bars) + 1024;
 static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 
 // Whether the tensor-core update can run for this factor layout.
@@ -537,14 +504,13 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
     const RoundView* rv = static_cast<const RoundView*>(round_state);
-    // K(R, S_i): formed in the update kernel's epilogue for d <= kMaxDF, else by
-    // update_kcols_kernel into an N x 64 buffer that the update kernel loads by TMA
-    const int fuse_k = d <= kMaxDF ? 1 : 0;
+    // K(R, S_i): update_kcols_kernel writes an N x 64 buffer that the update
+    // kernel loads by TMA, one 128-row tile per row block
     float* Kc = nullptr;
     static thread_local const void* last_K = nullptr;
     static thread_local int64_t last_KN = -1;
     static thread_local CUtensorMap tmk;
-    if (!fuse_k) {
+    {
         Kc = arena_get<float>(ctx, "utc.kc", (size_t)N * kCols, &rc);
         if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
         if (Kc != last_K || N != last_KN) {
@@ -561,7 +527,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
             last_KN = N;
         }
     }
-    if (!fuse_k) {
+    {
         ProfScope ps(ctx, "rp_update_kcols", s);
         const size_t ksm = (size_t)(kRows + kCols) * (d + 1) * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
@@ -580,7 +546,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     {
         ProfScope ps(ctx, "rp_update", s);
         update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, tmk, F, ldF, N, minv_f, b, bprep, rv, dvec, dblk,
-                                                          err, X, d, (float)scale, sacc, fuse_k);
+                                                          err);
         KEVD_LAUNCH(ctx);
     }
     return KEVD_OK;
