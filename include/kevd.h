@@ -24,6 +24,9 @@
  *     written (they synchronise the stream when they return host data).
  *   - A context is bound to one device and is not internally locked: use one
  *     context per host thread.
+ *   - Sample dimension d (features per state): 1..1024 everywhere; rows are
+ *     staged in shared memory a fixed-width chunk of features at a time, so
+ *     the reference's delay windows (Nq = 512) are accepted as they are.
  *   - Kernel: K(i,j) = exp(-scale * ||x_i - x_j||^2).  The Hankel view of the
  *     reference uses scale = 1/(Nq*bw) (ks_arpclm.cu:275); dense states use
  *     scale = 1/eps.
@@ -130,7 +133,7 @@ int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d,
  * tiles (0: chosen from the batch size) and placed in one device work queue; a
  * persistent grid takes items with an atomic counter and a second kernel sums
  * each job's item partials in item order (deterministic).  Per job: sums[j] as
- * kevd_calibrate, n_scales <= 64, d <= 128.  X: device; scales, sums: host. */
+ * kevd_calibrate, n_scales <= 64, d <= 1024.  X: device; scales, sums: host. */
 typedef struct {
     const float* X;
     int64_t N;
@@ -162,7 +165,7 @@ int kevd_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
 
 typedef struct {
     int64_t k_max;          /* factor capacity (target rank)                 */
-    int32_t block;          /* proposals per round b, 1..128                  */
+    int32_t block;          /* proposals per round b, 1..64                   */
     int32_t max_rounds;     /* round limit                                    */
     double tol;             /* rejection tolerance (reference: 1e-10)         */
     double err_target;      /* stop once trace error <= this (0: never)       */

@@ -26,7 +26,9 @@ namespace {
 
 constexpr int kTile = 128;
 constexpr int kMaxScalesB = 64;
-constexpr int kMaxDB = 128;
+constexpr int kMaxDB = 1024;
+constexpr int kFC = 64;            // feature chunk staged in shared memory
+constexpr int kFP = kFC + 1;
 
 struct JobDesc {
     const float* X;
@@ -60,23 +62,23 @@ __device__ __forceinline__ void tile_ij(int64_t t, int64_t& ti, int64_t& tj) {
     tj = t - i * (i + 1) / 2;
 }
 
-__device__ __forceinline__ void stage_rows(const float* __restrict__ X, int64_t N, int d, int64_t r0, float* dst) {
-    const int dp = d + 1;
-    for (int e = threadIdx.x; e < kTile * d; e += blockDim.x) {
-        const int rr = e / d, kk = e - rr * d;
+__device__ __forceinline__ void stage_chunk(const float* __restrict__ X, int64_t N, int d, int64_t r0, int c0, int w,
+                                            float* dst) {
+    for (int e = threadIdx.x; e < kTile * w; e += blockDim.x) {
+        const int rr = e / w, kk = e - rr * w;
         const int64_t r = r0 + rr;
-        dst[rr * dp + kk] = (r < N) ? X[r * d + kk] : 0.f;
+        dst[rr * kFP + kk] = (r < N) ? X[r * d + c0 + kk] : 0.f;
     }
 }
 
 __global__ void __launch_bounds__(256, 2)
 calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict__ items, int item_base,
-                       int n_items, const float* __restrict__ c2all, int dmax, int* __restrict__ counter,
+                       int n_items, const float* __restrict__ c2all, int* __restrict__ counter,
                        double* __restrict__ partial) {
     extern __shared__ float sm[];
     float* xi = sm;
-    float* xj = sm + kTile * (dmax + 1);
-    float* cs = xj + kTile * (dmax + 1);     // kMaxScalesB
+    float* xj = sm + kTile * kFP;
+    float* cs = xj + kTile * kFP;            // kMaxScalesB
     float* red = cs + kMaxScalesB;           // 8 warps x kMaxScalesB
     __shared__ int cur;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -89,34 +91,37 @@ calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict_
         const int it = item_base + cur;
         const Item item = items[it];
         const JobDesc jb = jobs[item.job];
-        const int d = jb.d, dp = d + 1, ns = jb.n_scales;
+        const int d = jb.d, ns = jb.n_scales;
         for (int j = threadIdx.x; j < ns; j += blockDim.x) cs[j] = c2all[jb.scale_off + j];
         double acc = 0.0;   // thread j < ns owns eps j
         for (int64_t t = item.t0; t < item.t1; ++t) {
             int64_t ti, tj;
             tile_ij(t, ti, tj);
-            __syncthreads();
-            stage_rows(jb.X, jb.N, d, ti * kTile, xi);
-            stage_rows(jb.X, jb.N, d, tj * kTile, xj);
-            __syncthreads();
             float D[8][8];
 #pragma unroll
             for (int a = 0; a < 8; ++a)
 #pragma unroll
                 for (int b = 0; b < 8; ++b) D[a][b] = 0.f;
-            for (int k = 0; k < d; ++k) {
-                float vi[8], vj[8];
+            for (int c0 = 0; c0 < d; c0 += kFC) {
+                const int w = min(kFC, d - c0);
+                __syncthreads();
+                stage_chunk(jb.X, jb.N, d, ti * kTile, c0, w, xi);
+                stage_chunk(jb.X, jb.N, d, tj * kTile, c0, w, xj);
+                __syncthreads();
+                for (int k = 0; k < w; ++k) {
+                    float vi[8], vj[8];
 #pragma unroll
-                for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * dp + k];
+                    for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * kFP + k];
 #pragma unroll
-                for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * dp + k];
+                    for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * kFP + k];
 #pragma unroll
-                for (int a = 0; a < 8; ++a)
+                    for (int a = 0; a < 8; ++a)
 #pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        const float u = vi[a] - vj[b];
-                        D[a][b] = fmaf(u, u, D[a][b]);
-                    }
+                        for (int b = 0; b < 8; ++b) {
+                            const float u = vi[a] - vj[b];
+                            D[a][b] = fmaf(u, u, D[a][b]);
+                        }
+                }
             }
             const int64_t gi0 = ti * kTile + ty, gj0 = tj * kTile + tx;
 #pragma unroll
@@ -161,8 +166,8 @@ __global__ void calibrate_queue_reduce_kernel(const JobDesc* __restrict__ jobs, 
     }
 }
 
-size_t queue_smem(int dmax) {
-    return (2 * kTile * (size_t)(dmax + 1) + kMaxScalesB + 8 * kMaxScalesB) * sizeof(float);
+size_t queue_smem() {
+    return (2 * kTile * (size_t)kFP + kMaxScalesB + 8 * kMaxScalesB) * sizeof(float);
 }
 
 }  // namespace
@@ -175,7 +180,6 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     std::vector<Item> hi;
     std::vector<float> hc;
     int64_t total_tiles = 0;
-    int dmax = 1;
     for (int q = 0; q < n_jobs; ++q) {
         const kevd_calib_job& j = jobs[q];
         if (!j.X || !j.scales || !j.sums || j.N < 1 || j.d < 1 || j.d > kMaxDB || j.n_scales < 1 ||
@@ -184,20 +188,14 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
                              "1 <= n_scales <= %d", q, kMaxDB, kMaxScalesB);
         const int64_t nt = (j.N + kTile - 1) / kTile;
         total_tiles += nt * (nt + 1) / 2;
-        dmax = std::max(dmax, (int)j.d);
     }
     // item size: about 16 items per SM over the whole batch unless given
     int64_t per = tiles_per_item > 0 ? tiles_per_item
                                      : std::max<int64_t>(1, total_tiles / ((int64_t)ctx->num_sms * 16));
-    // jobs grouped by feature-dimension class (d <= 32, <= 64, <= 128): one
-    // persistent launch per class, shared memory sized for that class, so small-d
-    // datasets keep two CTAs per SM
-    const int cls_d[3] = {32, 64, 128};
-    std::vector<int> order;
-    for (int c = 0; c < 3; ++c)
-        for (int q = 0; q < n_jobs; ++q)
-            if ((c == 0 ? 0 : cls_d[c - 1]) < jobs[q].d && jobs[q].d <= cls_d[c]) order.push_back(q);
-    int cls_begin[4] = {0, 0, 0, 0};
+    // features are staged kFC at a time, so shared memory does not depend on d
+    // and one persistent launch serves every dataset of the batch
+    std::vector<int> order(n_jobs);
+    for (int q = 0; q < n_jobs; ++q) order[q] = q;
     for (int oi = 0; oi < n_jobs; ++oi) {
         const int q = order[oi];
         const kevd_calib_job& j = jobs[q];
@@ -218,8 +216,6 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
         for (int64_t t0 = 0; t0 < tiles; t0 += per) hi.push_back(Item{q, 0, t0, std::min(tiles, t0 + per)});
         d.n_items = (int32_t)hi.size() - d.item0;
         d.pad = 0;
-        const int c = j.d <= 32 ? 0 : (j.d <= 64 ? 1 : 2);
-        for (int cc = c + 1; cc < 4; ++cc) cls_begin[cc] = (int)hi.size();
     }
     if (hi.size() > (size_t)INT32_MAX / 2) return set_error(ctx, KEVD_ERR_ARG, "calibrate_batched: too many items");
     const int n_items = (int)hi.size();
@@ -227,24 +223,19 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     JobDesc* dj = arena_get<JobDesc>(ctx, "cb.jobs", n_jobs, &st);
     Item* di = arena_get<Item>(ctx, "cb.items", n_items, &st);
     float* dc = arena_get<float>(ctx, "cb.c2", hc.size(), &st);
-    int* counter = arena_get<int>(ctx, "cb.counter", 3, &st);
+    int* counter = arena_get<int>(ctx, "cb.counter", 1, &st);
     double* partial = arena_get<double>(ctx, "cb.partial", (size_t)n_items * kMaxScalesB, &st);
     double* out = arena_get<double>(ctx, "cb.out", (size_t)n_jobs * kMaxScalesB, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "calibrate_batched: out of device memory");
     KEVD_CUDA(ctx, cudaMemcpyAsync(dj, hj.data(), hj.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemcpyAsync(di, hi.data(), hi.size() * sizeof(Item), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemcpyAsync(dc, hc.data(), hc.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    KEVD_CUDA(ctx, cudaMemsetAsync(counter, 0, 3 * sizeof(int), s));
-    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_queue_kernel), (int)queue_smem(dmax)));
-    for (int c = 0; c < 3; ++c) {
-        const int b0 = cls_begin[c], b1 = c < 2 ? cls_begin[c + 1] : n_items;
-        if (b1 <= b0) continue;
-        const int dcls = std::min(dmax, cls_d[c]);
-        const size_t smem = queue_smem(dcls);
-        const int per_sm = smem * 2 <= (size_t)220 * 1024 ? 2 : 1;   // persistent: every CTA resident
+    KEVD_CUDA(ctx, cudaMemsetAsync(counter, 0, sizeof(int), s));
+    const size_t smem = queue_smem();
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&calibrate_queue_kernel), (int)smem));
+    {
         ProfScope ps(ctx, "calibrate_queue", s);
-        calibrate_queue_kernel<<<ctx->num_sms * per_sm, 256, smem, s>>>(dj, di, b0, b1 - b0, dc, dcls, counter + c,
-                                                                         partial);
+        calibrate_queue_kernel<<<ctx->num_sms * 2, 256, smem, s>>>(dj, di, 0, n_items, dc, counter, partial);
         KEVD_LAUNCH(ctx);
     }
     calibrate_queue_reduce_kernel<<<n_jobs, 64, 0, s>>>(dj, n_jobs, partial, out);

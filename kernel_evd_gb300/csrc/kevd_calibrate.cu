@@ -24,7 +24,9 @@ namespace kevd {
 
 constexpr int kCalTile = 128;
 constexpr int kCalMaxScales = 256;
-constexpr int kCalMaxD = 128;
+constexpr int kCalMaxD = 1024;
+constexpr int kFC = 64;            // feature chunk staged in shared memory
+constexpr int kFP = kFC + 1;       // its row pitch (bank-conflict padding)
 
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;
@@ -41,38 +43,46 @@ __device__ __forceinline__ void tri_tile(int64_t t, int64_t& ti, int64_t& tj) {
     tj = t - i * (i + 1) / 2;
 }
 
-// Loads rows [r0, r0+128) of X into a [128][d+1] shared tile (zeros past N).
-__device__ __forceinline__ void load_rows(const float* __restrict__ X, int64_t N, int d,
-                                          int64_t r0, float* dst) {
-    const int dp = d + 1;
-    for (int e = threadIdx.x; e < kCalTile * d; e += blockDim.x) {
-        const int rr = e / d, kk = e - rr * d;
+// Loads features [c0, c0 + w) of rows [r0, r0+128) of X into a [128][kFP]
+// shared tile (zeros past N).
+__device__ __forceinline__ void load_chunk(const float* __restrict__ X, int64_t N, int d, int64_t r0, int c0,
+                                           int w, float* dst) {
+    for (int e = threadIdx.x; e < kCalTile * w; e += blockDim.x) {
+        const int rr = e / w, kk = e - rr * w;
         const int64_t r = r0 + rr;
-        dst[rr * dp + kk] = (r < N) ? X[r * d + kk] : 0.f;
+        dst[rr * kFP + kk] = (r < N) ? X[r * d + c0 + kk] : 0.f;
     }
 }
 
-// 8 x 8 squared distances of thread (ty, tx): rows ty + 16a, cols tx + 16b.
-__device__ __forceinline__ void tile_dist(const float* xi, const float* xj, int d, int ty, int tx,
-                                          float (&D)[8][8]) {
-    const int dp = d + 1;
+// 8 x 8 squared distances of thread (ty, tx): rows ti*128 + ty + 16a against
+// rows tj*128 + tx + 16b, summed over the feature index in increasing order,
+// the features staged kFC at a time (any d).  Called by all threads of the CTA.
+__device__ __forceinline__ void tile_dist(const float* __restrict__ X, int64_t N, int d, int64_t ti, int64_t tj,
+                                          float* xi, float* xj, int ty, int tx, float (&D)[8][8]) {
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int b = 0; b < 8; ++b) D[a][b] = 0.f;
-    for (int k = 0; k < d; ++k) {
-        float vi[8], vj[8];
+    for (int c0 = 0; c0 < d; c0 += kFC) {
+        const int w = min(kFC, d - c0);
+        __syncthreads();
+        load_chunk(X, N, d, ti * kCalTile, c0, w, xi);
+        load_chunk(X, N, d, tj * kCalTile, c0, w, xj);
+        __syncthreads();
+        for (int k = 0; k < w; ++k) {
+            float vi[8], vj[8];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * dp + k];
+            for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * kFP + k];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * dp + k];
+            for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * kFP + k];
 #pragma unroll
-        for (int a = 0; a < 8; ++a)
+            for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const float t = vi[a] - vj[b];
-                D[a][b] = fmaf(t, t, D[a][b]);
-            }
+                for (int b = 0; b < 8; ++b) {
+                    const float t = vi[a] - vj[b];
+                    D[a][b] = fmaf(t, t, D[a][b]);
+                }
+        }
     }
 }
 
@@ -81,10 +91,9 @@ calibrate_tiles_kernel(const float* __restrict__ X, int64_t N, int d,
                        const float* __restrict__ c2, int n_scales, int64_t n_tiles,
                        double* __restrict__ partial) {
     extern __shared__ float sm[];
-    const int dp = d + 1;
     float* xi = sm;
-    float* xj = sm + kCalTile * dp;
-    float* cs = xj + kCalTile * dp;                      // n_scales
+    float* xj = sm + kCalTile * kFP;
+    float* cs = xj + kCalTile * kFP;                     // n_scales
     float* red = cs + kCalMaxScales;                     // 8 warps x n_scales
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -93,12 +102,8 @@ calibrate_tiles_kernel(const float* __restrict__ X, int64_t N, int d,
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         int64_t ti, tj;
         tri_tile(t, ti, tj);
-        __syncthreads();
-        load_rows(X, N, d, ti * kCalTile, xi);
-        load_rows(X, N, d, tj * kCalTile, xj);
-        __syncthreads();
         float D[8][8];
-        tile_dist(xi, xj, d, ty, tx, D);
+        tile_dist(X, N, d, ti, tj, xi, xj, ty, tx, D);
         const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
 #pragma unroll
         for (int a = 0; a < 8; ++a)
@@ -145,10 +150,9 @@ __global__ void __launch_bounds__(256, 1)
 calibrate_tiles_fp64_kernel(const float* __restrict__ X, int64_t N, int d, const double* __restrict__ sc,
                             int n_scales, int64_t n_tiles, double* __restrict__ partial) {
     extern __shared__ float sm[];
-    const int dp = d + 1;
     float* xi = sm;
-    float* xj = sm + kCalTile * dp;
-    double* cs = reinterpret_cast<double*>(xj + kCalTile * dp + 2);   // 8-byte aligned (dp*128*2 floats is even)
+    float* xj = sm + kCalTile * kFP;
+    double* cs = reinterpret_cast<double*>(xj + kCalTile * kFP + 2);   // 8-byte aligned (2 x 128 x kFP floats is even)
     double* red = cs + kCalMaxScales;                                   // 8 warps x n_scales
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -157,28 +161,31 @@ calibrate_tiles_fp64_kernel(const float* __restrict__ X, int64_t N, int d, const
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         int64_t ti, tj;
         tri_tile(t, ti, tj);
-        __syncthreads();
-        load_rows(X, N, d, ti * kCalTile, xi);
-        load_rows(X, N, d, tj * kCalTile, xj);
-        __syncthreads();
         double D[8][8];
 #pragma unroll
         for (int a = 0; a < 8; ++a)
 #pragma unroll
             for (int b = 0; b < 8; ++b) D[a][b] = 0.0;
-        for (int k = 0; k < d; ++k) {
-            double vi[8], vj[8];
+        for (int c0 = 0; c0 < d; c0 += kFC) {
+            const int w = min(kFC, d - c0);
+            __syncthreads();
+            load_chunk(X, N, d, ti * kCalTile, c0, w, xi);
+            load_chunk(X, N, d, tj * kCalTile, c0, w, xj);
+            __syncthreads();
+            for (int k = 0; k < w; ++k) {
+                double vi[8], vj[8];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) vi[a] = (double)xi[(ty + 16 * a) * dp + k];
+                for (int a = 0; a < 8; ++a) vi[a] = (double)xi[(ty + 16 * a) * kFP + k];
 #pragma unroll
-            for (int b = 0; b < 8; ++b) vj[b] = (double)xj[(tx + 16 * b) * dp + k];
+                for (int b = 0; b < 8; ++b) vj[b] = (double)xj[(tx + 16 * b) * kFP + k];
 #pragma unroll
-            for (int a = 0; a < 8; ++a)
+                for (int a = 0; a < 8; ++a)
 #pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    const double u = vi[a] - vj[b];
-                    D[a][b] = fma(u, u, D[a][b]);
-                }
+                    for (int b = 0; b < 8; ++b) {
+                        const double u = vi[a] - vj[b];
+                        D[a][b] = fma(u, u, D[a][b]);
+                    }
+            }
         }
         const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
 #pragma unroll
@@ -211,7 +218,8 @@ calibrate_tiles_fp64_kernel(const float* __restrict__ X, int64_t N, int d, const
 }
 
 static size_t calib_smem_fp64(int d) {
-    return 2 * kCalTile * (size_t)(d + 1) * sizeof(float) + 16 + 9 * kCalMaxScales * sizeof(double);
+    (void)d;
+    return 2 * kCalTile * (size_t)kFP * sizeof(float) + 16 + 9 * kCalMaxScales * sizeof(double);
 }
 
 int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales, int n_scales,
@@ -245,7 +253,8 @@ int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const do
 }
 
 static size_t calib_smem(int d) {
-    return (2 * kCalTile * (size_t)(d + 1) + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
+    (void)d;
+    return (2 * kCalTile * (size_t)kFP + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
 }
 
 int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
@@ -391,21 +400,16 @@ __global__ void __launch_bounds__(256, 2)
 median_tiles_kernel(const float* __restrict__ X, int64_t N, int d, int64_t n_tiles, int shift,
                     unsigned mask, unsigned prefix, int hi_shift, unsigned* __restrict__ hist) {
     extern __shared__ float sm[];
-    const int dp = d + 1;
     float* xi = sm;
-    float* xj = sm + kCalTile * dp;
-    unsigned* h = reinterpret_cast<unsigned*>(xj + kCalTile * dp);
+    float* xj = sm + kCalTile * kFP;
+    unsigned* h = reinterpret_cast<unsigned*>(xj + kCalTile * kFP);
     for (int e = threadIdx.x; e < kHistBins; e += blockDim.x) h[e] = 0u;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         int64_t ti, tj;
         tri_tile(t, ti, tj);
-        __syncthreads();
-        load_rows(X, N, d, ti * kCalTile, xi);
-        load_rows(X, N, d, tj * kCalTile, xj);
-        __syncthreads();
         float D[8][8];
-        tile_dist(xi, xj, d, ty, tx, D);
+        tile_dist(X, N, d, ti, tj, xi, xj, ty, tx, D);
         const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
 #pragma unroll
         for (int a = 0; a < 8; ++a)
@@ -456,7 +460,7 @@ int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64
     int st = KEVD_OK;
     unsigned* hist = arena_get<unsigned>(ctx, "med.hist", kHistBins, &st);
     if (st != KEVD_OK) return st;
-    const size_t smem = 2 * kCalTile * (size_t)(d + 1) * sizeof(float) + kHistBins * sizeof(unsigned);
+    const size_t smem = 2 * kCalTile * (size_t)kFP * sizeof(float) + kHistBins * sizeof(unsigned);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&median_tiles_kernel), (int)smem));
     const int shifts[3] = {20, 8, 0};
     const unsigned masks[3] = {0xfffu, 0xfffu, 0xffu};

@@ -493,47 +493,61 @@ int kevd_nystrom_prepare(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, do
 constexpr int kNyRows = 32;
 constexpr int kNyLm = 32;
 constexpr int kNyMaxOut = 9;   // ceil(32 * 65 / 256) outputs per thread
+constexpr int kNyFeat = 128;   // features staged at a time
 
 __global__ void __launch_bounds__(256) nystrom_eval_kernel(const float* __restrict__ Y, int64_t n,
                                                            const float* __restrict__ xs, const double* __restrict__ zp,
                                                            int64_t r, int d, int k_out, double scale,
                                                            float* __restrict__ Uy) {
     extern __shared__ __align__(16) unsigned char ny_smem[];
-    const int dp = d + 1, kc = k_out + 1;
+    constexpr int dp = kNyFeat + 1;
+    const int kc = k_out + 1;
     double* kv = reinterpret_cast<double*>(ny_smem);     // 32 x 33
     double* zc = kv + kNyRows * (kNyLm + 1);             // 32 landmarks x kc
-    float* ys = reinterpret_cast<float*>(zc + kNyLm * kc);  // 32 x dp
+    float* ys = reinterpret_cast<float*>(zc + kNyLm * kc);  // 32 x dp (one feature chunk)
     float* xc = ys + kNyRows * dp;                       // 32 x dp
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const float fscale = (float)scale;
     const int64_t row0 = (int64_t)blockIdx.x * kNyRows;
-    for (int e = threadIdx.x; e < kNyRows * d; e += 256) {
-        const int rr = e / d, kk = e - rr * d;
-        ys[rr * dp + kk] = (row0 + rr < n) ? Y[(row0 + rr) * d + kk] : 0.f;
-    }
+    // with one feature chunk the query rows are staged once for all landmarks
+    const bool one_chunk = d <= kNyFeat;
+    if (one_chunk)
+        for (int e = threadIdx.x; e < kNyRows * d; e += 256) {
+            const int rr = e / d, kk = e - rr * d;
+            ys[rr * dp + kk] = (row0 + rr < n) ? Y[(row0 + rr) * d + kk] : 0.f;
+        }
     double acc[kNyMaxOut];
 #pragma unroll
     for (int q = 0; q < kNyMaxOut; ++q) acc[q] = 0.0;
     const int n_out = kNyRows * kc;
     for (int64_t j0 = 0; j0 < r; j0 += kNyLm) {
         __syncthreads();
-        for (int e = threadIdx.x; e < kNyLm * d; e += 256) {
-            const int jj = e / d, kk = e - jj * d;
-            xc[jj * dp + kk] = (j0 + jj < r) ? xs[(j0 + jj) * d + kk] : 0.f;
-        }
         for (int e = threadIdx.x; e < kNyLm * kc; e += 256) {
             const int jj = e / kc, c = e - jj * kc;
             zc[jj * kc + c] = (j0 + jj < r) ? zp[(int64_t)c * r + j0 + jj] : 0.0;
         }
-        __syncthreads();
-        // K(row ty + 8i, landmark tx)
+        // K(row ty + 8i, landmark tx): features kNyFeat at a time, in increasing order
         float dist[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kk = 0; kk < d; ++kk) {
-            const float c = xc[tx * dp + kk];
+        for (int f0 = 0; f0 < d; f0 += kNyFeat) {
+            const int w = min(kNyFeat, d - f0);
+            __syncthreads();
+            if (!one_chunk)
+                for (int e = threadIdx.x; e < kNyRows * w; e += 256) {
+                    const int rr = e / w, kk = e - rr * w;
+                    ys[rr * dp + kk] = (row0 + rr < n) ? Y[(row0 + rr) * d + f0 + kk] : 0.f;
+                }
+            for (int e = threadIdx.x; e < kNyLm * w; e += 256) {
+                const int jj = e / w, kk = e - jj * w;
+                xc[jj * dp + kk] = (j0 + jj < r) ? xs[(j0 + jj) * d + f0 + kk] : 0.f;
+            }
+            __syncthreads();
+            for (int kk = 0; kk < w; ++kk) {
+                const float c = xc[tx * dp + kk];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float t = ys[(ty + 8 * i) * dp + kk] - c;
-                dist[i] = fmaf(t, t, dist[i]);
+                for (int i = 0; i < 4; ++i) {
+                    const float t = ys[(ty + 8 * i) * dp + kk] - c;
+                    dist[i] = fmaf(t, t, dist[i]);
+                }
             }
         }
 #pragma unroll
@@ -567,7 +581,8 @@ __global__ void __launch_bounds__(256) nystrom_eval_kernel(const float* __restri
 }
 
 static size_t nystrom_smem(int d, int k_out) {
-    return (size_t)kNyRows * (kNyLm + 1) * 8 + (size_t)kNyLm * (k_out + 1) * 8 + 2 * (size_t)kNyRows * (d + 1) * 4;
+    (void)d;
+    return (size_t)kNyRows * (kNyLm + 1) * 8 + (size_t)kNyLm * (k_out + 1) * 8 + 2 * (size_t)kNyRows * (kNyFeat + 1) * 4;
 }
 
 int kevd_nystrom_eval(kevd_ctx* ctx, const kevd_model* model, const float* Y, int64_t n, float* Uy,

@@ -923,7 +923,30 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     }
     // dense 2: W = L^T B L
     const double one = 1.0;
-    {
+    if (sizeof(T) == 4) {
+        // FP32 factor: W only has to deliver the leading subspace, which is
+        // refined against F afterwards, and B carries the 1e-5 error of the
+        // 3xTF32 Gram, so W is formed in FP32 (two strmm) and widened back
+        ProfScope p2(ctx, "dense_trmm", s);
+        float* Lf = arena_get<float>(ctx, "ev.Lf", (size_t)k * k, &st);
+        float* Bf = arena_get<float>(ctx, "ev.Bf", (size_t)k * k, &st);
+        float* Wf = arena_get<float>(ctx, "ev.Wf32", (size_t)k * k, &st);
+        if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+        const int g = ctx->num_sms * 4;
+        ev_d2f_kernel<<<g, 256, 0, s>>>(A, Lf, k * k);
+        KEVD_LAUNCH(ctx);
+        ev_d2f_kernel<<<g, 256, 0, s>>>(B, Bf, k * k);
+        KEVD_LAUNCH(ctx);
+        const float onef = 1.f;
+        KEVD_BLAS(ctx, cublasStrmm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                   CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &onef, Lf, (int)k, Bf, (int)k, Wf,
+                                   (int)k));
+        KEVD_BLAS(ctx, cublasStrmm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                                   CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &onef, Lf, (int)k, Wf, (int)k, Wf,
+                                   (int)k));
+        ev_f2d_kernel<<<g, 256, 0, s>>>(Wf, W, k * k);
+        KEVD_LAUNCH(ctx);
+    } else {
         ProfScope p2(ctx, "dense_trmm", s);
         KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
                                    CUBLAS_DIAG_NON_UNIT, (int)k, (int)k, &one, A, (int)k, B, (int)k, W,

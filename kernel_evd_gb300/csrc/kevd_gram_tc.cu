@@ -12,17 +12,20 @@
 // ks_kevd.cu:1152-1158).  The relative error of a Gram entry is about 1e-5;
 // eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
 //
-// CTA roles (320 threads):
+// CTA roles (448 threads):
 //   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
 //               lanes 32q..32q+31 = tile rows)
-//   warps 4-7   converters: thread m owns row m of both operand tiles (factor
-//               columns a0+m and b0+m, 32 rows of F each): row scaling and the
-//               tf32 split; the a operand goes to Tensor Memory (tcgen05.st,
-//               hi and lo columns per stage), the b operand stays in shared
-//               memory (hi in place, lo beside it)
+//   warps 4-7   a converters: thread m owns row m of the a tile (factor column
+//               a0+m, 32 rows of F): row scaling and the tf32 split, written to
+//               the stage's Tensor Memory a-slot (tcgen05.st, hi and lo columns)
 //   warp 8      TMA producer
 //   warp 9      TMEM allocation and the single MMA-issuing thread (A from
 //               Tensor Memory, B from shared memory)
+//   warps 10-13 b converters: row m of the b tile, split in shared memory (hi
+//               in place, lo in the b-lo tile)
+// The conversion is the per-stage critical path (measured: with one group of
+// four warps doing both operands the MMA waited on it half the time), hence
+// two groups of four, one warp per SM sub-partition each.
 // A 4-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
 // double-buffered TMEM accumulator (2 x 128 columns) are handed over with
 // mbarriers; every wait is bounded and sets an error flag on timeout.
@@ -50,11 +53,12 @@ constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
 constexpr int kStageBytes = 3 * kOpBytes;   // a (raw), b hi, b lo
 constexpr int kEpiWarps = 4;        // warps 0-3
-constexpr int kCvtWarp0 = 4;        // warps 4-7
-constexpr int kCvtWarps = 4;
+constexpr int kCvtWarp0 = 4;        // warps 4-7: a operand -> Tensor Memory
 constexpr int kProdWarp = 8;
 constexpr int kMmaWarp = 9;
-constexpr int kThreads = 10 * 32;
+constexpr int kCvtBWarp0 = 10;      // warps 10-13: b operand, in shared memory
+constexpr int kCvtWarps = 8;        // arrivals per stage on the "converted" barrier
+constexpr int kThreads = 14 * 32;
 constexpr uint32_t kTmemCols = 512;       // accumulators [0,256), a-operand slots [256,512)
 constexpr uint32_t kTmemA = 256;
 constexpr uint32_t kTmemASlot = 64;       // hi columns [0,32), lo [32,64)
@@ -192,9 +196,11 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
             }
         }
         __syncwarp();
-    } else if (warp >= kCvtWarp0 && warp < kCvtWarp0 + kCvtWarps) {
-        // ---------------- converters: thread m owns row m of the a and b tiles
-        const int m = (warp - kCvtWarp0) * 32 + lane;
+    } else if ((warp >= kCvtWarp0 && warp < kCvtWarp0 + 4) || warp >= kCvtBWarp0) {
+        // ---------------- converters: thread m owns row m of the a tile (warps
+        // 4-7, to Tensor Memory) or of the b tile (warps 10-13, in place)
+        const bool grp_a = warp < kProdWarp;
+        const int m = 32 * (warp & 3) + lane;
         const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);   // this warp's TMEM lanes
         const bool aok = (a0 + m) < k, bok = (b0 + m) < k;
         // row weights one stage ahead of their use
@@ -214,17 +220,19 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
             }
             uint8_t* st = base + (size_t)slot * kStageAlloc;
             float y[32], h[32];
-            // a operand -> Tensor Memory
-            const uint32_t ta = tlane + kTmemA + (uint32_t)slot * kTmemASlot;
-            load_row(st, m, y);
-            scale_split(y, h, w, aok);
-            tc::tmem_st32(ta, h);
-            if (diag) store_row(st, m, h);
-            lo_part(y, h);
-            tc::tmem_st32(ta + 32, h);
-            if (diag) {
-                store_row(st + 2 * kOpBytes, m, h);   // b = a: hi in place in the a tile, lo in the b-lo tile
-            } else {
+            if (grp_a) {
+                // a operand -> Tensor Memory (on a diagonal tile also b, in place)
+                const uint32_t ta = tlane + kTmemA + (uint32_t)slot * kTmemASlot;
+                load_row(st, m, y);
+                scale_split(y, h, w, aok);
+                tc::tmem_st32(ta, h);
+                if (diag) store_row(st, m, h);
+                lo_part(y, h);
+                tc::tmem_st32(ta + 32, h);
+                if (diag) store_row(st + 2 * kOpBytes, m, h);   // b = a: lo in the b-lo tile
+                tc::tmem_wait_st();
+                tc::tc_fence_before();
+            } else if (!diag) {
                 uint8_t* bt = st + kOpBytes;
                 load_row(bt, m, y);
                 scale_split(y, h, w, bok);
@@ -232,9 +240,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                 lo_part(y, h);
                 store_row(st + 2 * kOpBytes, m, h);
             }
-            tc::tmem_wait_st();
             tc::fence_async_smem();
-            tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }

@@ -15,6 +15,10 @@
 
 namespace kevd {
 
+// Largest sample dimension d (features per state) the kernels accept; rows
+// are staged in shared memory a fixed-width chunk of features at a time.
+constexpr int kMaxFeatures = 1024;
+
 constexpr int kNumSMs = 152;
 
 // Status with a message stored in the context.

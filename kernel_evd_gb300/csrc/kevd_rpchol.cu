@@ -37,6 +37,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
 constexpr int kRowBlock = 128;   // rows per update CTA (= rows per d partial sum)
 constexpr int kMaxBlock = 64;    // proposals per round supported by the SIMT update
 constexpr int kColChunk = 32;    // F columns per hgram CTA
+constexpr int kFeat = 64;        // features staged at a time by the SIMT update
 constexpr int kSampleThreads = 1024;
 
 struct RoundState {
@@ -223,18 +224,31 @@ rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ 
         // K(S', S') in FP64, rows split over the remaining CTAs
         const int nk = gridDim.x - n_split;
         const int part = blockIdx.x - n_split;
-        for (int e = tid; e < b * d; e += 256) {
-            const int p = e / d, k = e - p * d;
-            xs[p * 129 + k] = X[props[p] * d + k];
-        }
+        // rows of S' staged in shared memory up to 128 features, read from
+        // global memory (L2-resident, b rows) beyond; same summation order
+        const bool staged = d <= 128;
+        if (staged)
+            for (int e = tid; e < b * d; e += 256) {
+                const int p = e / d, k = e - p * d;
+                xs[p * 129 + k] = X[props[p] * d + k];
+            }
         __syncthreads();
         for (int e = tid; e < b * b; e += 256) {
             const int p = e / b, q = e - p * b;
             if (p % nk != part) continue;
             double acc = 0.0;
-            for (int k = 0; k < d; ++k) {
-                const double t = (double)xs[p * 129 + k] - (double)xs[q * 129 + k];
-                acc += t * t;
+            if (staged) {
+                for (int k = 0; k < d; ++k) {
+                    const double t = (double)xs[p * 129 + k] - (double)xs[q * 129 + k];
+                    acc += t * t;
+                }
+            } else {
+                const float* xp = X + props[p] * d;
+                const float* xq = X + props[q] * d;
+                for (int k = 0; k < d; ++k) {
+                    const double t = (double)__ldg(xp + k) - (double)__ldg(xq + k);
+                    acc += t * t;
+                }
             }
             kss[p * b + q] = exp(-scale * acc);
         }
@@ -344,8 +358,9 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
     const int64_t r = st->r_old;
     constexpr int KC = UpdSmem<T>::KC;
     extern __shared__ __align__(16) unsigned char smraw[];
-    // region 1 (phase A: X rows; phase B: F tiles), then Tm, then Minv
-    const int dp = d + 1;
+    // region 1 (phase A: X rows, kFeat features at a time; phase B: F tiles),
+    // then Tm, then Minv
+    constexpr int dp = kFeat + 1;
     const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
     const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (KC + 1) * sizeof(T);
     const size_t reg1 = (reg1_a > reg1_b ? reg1_a : reg1_b + 0);
@@ -363,38 +378,42 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
     const int nrows = (int)min((int64_t)kRowBlock, N - row0);
 
     // phase A: K(R, S_i) into Tm
-    for (int e = tid; e < kRowBlock * d; e += 256) {
-        const int rr = e / d, k = e - rr * d;
-        xr[rr * dp + k] = (rr < nrows) ? X[(row0 + rr) * d + k] : 0.f;
-    }
-    for (int e = tid; e < nacc * d; e += 256) {
-        const int q = e / d, k = e - q * d;
-        xs[q * dp + k] = X[sacc[q] * d + k];
-    }
     for (int e = tid; e < nacc * nacc; e += 256) {
         const int a = e / nacc, q = e - a * nacc;
         Mv[a * (kMaxBlock + 1) + q] = sizeof(T) == 8 ? (T)minv[a * b + q] : (T)minv_f[a * b + q];
     }
-    __syncthreads();
     {
         T acc[8][4];
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = 0;
-        for (int k = 0; k < d; ++k) {
-            T vr[8], vs[4];
+        for (int c0 = 0; c0 < d; c0 += kFeat) {
+            const int w = min(kFeat, d - c0);
+            __syncthreads();
+            for (int e = tid; e < kRowBlock * w; e += 256) {
+                const int rr = e / w, k = e - rr * w;
+                xr[rr * dp + k] = (rr < nrows) ? X[(row0 + rr) * d + c0 + k] : 0.f;
+            }
+            for (int e = tid; e < nacc * w; e += 256) {
+                const int q = e / w, k = e - q * w;
+                xs[q * dp + k] = X[sacc[q] * d + c0 + k];
+            }
+            __syncthreads();
+            for (int k = 0; k < w; ++k) {
+                T vr[8], vs[4];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) vr[i] = (T)xr[(ty + 16 * i) * dp + k];
+                for (int i = 0; i < 8; ++i) vr[i] = (T)xr[(ty + 16 * i) * dp + k];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) vs[j] = (T)xs[min(tx + 16 * j, kMaxBlock - 1) * dp + k];
+                for (int j = 0; j < 4; ++j) vs[j] = (T)xs[min(tx + 16 * j, kMaxBlock - 1) * dp + k];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < 8; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const T t = vr[i] - vs[j];
-                    acc[i][j] += t * t;
-                }
+                    for (int j = 0; j < 4; ++j) {
+                        const T t = vr[i] - vs[j];
+                        acc[i][j] += t * t;
+                    }
+            }
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i)
@@ -503,7 +522,8 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
 
 template <typename T>
 static size_t update_smem(int d) {
-    const int dp = d + 1;
+    (void)d;
+    const int dp = kFeat + 1;
     const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
     const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (UpdSmem<T>::KC + 1) * sizeof(T);
     const size_t reg1 = ((std::max(reg1_a, reg1_b) + 15) / 16) * 16;
@@ -624,8 +644,8 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
 int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
                const kevd_rpchol_params* p, void* F, int64_t ldF, int64_t* piv, double* err,
                int32_t* accepted, kevd_rpchol_result* res, cudaStream_t s) {
-    if (!X || !p || !F || N < 1 || d < 1 || d > 128)
-        return set_error(ctx, KEVD_ERR_ARG, "rpchol: need X, F, N >= 1 and 1 <= d <= 128");
+    if (!X || !p || !F || N < 1 || d < 1 || d > kMaxFeatures)
+        return set_error(ctx, KEVD_ERR_ARG, "rpchol: need X, F, N >= 1 and 1 <= d <= %d", kMaxFeatures);
     if (p->block < 1 || p->block > kMaxBlock)
         return set_error(ctx, KEVD_ERR_ARG, "rpchol: block must be in [1, %d]", kMaxBlock);
     if (p->k_max < 1 || ldF < p->k_max || p->max_rounds < 1)
@@ -647,7 +667,7 @@ int run_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int n_jobs, int use
     if (!jobs || n_jobs < 1 || n_jobs > 1024) return set_error(ctx, KEVD_ERR_ARG, "rpchol_batched: 1..1024 jobs");
     for (int q = 0; q < n_jobs; ++q) {
         const kevd_rpchol_job& j = jobs[q];
-        if (!j.X || !j.F || !j.piv || j.N < 1 || j.d < 1 || j.d > 128 || j.block < 1 || j.block > kMaxBlock ||
+        if (!j.X || !j.F || !j.piv || j.N < 1 || j.d < 1 || j.d > kMaxFeatures || j.block < 1 || j.block > kMaxBlock ||
             j.k_max < 1 || j.ldF < j.k_max || j.max_rounds < 1 || !(j.scale > 0.0))
             return set_error(ctx, KEVD_ERR_ARG, "rpchol_batched: bad job %d", q);
     }

@@ -450,7 +450,7 @@ void kevd_server_destroy(kevd_server* s) {
 int kevd_server_submit_factorization(kevd_server* s, const float* X, int64_t N, int32_t d, double scale,
                                      int64_t k, int32_t block, int32_t k_out, uint64_t seed, int32_t precision,
                                      int64_t* request_id) {
-    if (!s || !X || !request_id || N < 2 || d < 1 || d > 128 || !(scale > 0.0) || k < 1 || k > N || block < 1 ||
+    if (!s || !X || !request_id || N < 2 || d < 1 || d > kMaxFeatures || !(scale > 0.0) || k < 1 || k > N || block < 1 ||
         block > 64 || k_out < 1 || k_out > kQueryMaxOut || k_out > k ||
         (precision != KEVD_FP64 && precision != KEVD_MIXED))
         return KEVD_ERR_ARG;

@@ -67,7 +67,8 @@ constexpr int kBOp = kCols * kKs * 4;     // 8 KB
 constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
 constexpr int kThreads = 320;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
-constexpr int kMaxD = 128;
+constexpr int kMaxD = kMaxFeatures;
+constexpr int kFeatChunk = 64;      // features staged at a time by update_kcols_kernel
 
 struct Bars {
     uint64_t tma_full[kStages];
@@ -378,39 +379,44 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
     if (st->done || st->nacc == 0) return;
     const int nacc = st->nacc;
     extern __shared__ float ksm[];
-    const int dp = d + 1;
+    constexpr int dp = kFeatChunk + 1;
     float* xr = ksm;                 // 128 x dp
     float* xq = ksm + kRows * dp;    // 64 x dp
     const int64_t row0 = (int64_t)blockIdx.x * kRows;
-    for (int e = threadIdx.x; e < kRows * d; e += 256) {
-        const int rr = e / d, kk = e - rr * d;
-        const int64_t i = row0 + rr;
-        xr[rr * dp + kk] = (i < N) ? X[i * d + kk] : 0.f;
-    }
-    for (int e = threadIdx.x; e < kCols * d; e += 256) {
-        const int q = e / d, kk = e - q * d;
-        xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + kk] : 0.f;
-    }
-    __syncthreads();
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float acc[8][4];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[a][c] = 0.f;
-    for (int kk = 0; kk < d; ++kk) {
-        float vr[8], vq[4];
+    // features kFeatChunk at a time, summed in increasing order
+    for (int c0 = 0; c0 < d; c0 += kFeatChunk) {
+        const int w = min(kFeatChunk, d - c0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < kRows * w; e += 256) {
+            const int rr = e / w, kk = e - rr * w;
+            const int64_t i = row0 + rr;
+            xr[rr * dp + kk] = (i < N) ? X[i * d + c0 + kk] : 0.f;
+        }
+        for (int e = threadIdx.x; e < kCols * w; e += 256) {
+            const int q = e / w, kk = e - q * w;
+            xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + c0 + kk] : 0.f;
+        }
+        __syncthreads();
+        for (int kk = 0; kk < w; ++kk) {
+            float vr[8], vq[4];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
+            for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
+            for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
 #pragma unroll
-        for (int a = 0; a < 8; ++a)
+            for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const float t = vr[a] - vq[c];
-                acc[a][c] = fmaf(t, t, acc[a][c]);
-            }
+                for (int c = 0; c < 4; ++c) {
+                    const float t = vr[a] - vq[c];
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                }
+        }
     }
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
@@ -529,7 +535,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     }
     {
         ProfScope ps(ctx, "rp_update_kcols", s);
-        const size_t ksm = (size_t)(kRows + kCols) * (d + 1) * sizeof(float);
+        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 1) * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
         update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
         KEVD_LAUNCH(ctx);

@@ -41,6 +41,8 @@ __device__ inline double kexp<double>(double x) { return exp(x); }
 template <>
 __device__ inline float kexp<float>(float x) { return expf(x); }
 
+constexpr int kBlkFeat = 128;   // features staged at a time
+
 // One CTA computes a 32 x 32 tile; thread (tx, ty) computes rows ty + 8j.
 template <typename T>
 __global__ void __launch_bounds__(256) kernel_block_kernel(
@@ -48,31 +50,36 @@ __global__ void __launch_bounds__(256) kernel_block_kernel(
     const int64_t* __restrict__ rows, int64_t row0, int64_t nrows,
     const int64_t* __restrict__ cols, int64_t ncols, T* __restrict__ out, int64_t ld) {
     extern __shared__ float sm[];
-    const int dp = d + 1;
+    constexpr int dp = kBlkFeat + 1;
     float* xr = sm;             // 32 x dp
     float* xc = sm + 32 * dp;   // 32 x dp
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * 32 + tx;
     const int64_t r_base = (int64_t)blockIdx.y * 32;
     const int64_t c_base = (int64_t)blockIdx.x * 32;
-    for (int e = tid; e < 32 * d; e += 256) {
-        const int rr = e / d, kk = e - rr * d;
-        const int64_t r = r_base + rr;
-        const int64_t c = c_base + rr;
-        float vr = 0.f, vc = 0.f;
-        if (r < nrows) vr = Xr[(rows ? rows[r] : row0 + r) * d + kk];
-        if (c < ncols) vc = Xc[(cols ? cols[c] : c) * d + kk];
-        xr[rr * dp + kk] = vr;
-        xc[rr * dp + kk] = vc;
-    }
-    __syncthreads();
     T acc[4] = {0, 0, 0, 0};
-    for (int kk = 0; kk < d; ++kk) {
-        const T c = (T)xc[tx * dp + kk];
+    // features kBlkFeat at a time, summed in increasing order
+    for (int c0 = 0; c0 < d; c0 += kBlkFeat) {
+        const int w = min(kBlkFeat, d - c0);
+        __syncthreads();
+        for (int e = tid; e < 32 * w; e += 256) {
+            const int rr = e / w, kk = e - rr * w;
+            const int64_t r = r_base + rr;
+            const int64_t c = c_base + rr;
+            float vr = 0.f, vc = 0.f;
+            if (r < nrows) vr = Xr[(rows ? rows[r] : row0 + r) * d + c0 + kk];
+            if (c < ncols) vc = Xc[(cols ? cols[c] : c) * d + c0 + kk];
+            xr[rr * dp + kk] = vr;
+            xc[rr * dp + kk] = vc;
+        }
+        __syncthreads();
+        for (int kk = 0; kk < w; ++kk) {
+            const T c = (T)xc[tx * dp + kk];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const T t = (T)xr[(ty + 8 * j) * dp + kk] - c;
-            acc[j] += t * t;
+            for (int j = 0; j < 4; ++j) {
+                const T t = (T)xr[(ty + 8 * j) * dp + kk] - c;
+                acc[j] += t * t;
+            }
         }
     }
     const int64_t c = c_base + tx;
@@ -89,14 +96,14 @@ int launch_kernel_block(kevd_ctx* ctx, const float* X, int64_t N, int d, double 
                         int64_t ncols, int precision, void* out, int64_t ld, cudaStream_t s,
                         const float* Xc) {
     if (!Xc) Xc = X;
-    if (!X || !out || d < 1 || d > 1024 || nrows < 0 || ncols < 0 || ld < ncols)
+    if (!X || !out || d < 1 || d > kMaxFeatures || nrows < 0 || ncols < 0 || ld < ncols)
         return set_error(ctx, KEVD_ERR_ARG, "kernel_block: bad arguments");
     if (!rows && (row0 < 0 || row0 + nrows > N))
         return set_error(ctx, KEVD_ERR_ARG, "kernel_block: row range outside [0, N)");
     if (nrows == 0 || ncols == 0) return KEVD_OK;
     dim3 grid(ceil_div(ncols, 32), ceil_div(nrows, 32));
     if (grid.y > 65535) return set_error(ctx, KEVD_ERR_ARG, "kernel_block: too many rows");
-    size_t smem = 2 * 32 * (size_t)(d + 1) * sizeof(float);
+    size_t smem = 2 * 32 * (size_t)(kBlkFeat + 1) * sizeof(float);
     if (precision == KEVD_FP64) {
         if (smem > 48 * 1024)
             KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&kernel_block_kernel<double>), (int)smem));
