@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--cal-n", type=int, default=200_000, help="states in the calibration measurement (0: skip)")
     ap.add_argument("--c4-datasets", type=int, default=48, help="datasets in the batched phase (0: skip)")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the block-size autotuner (profiling runs)")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the serving window (0: no serving phase)")
     ap.add_argument("--fact-rate", type=float, default=20.0, help="factorization requests per second")
@@ -478,9 +479,9 @@ def main():
     # block size: the autotuner times b in {16, 32, 64} on this data (a 131,072-row
     # prefix to rank 512); --b 0 runs the step with its choice
     from kernel_evd_gb300 import autotune
-    tuned = autotune.tune_block(ctx, Xd, scale, args.k, candidates=(16, 32, 64))
+    tuned = None if args.no_autotune else autotune.tune_block(ctx, Xd, scale, args.k, candidates=(16, 32, 64))
     if args.b == 0:
-        args.b = int(tuned["block"])
+        args.b = int(tuned["block"]) if tuned else 64
     F = torch.empty((N, args.k), dtype=torch.float32, device="cuda")
     U = torch.empty((N, args.kout), dtype=torch.float32, device="cuda")
 
@@ -651,7 +652,7 @@ def main():
                                        f"b={args.b}, top {args.kout}, mixed precision",
                            "eps": eps, "median_sqdist": med, "calibration_rows": n_cal,
                            "block_autotune": {"chosen": int(tuned["block"]),
-                                              "ms_per_column": tuned["ms_per_column"]},
+                                              "ms_per_column": tuned["ms_per_column"]} if tuned else None,
                            "l2": "inputs larger than L2 (X 512 MB, F 16 GB)",
                            "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"},
                 "rank": int(fac.rank), "rounds": int(fac.rounds), "trace_error": fac.trace_error,

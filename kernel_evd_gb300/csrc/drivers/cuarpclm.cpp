@@ -1,0 +1,95 @@
+// Stage 2 driver (the reference's ./cuarpclm, ks_arpclm.cu:566-1152): block
+// RPCholesky of the delay-embedded samples; writes L^{-1} and the pivot set
+// and prints the per-round table.  Compile-time configuration as in the
+// reference; override with -D.
+#include <ctime>
+
+#include "driver_io.h"
+
+#ifndef LFACT
+#define LFACT 22
+#endif
+#ifndef MGRID
+#define MGRID 8
+#endif
+#ifndef NDATA
+#define NDATA 2000
+#endif
+#ifndef NQ
+#define NQ 32
+#endif
+#ifndef BLK
+#define BLK 32
+#endif
+#ifndef NROUNDS
+#define NROUNDS 8
+#endif
+#ifndef BW
+#define BW 0.8
+#endif
+#ifndef PRECISION
+#define PRECISION KEVD_FP64
+#endif
+
+int main() {
+    const time_t t0 = time(nullptr);
+    const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ, Nrounds = NROUNDS;
+    const size_t N = Ndata - Nq + 1, NM = N * M, rmax = Nrounds * BLK;
+    char fname[256], linv_file[256], spiv_file[256];
+    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.bin", Ndata, M, Lfact);
+    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
+    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
+    printf("Data file: %s\nData set: u\n", fname);
+    printf("Block size: %d  Devices: 1  Rows/device: %zu  Cols/device: %zu\n\n", BLK, NM, rmax);
+    std::vector<float> u = read_array<float>(fname, Ndata * M);
+
+    kevd_ctx* ctx = nullptr;
+    if (kevd_ctx_create(0, &ctx) != KEVD_OK) {
+        fprintf(stderr, "no CUDA device\n");
+        return 1;
+    }
+    float *u_dev = nullptr, *X_dev = nullptr;
+    void* F = nullptr;
+    const size_t fsz = (PRECISION == KEVD_FP64) ? sizeof(double) : sizeof(float);
+    DRV_CUDA(cudaMalloc(&u_dev, u.size() * sizeof(float)));
+    DRV_CUDA(cudaMalloc(&X_dev, NM * Nq * sizeof(float)));
+    DRV_CUDA(cudaMalloc(&F, NM * rmax * fsz));
+    DRV_CUDA(cudaMemcpy(u_dev, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice));
+    DRV_KEVD(ctx, kevd_hankel_rows(ctx, u_dev, (int64_t)Ndata, (int64_t)M, (int64_t)Nq, X_dev, nullptr));
+
+    kevd_rpchol_params p = {};
+    p.k_max = (int64_t)rmax;
+    p.block = BLK;
+    p.max_rounds = (int32_t)Nrounds;
+    p.tol = 1e-10;
+    p.seed = 1234;
+    p.precision = PRECISION;
+    std::vector<int64_t> spiv(rmax);
+    std::vector<double> err(Nrounds);
+    std::vector<int32_t> hm(Nrounds);
+    kevd_rpchol_result res = {};
+    DRV_KEVD(ctx, kevd_rpchol(ctx, X_dev, (int64_t)NM, (int32_t)Nq, 1.0 / ((double)Nq * BW), &p, F, (int64_t)rmax,
+                              spiv.data(), err.data(), hm.data(), &res, nullptr));
+    const size_t Nr = (size_t)res.rank;
+    std::vector<double> linv(Nr * Nr);
+    DRV_KEVD(ctx, kevd_linv_from_factor(ctx, F, PRECISION, (int64_t)rmax, spiv.data(), (int64_t)Nr, linv.data(),
+                                        nullptr));
+    write_array(linv_file, linv.data(), linv.size());
+    std::vector<uint64_t> spiv_u(spiv.begin(), spiv.begin() + Nr);
+    write_array(spiv_file, spiv_u.data(), spiv_u.size());
+
+    printf("\nAccepted rank: %zu in %zu rounds\n", Nr, Nrounds);
+    printf("# round accepted cumrank relerr\n");
+    size_t cum = 0;
+    for (size_t i = 0; i < Nrounds; ++i) {
+        const size_t a = i < (size_t)res.rounds ? (size_t)hm[i] : 0;
+        cum += a;
+        printf("%zu %zu %zu %.5e\n", i, a, cum, i < (size_t)res.rounds ? err[i] : err[res.rounds - 1]);
+    }
+    cudaFree(F);
+    cudaFree(X_dev);
+    cudaFree(u_dev);
+    kevd_ctx_destroy(ctx);
+    printf("Total time: %.2f s\n", difftime(time(nullptr), t0));
+    return 0;
+}

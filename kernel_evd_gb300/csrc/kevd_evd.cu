@@ -431,163 +431,182 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j (FP32 products and 8-row FP32
-// partials, round to nearest: their errors are unbiased and average out in H;
-// the partials are added with compensation over the CTA's row range).  thread: columns 4 (tid >> 4)..+4,
-// U columns 2 (tid & 15)..+2.
-__global__ void __launch_bounds__(256)
+// CTA's rows, for a block of 64 columns j.  128 threads, thread (jg, qg) owns
+// columns j = 4 jg..4 jg+3 and q = 4 qg..4 qg+3: per row one 16-byte load of
+// F and one of the weights feed 16 FMAs.  FP32 products and 8-row FP32
+// partials (round to nearest: their errors are unbiased and average out in
+// H); the partials are added with compensation over the CTA's row range.
+__global__ void __launch_bounds__(128)
 evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
               const double* __restrict__ dinv, int64_t rows_per, double* __restrict__ partial) {
-    __shared__ float Fs[64][65];
-    __shared__ __align__(16) float Ws[64][32];
+    constexpr int kP = 68;   // row pitch: 16-byte aligned rows
+    __shared__ __align__(16) float Fs[64][kP];   // [row i][column j]
+    __shared__ __align__(16) float Ws[64][32];   // [row i][q]
     const int tid = threadIdx.x;
-    const int jr = 4 * (tid >> 4), qc = 2 * (tid & 15);
+    const int jg = tid >> 3, qg = tid & 7;
     const int64_t j0 = (int64_t)blockIdx.x * 64;
     const int64_t r0 = (int64_t)blockIdx.y * rows_per;
     const int64_t r1 = min(N, r0 + rows_per);
-    float ks[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-    float kc[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    float ks[4][4], kc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) ks[a][b] = kc[a][b] = 0.f;
     for (int64_t i0 = r0; i0 < r1; i0 += 64) {
         __syncthreads();
-        for (int e = tid; e < 64 * 64; e += 256) {
-            const int jj = e >> 6, ii = e & 63;
+        for (int e = tid; e < 64 * 64; e += 128) {
+            const int jj = e >> 6, ii = e & 63;   // consecutive threads: consecutive rows (coalesced)
             const int64_t j = j0 + jj, i = i0 + ii;
-            Fs[jj][ii] = (j < k && i < r1) ? FT[j * ldT + i] : 0.f;
+            Fs[ii][jj] = (j < k && i < r1) ? FT[j * ldT + i] : 0.f;
         }
-        for (int e = tid; e < 64 * 32; e += 256) {
+        for (int e = tid; e < 64 * 32; e += 128) {
             const int ii = e >> 5, q = e & 31;
             const int64_t i = i0 + ii;
             Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
         }
         __syncthreads();
-        // 8-row FP32 partials (fma chains), each added with compensation
 #pragma unroll 1
         for (int i8 = 0; i8 < 64; i8 += 8) {
-            float p[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+            float p[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) p[a][b] = 0.f;
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                const float w0 = Ws[i8 + u][qc], w1 = Ws[i8 + u][qc + 1];
+                const float4 f = *reinterpret_cast<const float4*>(&Fs[i8 + u][4 * jg]);
+                const float4 w = *reinterpret_cast<const float4*>(&Ws[i8 + u][4 * qg]);
+                const float fv[4] = {f.x, f.y, f.z, f.w}, wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const float f = Fs[jr + a][i8 + u];
-                    p[a][0] = fmaf(f, w0, p[a][0]);
-                    p[a][1] = fmaf(f, w1, p[a][1]);
-                }
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) p[a][b] = fmaf(fv[a], wv[b], p[a][b]);
             }
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                kahan_add(ks[a][0], kc[a][0], p[a][0]);
-                kahan_add(ks[a][1], kc[a][1], p[a][1]);
-            }
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) kahan_add(ks[a][b], kc[a][b], p[a][b]);
         }
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        const int64_t j = j0 + jr + a;
+        const int64_t j = j0 + 4 * jg + a;
         if (j >= k) continue;
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int q = qc + b;
+        for (int b = 0; b < 4; ++b) {
+            const int q = 4 * qg + b;
             if (q < m) partial[((int64_t)blockIdx.y * k + j) * m + q] = (double)ks[a][b] - (double)kc[a][b];
         }
     }
 }
 
-// Rayleigh-Ritz H and M partials over 256-row tiles: w_i = F_i (T1h + T1l)
+// Rayleigh-Ritz H and M partials over 64-row tiles: w_i = F_i (T1h + T1l)
 // (T1 as an FP32 hi/lo pair, k x 32), H += (w/sqrt(q))(w/sqrt(q))^T, M += u u^T.
-__global__ void __launch_bounds__(256, 1)
+// 128 threads; for w thread (ig, qg) owns rows 4 ig..4 ig+3 and columns
+// 4 qg..4 qg+3 (16-byte loads of F and of the T1 rows from shared memory, 8-term
+// FP32 partials added with compensation); for H and M thread t owns entries
+// t + 128 r of the 32 x 32 matrices, summed over the tile with compensation and
+// across tiles in FP64.
+constexpr int kHmRows = 64;
+__global__ void __launch_bounds__(128)
 evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ T1hl,
               int m, const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
-    __shared__ __align__(16) float Ts[2][32][32];   // hi, lo for a 32-row chunk of T1
-    __shared__ float Ws[256][33];
+    __shared__ __align__(16) float Fs[32][kHmRows];   // [column j of the chunk][row i]
+    __shared__ __align__(16) float Ts[2][32][32];     // hi, lo of a 32-column chunk of T1
+    __shared__ float Ws[kHmRows][33];
     const int tid = threadIdx.x;
-    double h64[4] = {0, 0, 0, 0}, m64[4] = {0, 0, 0, 0};
-    const int64_t n_tiles = (N + 255) / 256;
-    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const int64_t i = t * 256 + tid;
-        float w[32], wc[32];
+    const int ig = tid >> 3, qg = tid & 7;
+    double h64[8], m64[8];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) w[q] = wc[q] = 0.f;
+    for (int r = 0; r < 8; ++r) h64[r] = m64[r] = 0.0;
+    const int64_t n_tiles = (N + kHmRows - 1) / kHmRows;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const int64_t i0 = t * kHmRows;
+        float ws[4][4], wc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) ws[a][b] = wc[a][b] = 0.f;
         for (int64_t j0 = 0; j0 < k; j0 += 32) {
             __syncthreads();
-            for (int e = tid; e < 32 * 32; e += 256) {
+            for (int e = tid; e < 32 * kHmRows; e += 128) {
+                const int jj = e / kHmRows, ii = e - jj * kHmRows;   // coalesced along rows
+                const int64_t j = j0 + jj, i = i0 + ii;
+                Fs[jj][ii] = (j < k && i < N) ? FT[j * ldT + i] : 0.f;
+            }
+            for (int e = tid; e < 32 * 32; e += 128) {
                 const int jj = e >> 5, q = e & 31;
                 const int64_t j = j0 + jj;
                 Ts[0][jj][q] = (j < k) ? T1hl[(2 * j) * 32 + q] : 0.f;
                 Ts[1][jj][q] = (j < k) ? T1hl[(2 * j + 1) * 32 + q] : 0.f;
             }
             __syncthreads();
-            if (i < N) {
-                // 4 rows x (hi, lo) products per column in FP32, then one compensated
-                // add of that 8-term sum
-                const int jn = (int)min((int64_t)32, k - j0);
-                float fn[4];   // the next 4-row group, loaded one step ahead
+#pragma unroll 1
+            for (int j8 = 0; j8 < 32; j8 += 8) {
+                float p[4][4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) fn[u] = (u < jn) ? FT[(j0 + u) * ldT + i] : 0.f;
-                for (int jj = 0; jj < jn; jj += 4) {
-                    float part[32];
+                for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int q = 0; q < 32; ++q) part[q] = 0.f;
-                    float f[4];
+                    for (int b = 0; b < 4; ++b) p[a][b] = 0.f;
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        f[u] = fn[u];
-                        fn[u] = (jj + 4 + u < jn) ? FT[(j0 + jj + 4 + u) * ldT + i] : 0.f;
-                    }
+                for (int u = 0; u < 8; ++u) {
+                    const float4 f = *reinterpret_cast<const float4*>(&Fs[j8 + u][4 * ig]);
+                    const float4 th = *reinterpret_cast<const float4*>(&Ts[0][j8 + u][4 * qg]);
+                    const float4 tl = *reinterpret_cast<const float4*>(&Ts[1][j8 + u][4 * qg]);
+                    const float fv[4] = {f.x, f.y, f.z, f.w};
+                    const float hv[4] = {th.x, th.y, th.z, th.w}, lv[4] = {tl.x, tl.y, tl.z, tl.w};
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float4* th = reinterpret_cast<const float4*>(Ts[0][jj + u]);
-                        const float4* tl = reinterpret_cast<const float4*>(Ts[1][jj + u]);
+                    for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int q4 = 0; q4 < 8; ++q4) {
-                            const float4 a = th[q4], b = tl[q4];
-                            part[4 * q4 + 0] = fmaf(f[u], a.x, fmaf(f[u], b.x, part[4 * q4 + 0]));
-                            part[4 * q4 + 1] = fmaf(f[u], a.y, fmaf(f[u], b.y, part[4 * q4 + 1]));
-                            part[4 * q4 + 2] = fmaf(f[u], a.z, fmaf(f[u], b.z, part[4 * q4 + 2]));
-                            part[4 * q4 + 3] = fmaf(f[u], a.w, fmaf(f[u], b.w, part[4 * q4 + 3]));
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < 32; ++q) kahan_add(w[q], wc[q], part[q]);
+                        for (int b = 0; b < 4; ++b) p[a][b] = fmaf(fv[a], hv[b], fmaf(fv[a], lv[b], p[a][b]));
                 }
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) kahan_add(ws[a][b], wc[a][b], p[a][b]);
             }
         }
         __syncthreads();
-        const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
 #pragma unroll
-        for (int q = 0; q < 32; ++q) Ws[tid][q] = (q < m) ? (w[q] - wc[q]) * sq : 0.f;
+        for (int a = 0; a < 4; ++a) {
+            const int64_t i = i0 + 4 * ig + a;
+            const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int q = 4 * qg + b;
+                Ws[4 * ig + a][q] = (q < m) ? (ws[a][b] - wc[a][b]) * sq : 0.f;
+            }
+        }
         __syncthreads();
 #pragma unroll
-        for (int qq = 0; qq < 4; ++qq) {
-            const int e = tid + 256 * qq;
+        for (int r = 0; r < 8; ++r) {
+            const int e = tid + 128 * r;
             const int ja = e >> 5, jb = e & 31;
             float hs = 0.f, hc = 0.f;
-            for (int rr = 0; rr < 256; ++rr) kahan_add(hs, hc, Ws[rr][ja] * Ws[rr][jb]);
-            h64[qq] += (double)hs - (double)hc;
+            for (int rr = 0; rr < kHmRows; ++rr) kahan_add(hs, hc, Ws[rr][ja] * Ws[rr][jb]);
+            h64[r] += (double)hs - (double)hc;
         }
         __syncthreads();
-        {
-            float uu[32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) uu[q] = (i < N && q < m) ? U[i * m + q] : 0.f;
-#pragma unroll
-            for (int q = 0; q < 32; ++q) Ws[tid][q] = uu[q];
+        for (int e = tid; e < kHmRows * 32; e += 128) {
+            const int rr = e >> 5, q = e & 31;
+            const int64_t i = i0 + rr;
+            Ws[rr][q] = (i < N && q < m) ? U[i * m + q] : 0.f;
         }
         __syncthreads();
 #pragma unroll
-        for (int qq = 0; qq < 4; ++qq) {
-            const int e = tid + 256 * qq;
+        for (int r = 0; r < 8; ++r) {
+            const int e = tid + 128 * r;
             const int ja = e >> 5, jb = e & 31;
             float ms = 0.f, mc = 0.f;
-            for (int rr = 0; rr < 256; ++rr) kahan_add(ms, mc, Ws[rr][ja] * Ws[rr][jb]);
-            m64[qq] += (double)ms - (double)mc;
+            for (int rr = 0; rr < kHmRows; ++rr) kahan_add(ms, mc, Ws[rr][ja] * Ws[rr][jb]);
+            m64[r] += (double)ms - (double)mc;
         }
     }
     double* out = partial + (int64_t)blockIdx.x * 2048;
 #pragma unroll
-    for (int qq = 0; qq < 4; ++qq) {
-        out[tid + 256 * qq] = h64[qq];
-        out[1024 + tid + 256 * qq] = m64[qq];
+    for (int r = 0; r < 8; ++r) {
+        out[tid + 128 * r] = h64[r];
+        out[1024 + tid + 128 * r] = m64[r];
     }
 }
 
@@ -652,19 +671,19 @@ static int rayleigh_ritz(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N,
     double* tpart = arena_get<double>(ctx, "rr.tpart", (size_t)ny * k * m, &st);
     double* T1 = arena_get<double>(ctx, "rr.T1", (size_t)k * m, &st);
     float* T1hl = arena_get<float>(ctx, "rr.T1hl", (size_t)k * 64, &st);
-    const int nhm = ctx->num_sms * 2;
+    const int nhm = ctx->num_sms * 4;
     double* hmpart = arena_get<double>(ctx, "rr.hmpart", (size_t)nhm * 2048, &st);
     double* HM = arena_get<double>(ctx, "rr.HM", 2048, &st);
     double* w = arena_get<double>(ctx, "rr.w", 64, &st);
     int* info = arena_get<int>(ctx, "rr.info", 1, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
-    evt_t1_kernel<<<dim3(ceil_div(k, 64), ny), 256, 0, s>>>(FT, ldT, N, k, U, m, dinv, rows_per, tpart);
+    evt_t1_kernel<<<dim3(ceil_div(k, 64), ny), 128, 0, s>>>(FT, ldT, N, k, U, m, dinv, rows_per, tpart);
     KEVD_LAUNCH(ctx);
     rr_sum_kernel<<<ceil_div(k * m, 256), 256, 0, s>>>(tpart, ny, k * m, T1);
     KEVD_LAUNCH(ctx);
     evt_split_t1_kernel<<<ceil_div(k * 32, 256), 256, 0, s>>>(T1, k, m, T1hl);
     KEVD_LAUNCH(ctx);
-    evt_hm_kernel<<<nhm, 256, 0, s>>>(FT, ldT, N, k, T1hl, m, U, qinv, hmpart);
+    evt_hm_kernel<<<nhm, 128, 0, s>>>(FT, ldT, N, k, T1hl, m, U, qinv, hmpart);
     KEVD_LAUNCH(ctx);
     rr_sum_kernel<<<8, 256, 0, s>>>(hmpart, nhm, 2048, HM);
     KEVD_LAUNCH(ctx);

@@ -1,0 +1,75 @@
+"""The three stage drivers (kernel_evd_gb300/bin: cuband, cuarpclm, cukevd) run
+as the reference's programs do: no arguments, compile-time configuration,
+files under ./data (raw arrays in place of HDF5 datasets), bw0.out and the
+round table on stdout.  Their outputs are checked against the FP64 oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import calibrate, evd, kernel, ks, rpchol
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(ROOT, "kernel_evd_gb300", "bin")
+M, NQ, LFACT, BLK, NROUNDS, BW = 8, 32, 22, 32, 8, 0.8
+
+
+def _write_u(d, ndata):
+    S = ks.seeded_mode(ndata, M=64, seed=3, warm_time=60.0)       # ndata times x 64 gridpoints
+    u = np.ascontiguousarray(S[:, :M].T).astype(np.float32)         # M gridpoints, time fastest
+    u.ravel().tofile(os.path.join(d, "data", f"ks_true_{ndata}_{M}_{LFACT}_u32.bin"))
+    return u.ravel()
+
+
+def _run(d, prog):
+    exe = os.path.join(BIN, prog)
+    if not os.path.exists(exe):
+        pytest.skip(f"{prog} not built")
+    r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+def test_cuband_selects_the_oracle_bandwidth(tmp_path):
+    d = str(tmp_path)
+    os.makedirs(os.path.join(d, "data"))
+    u = _write_u(d, 600)
+    out = _run(d, "cuband")
+    assert "Total time:" in out
+    lines = open(os.path.join(d, "bw0.out")).read().split("\n")
+    eopt = float(lines[-3])
+    X = kernel.hankel_rows(u, 600, M, NQ).astype(np.float64)
+    bw = calibrate.reference_sweep().astype(np.float64)
+    T = calibrate.pair_sums(X, 1.0 / (NQ * bw))
+    logS, slope, idmax, eopt_ref, mdim = calibrate.select(bw, T, X.shape[0])
+    assert eopt == pytest.approx(eopt_ref, rel=1e-5)
+    got = np.array([[float(v) for v in l.split()] for l in lines[:len(bw) - 2]])
+    np.testing.assert_allclose(got[:, 1], logS[1:-1], rtol=1e-4, atol=1e-6)
+
+
+def test_cuarpclm_then_cukevd_match_the_oracle(tmp_path):
+    d = str(tmp_path)
+    os.makedirs(os.path.join(d, "data"))
+    ndata = 2000
+    u = _write_u(d, ndata)
+    out = _run(d, "cuarpclm")
+    assert "# round accepted cumrank relerr" in out
+    N = ndata - NQ + 1
+    spiv = np.fromfile(os.path.join(d, "data", f"spiv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.bin"), dtype=np.uint64)
+    linv = np.fromfile(os.path.join(d, "data", f"linv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.bin"), dtype=np.float64)
+    X = kernel.hankel_rows(u, ndata, M, NQ).astype(np.float64)
+    scale = 1.0 / (NQ * BW)
+    ref = rpchol.rpcholesky(X, scale, BLK * NROUNDS, BLK, seed=1234, n_rounds=NROUNDS)
+    np.testing.assert_array_equal(spiv.astype(np.int64), ref["piv"])
+    r = spiv.size
+    Li = rpchol.linv_from_F(ref["F"], ref["piv"])
+    np.testing.assert_allclose(linv.reshape(r, r, order="F"), Li, rtol=0, atol=1e-8 * np.abs(Li).max())
+    out = _run(d, "cukevd")
+    lam = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_lam.bin"), dtype=np.float64)
+    U = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_U.bin"), dtype=np.float32)
+    e = evd.evd_from_factor(ref["F"], 16)
+    np.testing.assert_allclose(lam[-16:], e["lam"][-16:], rtol=0, atol=1e-9)
+    assert U.size == X.shape[0] * 16
