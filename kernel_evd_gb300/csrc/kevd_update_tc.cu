@@ -378,8 +378,8 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
                     const RoundView* st, float* __restrict__ Kc) {
     if (st->done || st->nacc == 0) return;
     const int nacc = st->nacc;
-    extern __shared__ float ksm[];
-    constexpr int dp = kFeatChunk + 1;
+    extern __shared__ __align__(16) float ksm[];
+    constexpr int dp = kFeatChunk + 4;   // 16-byte aligned rows
     float* xr = ksm;                 // 128 x dp
     float* xq = ksm + kRows * dp;    // 64 x dp
     const int64_t row0 = (int64_t)blockIdx.x * kRows;
@@ -393,27 +393,37 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
     for (int c0 = 0; c0 < d; c0 += kFeatChunk) {
         const int w = min(kFeatChunk, d - c0);
         __syncthreads();
-        for (int e = threadIdx.x; e < kRows * w; e += 256) {
-            const int rr = e / w, kk = e - rr * w;
+        const int w4 = (w + 3) & ~3;   // staged width, zero-padded to a multiple of 4
+        for (int e = threadIdx.x; e < kRows * w4; e += 256) {
+            const int rr = e / w4, kk = e - rr * w4;
             const int64_t i = row0 + rr;
-            xr[rr * dp + kk] = (i < N) ? X[i * d + c0 + kk] : 0.f;
+            xr[rr * dp + kk] = (i < N && kk < w) ? X[i * d + c0 + kk] : 0.f;
         }
-        for (int e = threadIdx.x; e < kCols * w; e += 256) {
-            const int q = e / w, kk = e - q * w;
-            xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + c0 + kk] : 0.f;
+        for (int e = threadIdx.x; e < kCols * w4; e += 256) {
+            const int q = e / w4, kk = e - q * w4;
+            xq[q * dp + kk] = (q < nacc && kk < w) ? X[sacc[q] * d + c0 + kk] : 0.f;
         }
         __syncthreads();
-        for (int kk = 0; kk < w; ++kk) {
-            float vr[8], vq[4];
+        // four features per 16-byte load; padded features are zero in both
+        // operands and add nothing (0 - 0 squared), so the sum and its order
+        // over the real features are unchanged
+        for (int k4 = 0; k4 < w4; k4 += 4) {
+            float4 vr[8], vq[4];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
+            for (int a = 0; a < 8; ++a) vr[a] = *reinterpret_cast<const float4*>(xr + (ty + 16 * a) * dp + k4);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
+            for (int c = 0; c < 4; ++c) vq[c] = *reinterpret_cast<const float4*>(xq + (tx + 16 * c) * dp + k4);
 #pragma unroll
             for (int a = 0; a < 8; ++a)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const float t = vr[a] - vq[c];
+                    float t = vr[a].x - vq[c].x;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].y - vq[c].y;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].z - vq[c].z;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].w - vq[c].w;
                     acc[a][c] = fmaf(t, t, acc[a][c]);
                 }
         }
@@ -535,7 +545,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     }
     {
         ProfScope ps(ctx, "rp_update_kcols", s);
-        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 1) * sizeof(float);
+        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 4) * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
         update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
         KEVD_LAUNCH(ctx);
