@@ -385,58 +385,49 @@ evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     if (!(acc > 0.0)) atomicOr(bad, 1);
 }
 
-// U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32).
-// CTA = 64 rows x 32 columns, 128 threads; thread (ig, qg) owns rows
-// 4 ig..4 ig+3 and columns 4 qg..4 qg+3: per j one 16-byte load of F and one
-// of Z feed 16 FMAs (FP32, j in increasing order).
-__global__ void __launch_bounds__(128)
+// U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32)
+__global__ void __launch_bounds__(256)
 evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ Z, int m,
              const double* __restrict__ dinv, float* __restrict__ U) {
-    __shared__ __align__(16) float Fs[32][64];   // [column j of the chunk][row i]
-    __shared__ __align__(16) float Zs[32][32];   // [column j of the chunk][q]
-    const int tid = threadIdx.x;
-    const int ig = tid >> 3, qg = tid & 7;
-    const int64_t i0 = (int64_t)blockIdx.x * 64;
-    float acc[4][4];
+    __shared__ __align__(16) float Zs[128][32];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float acc[32];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-    for (int64_t j0 = 0; j0 < k; j0 += 32) {
+    for (int q = 0; q < 32; ++q) acc[q] = 0.f;
+    for (int64_t j0 = 0; j0 < k; j0 += 128) {
         __syncthreads();
-        for (int e = tid; e < 32 * 64; e += 128) {
-            const int jj = e >> 6, ii = e & 63;   // coalesced along rows
-            const int64_t j = j0 + jj, i = i0 + ii;
-            Fs[jj][ii] = (j < k && i < N) ? FT[j * ldT + i] : 0.f;
-        }
-        for (int e = tid; e < 32 * 32; e += 128) {
+        for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
             const int jj = e >> 5, q = e & 31;
             const int64_t j = j0 + jj;
             Zs[jj][q] = (j < k && q < m) ? (float)Z[(int64_t)q * k + j] : 0.f;
         }
         __syncthreads();
-#pragma unroll 8
-        for (int jj = 0; jj < 32; ++jj) {
-            const float4 f = *reinterpret_cast<const float4*>(&Fs[jj][4 * ig]);
-            const float4 z = *reinterpret_cast<const float4*>(&Zs[jj][4 * qg]);
-            const float fv[4] = {f.x, f.y, f.z, f.w}, zv[4] = {z.x, z.y, z.z, z.w};
+        if (i < N) {
+            const int jn = (int)min((int64_t)128, k - j0);
+            for (int jj = 0; jj < jn; jj += 4) {
+                float f[4];
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+                for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
 #pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(fv[a], zv[b], acc[a][b]);
+                for (int u = 0; u < 4; ++u) {
+                    const float4* zr = reinterpret_cast<const float4*>(Zs[jj + u]);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                        const float4 z = zr[q4];
+                        acc[4 * q4 + 0] = fmaf(f[u], z.x, acc[4 * q4 + 0]);
+                        acc[4 * q4 + 1] = fmaf(f[u], z.y, acc[4 * q4 + 1]);
+                        acc[4 * q4 + 2] = fmaf(f[u], z.z, acc[4 * q4 + 2]);
+                        acc[4 * q4 + 3] = fmaf(f[u], z.w, acc[4 * q4 + 3]);
+                    }
+                }
+            }
         }
     }
+    if (i >= N) return;
+    const double di = dinv[i];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int64_t i = i0 + 4 * ig + a;
-        if (i >= N) continue;
-        const double di = dinv[i];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int q = 4 * qg + b;
-            if (q < m) U[i * m + q] = (float)((double)acc[a][b] * di);
-        }
-    }
+    for (int q = 0; q < 32; ++q)
+        if (q < m) U[i * m + q] = (float)((double)acc[q] * di);
 }
 
 // Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
@@ -1019,7 +1010,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     {
         ProfScope ps(ctx, "ev_u", s);
         if (sizeof(T) == 4 && k_out <= 32)
-            evt_u_kernel<<<ceil_div(N, 64), 128, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U);
+            evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U);
         else
             ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
         KEVD_LAUNCH(ctx);

@@ -1,31 +1,41 @@
 // Weighted Gram G = Y^T Y, Y = diag(s) F, of an FP32 factor on the tcgen05
 // tensor cores (the A and B Grams of the bistochastic EVD).
 //
-// Precision: 3xTF32.  Each element y is split as hi = rn_tf32(y) and
-// lo = rn_tf32(y - hi) (both exact tf32 values, so every product is exact in
-// FP32 and the split error is unbiased, about 2^-23 |y|); a 128 x 128 output
+// Precision: 3xTF32 with the weights on one side, G = (diag(s^2) F)^T F.
+// The tensor core reads an FP32 operand as tf32 by dropping its low 13
+// mantissa bits, so an element v is used as hi = trunc_tf32(v) when passed
+// as it is, and lo = v - hi is exact in FP32 (its own read drops at most
+// 2^-21 |v|).  The a operand is y = s_i^2 F[i][a] (hi: y itself, lo: y -
+// trunc(y), both in Tensor Memory); the b operand is the raw F tile (hi: the
+// TMA tile as loaded, lo: F - trunc(F) in the b-lo tile).  A 128 x 128 output
 // tile accumulates hi_a lo_b^T + lo_a hi_b^T + hi_a hi_b^T in FP32 in Tensor
-// Memory (the dropped lo_a lo_b^T is about 2^-24 relative and of random sign).  The tensor-core accumulator rounds each update
-// with a one-sided bias, so the FP32 partial is kept short: every 1024 rows it
-// is added into an FP64 tile in global memory and the long sum over N rows is
-// FP64 (the Gram accumulators of the reference are FP64,
-// ks_kevd.cu:1152-1158).  The relative error of a Gram entry is about 1e-5;
-// eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
+// Memory; the dropped parts (lo_a lo_b, the truncation of the lo reads) are
+// below 2^-20 of each product and shrink its magnitude by about 5e-7 on
+// average.  The tensor-core accumulator rounds each update with a one-sided
+// bias, so the FP32 partial is kept short: every 1024 rows it is added into
+// an FP64 tile in global memory and the long sum over N rows is FP64 (the
+// Gram accumulators of the reference are FP64, ks_kevd.cu:1152-1158).  The
+// relative error of a Gram entry is about 1e-5; eigenvalues are then refined
+// in FP64 by Rayleigh-Ritz (kevd_evd.cu).
 //
 // CTA roles (448 threads):
 //   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
 //               lanes 32q..32q+31 = tile rows)
 //   warps 4-7   a converters: thread m owns row m of the a tile (factor column
-//               a0+m, 32 rows of F): row scaling and the tf32 split, written to
-//               the stage's Tensor Memory a-slot (tcgen05.st, hi and lo columns)
+//               a0+m, 32 rows of F): row weights and the hi/lo split, written
+//               to the stage's Tensor Memory a-slot (tcgen05.st, hi and lo
+//               columns)
 //   warp 8      TMA producer
 //   warp 9      TMEM allocation and the single MMA-issuing thread (A from
 //               Tensor Memory, B from shared memory)
-//   warps 10-13 b converters: row m of the b tile, split in shared memory (hi
-//               in place, lo in the b-lo tile)
-// The conversion is the per-stage critical path (measured: with one group of
-// four warps doing both operands the MMA waited on it half the time), hence
-// two groups of four, one warp per SM sub-partition each.
+//   warps 10-13 b converters: row m of the b tile, its lo part into the b-lo
+//               tile (the raw tile is the hi operand)
+// The conversion and the MMA issue are the per-stage critical paths: two
+// groups of four converter warps (one per SM sub-partition each), and the
+// MMA thread issues a stage's 12 MMAs back to back from precomputed
+// descriptors (measured on GB300: a kind::tf32 MMA of 128 x 128 x 8 takes 64
+// cycles when issued back to back, 128 x 64 x 8 takes 48, and each dependent
+// instruction between two MMAs adds its latency).
 // A 4-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
 // double-buffered TMEM accumulator (2 x 128 columns) are handed over with
 // mbarriers; every wait is bounded and sets an error flag on timeout.
@@ -66,6 +76,7 @@ static_assert(kTmemA + kStages * kTmemASlot <= kTmemCols, "Tensor Memory holds 5
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
+    alignas(16) float w2[kStages][32];   // squared row weights of each stage (bulk copy with the tiles)
     uint64_t tma[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -87,14 +98,14 @@ __device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
 }
 
 // Per stage (32 rows of F = 32 columns of FT):
-//   [a 16 KB][b hi 16 KB][b lo 16 KB]
+//   [a 16 KB][b 16 KB][b lo 16 KB]
 // The TMA writes the raw FT boxes (128 factor columns x 32 rows, K-major,
-// SWIZZLE_128B) into the a and b tiles.  With y = s_i * F[i][c], the converters
-// write rn_tf32(y) and rn_tf32(y - hi) of the a tile into the stage's Tensor
-// Memory a-slot, and overwrite the b tile in place with its hi part, its lo part
-// going to the b-lo tile (on a diagonal tile b = a: the a tile itself becomes b
-// hi).  Element (m, k) of a tile sits at sw128_off(m, k), so a 16-byte chunk
-// holds 4 consecutive rows k of one column m.
+// SWIZZLE_128B) into the a and b tiles.  With y = s_i^2 F[i][c], the a
+// converters write y and y - trunc(y) into the stage's Tensor Memory a-slot;
+// the b converters write F - trunc(F) of the b tile into the b-lo tile and
+// leave the b tile as it is (on a diagonal tile b = a: the a converters also
+// write the b-lo tile).  Element (m, k) of a tile sits at sw128_off(m, k), so a
+// 16-byte chunk holds 4 consecutive rows k of one column m.
 constexpr int kStageAlloc = kStageBytes;   // a multiple of 1024: every stage stays 1024-aligned
 
 // Row m of a K-major SW128 tile: its 8 16-byte chunks (K = 4c .. 4c+3).
@@ -116,22 +127,8 @@ __device__ __forceinline__ void store_row(uint8_t* tile, int m, const float (&x)
             make_float4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
 }
 
-// y = w * x (zero for factor columns >= k), hi = rn_tf32(y), lo = rn_tf32(y - hi)
-__device__ __forceinline__ void scale_split(float (&y)[32], float (&h)[32], const float (&w)[32], bool colok) {
-#pragma unroll
-    for (int u = 0; u < 32; ++u) {
-        y[u] = colok ? y[u] * w[u] : 0.f;
-        h[u] = tc::tf32_rn(y[u]);
-    }
-}
-
-__device__ __forceinline__ void lo_part(const float (&y)[32], float (&h)[32]) {
-#pragma unroll
-    for (int u = 0; u < 32; ++u) h[u] = tc::tf32_rn(y[u] - h[u]);
-}
-
 __global__ void __launch_bounds__(kThreads, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict__ srow, int64_t N, int64_t k,
+gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict__ w2, int64_t N, int64_t k,
                int n_tiles, int64_t rows_per, double* __restrict__ partial, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -190,7 +187,8 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                     tc::tma_prefetch_2d(&tmF, xp, (int)a0);
                     if (!diag) tc::tma_prefetch_2d(&tmF, xp, (int)b0);
                 }
-                tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
+                tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes + kTK * 4);
+                tc::bulk_load(bar->w2[slot], w2 + x, kTK * 4, &bar->tma[slot]);
                 tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
                 if (!diag) tc::tma_load_2d(st + kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
             }
@@ -198,56 +196,71 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
         __syncwarp();
     } else if ((warp >= kCvtWarp0 && warp < kCvtWarp0 + 4) || warp >= kCvtBWarp0) {
         // ---------------- converters: thread m owns row m of the a tile (warps
-        // 4-7, to Tensor Memory) or of the b tile (warps 10-13, in place)
+        // 4-7, to Tensor Memory) or of the b tile (warps 10-13, lo part only)
         const bool grp_a = warp < kProdWarp;
         const int m = 32 * (warp & 3) + lane;
         const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);   // this warp's TMEM lanes
-        const bool aok = (a0 + m) < k, bok = (b0 + m) < k;
-        // row weights one stage ahead of their use
-        float sv_next = (r0 + lane < r1) ? (float)__ldg(srow + r0 + lane) : 0.f;
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
-            const float sv = sv_next;
-            const int64_t inext = r0 + (s + 1) * kTK + lane;
-            sv_next = (inext < r1) ? (float)__ldg(srow + inext) : 0.f;
-            float w[32];
-#pragma unroll
-            for (int u = 0; u < 32; ++u) w[u] = __shfl_sync(0xffffffffu, sv, u);
+            float x[32], l[32];
             if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
                 atomicExch(err, 5);
                 break;
             }
             uint8_t* st = base + (size_t)slot * kStageAlloc;
-            float y[32], h[32];
             if (grp_a) {
-                // a operand -> Tensor Memory (on a diagonal tile also b, in place)
+                // a operand -> Tensor Memory: y = s^2 x as the hi operand (the
+                // tensor core reads its top 19 bits) and y - trunc(y) as lo; on a
+                // diagonal tile the raw a tile is also b, whose lo part goes to
+                // the b-lo tile
                 const uint32_t ta = tlane + kTmemA + (uint32_t)slot * kTmemASlot;
-                load_row(st, m, y);
-                scale_split(y, h, w, aok);
-                tc::tmem_st32(ta, h);
-                if (diag) store_row(st, m, h);
-                lo_part(y, h);
-                tc::tmem_st32(ta + 32, h);
-                if (diag) store_row(st + 2 * kOpBytes, m, h);   // b = a: lo in the b-lo tile
+                load_row(st, m, x);
+                float y[32];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot])[c];
+                    y[4 * c + 0] = x[4 * c + 0] * wv.x;
+                    y[4 * c + 1] = x[4 * c + 1] * wv.y;
+                    y[4 * c + 2] = x[4 * c + 2] * wv.z;
+                    y[4 * c + 3] = x[4 * c + 3] * wv.w;
+                }
+#pragma unroll
+                for (int u = 0; u < 32; ++u) l[u] = y[u] - tc::tf32_trunc(y[u]);
+                tc::tmem_st32(ta, y);
+                tc::tmem_st32(ta + 32, l);
+                if (diag) {
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
+                    store_row(st + 2 * kOpBytes, m, l);
+                }
                 tc::tmem_wait_st();
                 tc::tc_fence_before();
             } else if (!diag) {
-                uint8_t* bt = st + kOpBytes;
-                load_row(bt, m, y);
-                scale_split(y, h, w, bok);
-                store_row(bt, m, h);
-                lo_part(y, h);
-                store_row(st + 2 * kOpBytes, m, h);
+                load_row(st + kOpBytes, m, x);
+#pragma unroll
+                for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
+                store_row(st + 2 * kOpBytes, m, l);
             }
             tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }
     } else if (warp == kMmaWarp) {
-        // ---------------- MMA issuer
+        // ---------------- MMA issuer.  The tensor core takes an MMA only when
+        // the previous one is nearly done, so every address of a stage is in a
+        // register before its 12 MMAs are issued back to back.
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_tf32(kTT, kTT);
+            // low descriptor words of each slot's b-hi (raw b, or raw a on a
+            // diagonal tile) and b-lo tiles; the high word is a constant
+            uint32_t bh0[kStages], bl0[kStages];
+#pragma unroll
+            for (int sl = 0; sl < kStages; ++sl) {
+                uint8_t* stg = base + (size_t)sl * kStageAlloc;
+                bh0[sl] = tc::desc_lo_sw128(tc::smem_u32(diag ? stg : stg + kOpBytes));
+                bl0[sl] = tc::desc_lo_sw128(tc::smem_u32(stg + 2 * kOpBytes));
+            }
             bool ok = true;
             for (int64_t c = 0; c < n_chunks && ok; ++c) {
                 const int tb_ = (int)(c & 1);
@@ -258,30 +271,36 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
                 }
                 tc::tc_fence_after();
                 const uint32_t d = tbase + (uint32_t)(tb_ * kTT);
-                const int64_t s0 = c * kFlushStages;
+                const int64_t s0 = c * kFlushStages;   // a multiple of kStages: slot = s - s0 (mod kStages)
                 const int64_t s1 = min(n_stages, s0 + kFlushStages);
-                for (int64_t s = s0; s < s1; ++s) {
-                    const int slot = (int)(s % kStages);
-                    const uint32_t use = (uint32_t)(s / kStages);
-                    if (!tc::mbar_wait(&bar->full[slot], use & 1u, kTimeoutNs)) {
-                        ok = false;
-                        break;
-                    }
-                    tc::tc_fence_after();
-                    uint8_t* st = base + (size_t)slot * kStageAlloc;
-                    const uint32_t ahi = tbase + kTmemA + (uint32_t)slot * kTmemASlot, alo = ahi + 32;
-                    const uint32_t bhi = diag ? tc::smem_u32(st) : tc::smem_u32(st + kOpBytes);
-                    const uint32_t blo = tc::smem_u32(st + 2 * kOpBytes);
+                for (int64_t sb = s0; sb < s1 && ok; sb += kStages) {
+                    const uint32_t use = (uint32_t)(sb / kStages);
 #pragma unroll
-                    for (int j = 0; j < kTK / 8; ++j) {
-                        const uint32_t koff = (uint32_t)(j * 32);   // 8 tf32 = 32 bytes = 8 TMEM columns
-                        const uint64_t dbh = tc::desc_kmajor_sw128(bhi + koff);
-                        const uint64_t dbl = tc::desc_kmajor_sw128(blo + koff);
-                        tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbl, idesc, (s > s0 || j > 0) ? 1u : 0u);
-                        tc::mma_tf32_tmem_a(d, alo + 8 * j, dbh, idesc, 1u);
-                        tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbh, idesc, 1u);
+                    for (int sl = 0; sl < kStages; ++sl) {
+                        if (sb + sl >= s1) break;
+                        if (!tc::mbar_wait(&bar->full[sl], use & 1u, kTimeoutNs)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * kTmemASlot, alo = ahi + 32;
+                        uint64_t dbh[kTK / 8], dbl[kTK / 8];
+#pragma unroll
+                        for (int j = 0; j < kTK / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
+                            dbh[j] = tc::desc_sw128_from_lo(bh0[sl] + 2u * j);
+                            dbl[j] = tc::desc_sw128_from_lo(bl0[sl] + 2u * j);
+                            tc::reg_pin(dbh[j]);
+                            tc::reg_pin(dbl[j]);
+                        }
+                        const uint32_t acc0 = (sb + sl > s0) ? 1u : 0u;
+#pragma unroll
+                        for (int j = 0; j < kTK / 8; ++j) {
+                            tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbl[j], idesc, j > 0 ? 1u : acc0);
+                            tc::mma_tf32_tmem_a(d, alo + 8 * j, dbh[j], idesc, 1u);
+                            tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbh[j], idesc, 1u);
+                        }
+                        tc::mma_commit(&bar->empty[sl]);
                     }
-                    tc::mma_commit(&bar->empty[slot]);
                 }
                 if (ok) tc::mma_commit(&bar->accf[tb_]);
             }
@@ -323,6 +342,13 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const double* __restrict
     if (warp == kMmaWarp) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
+// w2[i] = s_i^2 rounded to FP32 for i < N, zero up to len (the last stage of
+// the last row split may run past N).
+__global__ void gram_w2_kernel(const double* __restrict__ s, int64_t N, int64_t len, float* __restrict__ w2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+        w2[i] = (i < N) ? (float)(s[i] * s[i]) : 0.f;
+}
+
 // Sum the row-split partial tiles and write the full symmetric k x k matrix
 // (column-major).
 __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_tiles, int n_split, int64_t k,
@@ -334,6 +360,9 @@ __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_
         const int ib = e / kTT, ia = e - ib * kTT;   // partial tiles are [n][m]
         const int64_t ga = ta * kTT + ia, gb = tb * kTT + ib;
         if (ga >= k || gb >= k) continue;
+        // the weights sit on the a side only, so a diagonal tile is not exactly
+        // symmetric: its lower triangle (ga >= gb) is mirrored
+        if (ta == tb && ia < ib) continue;
         double s = 0.0;
         for (int p = 0; p < n_split; ++p) s += partial[((int64_t)p * n_tiles + t) * kTT * kTT + e];
         G[gb * k + ga] = s;
@@ -422,12 +451,19 @@ int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t 
     int rc = KEVD_OK;
     double* partial = arena_get<double>(ctx, "tc.gpart", (size_t)n_split * n_tiles * kTT * kTT, &rc);
     int* err = arena_get<int>(ctx, "tc.err", 1, &rc);
+    // squared weights, one 128-byte bulk copy per stage (row offsets are
+    // multiples of 32, so every copy is 128-byte aligned)
+    const int64_t w2_len = (N + kTK - 1) / kTK * kTK + kTK;
+    float* w2 = arena_get<float>(ctx, "tc.w2", (size_t)w2_len, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
     KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
+    gram_w2_kernel<<<(int)std::min<int64_t>((w2_len + 255) / 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(
+        s, N, w2_len, w2);
+    KEVD_LAUNCH(ctx);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel), (int)kSmemBytes));
     {
         ProfScope ps(ctx, "gram_tc", st);
-        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, s, N, k, n_tiles, rows_per, partial,
+        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, w2, N, k, n_tiles, rows_per, partial,
                                                                        err);
         KEVD_LAUNCH(ctx);
     }

@@ -182,6 +182,25 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t saddr) {
     return d;
 }
 
+// The same descriptor split into its two 32-bit words: the low word carries
+// the start address (bits 0-13, address >> 4) and the leading byte offset,
+// the high word is a constant.  Adding 2 to the low word moves the start by
+// 32 bytes (one MMA's K for 32-bit elements) within a 128-byte row.
+__host__ __device__ constexpr uint32_t desc_hi_sw128() {
+    return (1024u >> 4) | (1u << (46 - 32)) | (2u << (61 - 32));
+}
+static_assert(((uint64_t)desc_hi_sw128() << 32) == (((uint64_t)(1024u >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61)),
+              "high descriptor word: stride byte offset 1024, version 1, SWIZZLE_128B");
+__device__ __forceinline__ uint32_t desc_lo_sw128(uint32_t saddr) {
+    return ((saddr & 0x3FFFFu) >> 4) | (1u << 16);
+}
+__device__ __forceinline__ uint64_t desc_sw128_from_lo(uint32_t lo) {
+    return ((uint64_t)desc_hi_sw128() << 32) | lo;
+}
+// Keep a value in a register from here on (the compiler may not sink its
+// computation past this point).
+__device__ __forceinline__ void reg_pin(uint64_t& v) { asm volatile("" : "+l"(v)); }
+
 // Instruction descriptor, kind::tf32: D f32, A and B tf32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
@@ -221,6 +240,13 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 // (32 elements of K per 128-byte row).
 __host__ __device__ constexpr uint32_t sw128_off(uint32_t row, uint32_t k) {
     return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + (k & 3u) * 4u;
+}
+
+// The tf32 value the tensor core reads from an FP32 operand: its low 13
+// mantissa bits are ignored (truncation toward zero), so x - tf32_trunc(x) is
+// exact in FP32 and is what a one-operand read drops.
+__device__ __forceinline__ float tf32_trunc(float x) {
+    return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
 }
 
 // Round to the nearest tf32 value (ties away from zero): the result has zero

@@ -15,12 +15,17 @@
 // FP32 registers with round-to-nearest, so the tensor-core accumulator's
 // rounding bias never builds up over r.
 //
-// CTA (320 threads, persistent over row blocks):
+// CTA (448 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
 //              and the pre-split S_i tiles (bulk copy)
 //   warp 1     TMEM allocation and the single MMA-issuing thread (A from
-//              Tensor Memory, B from shared memory)
-//   warps 2,3,8,9  converters: thread m owns row m of the F tile (its TMEM lane
+//              Tensor Memory, B from shared memory); a stage's 12 MMAs are
+//              issued back to back from descriptors computed before its wait
+//              (a 128 x 64 x 8 kind::tf32 MMA takes 48 cycles that way on
+//              GB300, and each dependent instruction between two MMAs adds
+//              its latency)
+//   warps 2,3,8,9 and 10-13  converters, two groups of four taking alternate
+//              stages: thread m owns row m of the F tile (its TMEM lane
 //              quarter is warp % 4), zeroes columns >= r and writes the hi and
 //              lo parts into the stage's Tensor Memory a-slot (tcgen05.st)
 //   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
@@ -65,7 +70,7 @@ constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
 constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
-constexpr int kThreads = 320;
+constexpr int kThreads = 448;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = kMaxFeatures;
 constexpr int kFeatChunk = 64;      // features staged at a time by update_kcols_kernel
@@ -82,7 +87,10 @@ struct Bars {
     uint32_t tmem_base;
 };
 
-__device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || w == 8 || w == 9; }
+// converter warps: group 0 = {2, 3, 8, 9} takes the even stages, group 1 =
+// {10, 11, 12, 13} the odd ones; warp % 4 is the TMEM lane quarter it writes
+__device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || w >= 8; }
+__device__ __forceinline__ int cvt_group(int w) { return w >= 10 ? 1 : 0; }
 
 struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
     int64_t rank;
@@ -114,10 +122,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
     Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // L_i^{-1} (FP32) for the epilogue
+    // L_i^{-1} (FP32) for the epilogue, transposed: mv[q][a] = L_i^{-1}[a][q]
+    // (zero above the diagonal and beyond nacc)
     for (int e = threadIdx.x; e < kCols * kCols; e += kThreads) {
-        const int a = e / kCols, q = e - a * kCols;
-        mv[e] = (a < nacc && q < nacc) ? minv_f[a * b + q] : 0.f;
+        const int q = e / kCols, a = e - q * kCols;
+        mv[e] = (a < nacc && q <= a) ? minv_f[a * b + q] : 0.f;
     }
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -183,43 +192,59 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         }
         __syncwarp();
     } else if (warp == 1) {
-        // ---------------- MMA issuer
+        // ---------------- MMA issuer.  The stages of this CTA run as one flat
+        // sequence g = 0, 1, ... (row block after row block) taken kStages at a
+        // time, so the ring slot of each stage, and with it every operand
+        // descriptor, is a compile-time index into registers filled once.
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
-            int64_t g = 0, pg = 0;
+            const uint32_t bh_base = tc::desc_lo_sw128(tc::smem_u32(base + kAOp));   // slot 0's b-hi tile
+            uint64_t dbh[kStages][kKs / 8], dbl[kStages][kKs / 8];
+#pragma unroll
+            for (int sl = 0; sl < kStages; ++sl)
+#pragma unroll
+                for (int j = 0; j < kKs / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
+                    const uint32_t bh = bh_base + (uint32_t)sl * (uint32_t)(kStageBytes >> 4);
+                    dbh[sl][j] = tc::desc_sw128_from_lo(bh + 2u * j);
+                    dbl[sl][j] = tc::desc_sw128_from_lo(bh + (uint32_t)(kBOp >> 4) + 2u * j);
+                    tc::reg_pin(dbh[sl][j]);
+                    tc::reg_pin(dbl[sl][j]);
+                }
+            const int64_t my_blocks = (nblk - blockIdx.x + gridDim.x - 1) / gridDim.x;
+            const int64_t total = my_blocks * n_st;
+            int s = 0;            // stage within the current row block
+            int64_t pg = 0;       // partial buffers used so far
             bool ok = true;
-            for (int64_t rb = blockIdx.x; rb < nblk && ok; rb += gridDim.x) {
-                for (int s = 0; s < n_st; ++s, ++g) {
-                    const int slot = (int)(g % kStages);
-                    const uint32_t use = (uint32_t)(g / kStages);
+            for (int64_t g0 = 0; g0 < total && ok; g0 += kStages) {
+                const uint32_t use = (uint32_t)(g0 / kStages);
+#pragma unroll
+                for (int sl = 0; sl < kStages; ++sl) {
+                    if (g0 + sl >= total) break;
                     const int tb = (int)(pg % kBufs);
                     const uint32_t tuse = (uint32_t)(pg / kBufs);
                     const bool first = (s % kPerPartial) == 0;
                     const bool last = (s % kPerPartial) == kPerPartial - 1 || s == n_st - 1;
+                    const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * 64u, alo = ahi + 32u;
+                    const uint32_t dt = tbase + (uint32_t)(tb * kCols);
+                    const uint32_t acc0 = first ? 0u : 1u;
                     if ((first && !tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs)) ||
-                        !tc::mbar_wait(&bar->cvt_full[slot], use & 1u, kTimeoutNs)) {
+                        !tc::mbar_wait(&bar->cvt_full[sl], use & 1u, kTimeoutNs)) {
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
-                    uint8_t* stg = base + (size_t)slot * kStageBytes;
-                    const uint32_t ahi = tbase + kTmemA + (uint32_t)slot * 64u, alo = ahi + 32u;
-                    const uint32_t bhi = tc::smem_u32(stg + kAOp), blo = tc::smem_u32(stg + kAOp + kBOp);
-                    const uint32_t dt = tbase + (uint32_t)(tb * kCols);
 #pragma unroll
                     for (int j = 0; j < kKs / 8; ++j) {
-                        const uint32_t ko = (uint32_t)(j * 32);   // 8 tf32: 32 bytes of B, 8 TMEM columns of A
-                        const uint64_t dbh = tc::desc_kmajor_sw128(bhi + ko);
-                        const uint64_t dbl = tc::desc_kmajor_sw128(blo + ko);
-                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh, idesc, (j > 0 || !first) ? 1u : 0u);
-                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbl, idesc, 1u);
-                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh, idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, j > 0 ? 1u : acc0);
+                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbl[sl][j], idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc, 1u);
                     }
-                    tc::mma_commit(&bar->empty[slot]);
+                    tc::mma_commit(&bar->empty[sl]);
                     if (last) {
                         tc::mma_commit(&bar->accf[tb]);
                         ++pg;
                     }
+                    if (++s == n_st) s = 0;
                 }
             }
             if (!ok) atomicExch(err, 12);
@@ -231,10 +256,12 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // ---------------- converters: thread m owns row m of the F tile
         const int m = 32 * (warp & 3) + lane;
         const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
+        const int grp = cvt_group(warp);
         int64_t g = 0;
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
             bool ok = true;
             for (int s = 0; s < n_st; ++s, ++g) {
+                if ((int)(g & 1) != grp) continue;
                 const int slot = (int)(g % kStages);
                 const uint32_t use = (uint32_t)(g / kStages);
                 if (!tc::mbar_wait(&bar->tma_full[slot], use & 1u, kTimeoutNs)) {
@@ -295,15 +322,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     continue;
                 }
                 tc::tc_fence_after();
-                float v[32], v2[32];
+                float v[32];
                 const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kCols);
-                tc::tmem_ld32(ta, v);          // both halves in flight, one wait
-                tc::tmem_ld32(ta + 32, v2);
-                tc::tmem_wait_ld();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    acc[j] += v[j];
-                    acc[32 + j] += v2[j];
+                for (int h = 0; h < 2; ++h) {   // one half at a time (register budget of 448 threads)
+                    tc::tmem_ld32(ta + 32u * h, v);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) acc[32 * h + j] += v[j];
                 }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
@@ -324,18 +350,39 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
                     acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
                 }
-                // G = T L_i^{-T}  (mv lower triangular, zero beyond nacc); G -> own tile row
+                // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
+                // chains, two 16-byte broadcast loads of L_i^{-1} per term); each
+                // G[a] sums e = 0..a in increasing order (the zero terms above the
+                // diagonal leave it unchanged); G -> own tile row
                 float sq = 0.f;
 #pragma unroll
-                for (int a = 0; a < kCols; ++a) {
-                    if (a < nacc) {
-                        float gsum = 0.f;
-                        const float* ma = mv + a * kCols;
+                for (int a0 = 0; a0 < kCols; a0 += 8) {
+                    if (a0 < nacc) {
+                        float g8[8];
 #pragma unroll
-                        for (int e = 0; e <= a; ++e) gsum = fmaf(acc[e], ma[e], gsum);
-                        *reinterpret_cast<float*>(ktile + (a >> 5) * kAOp +
-                                                  tc::sw128_off((uint32_t)rloc, (uint32_t)(a & 31))) = gsum;
-                        sq = fmaf(gsum, gsum, sq);
+                        for (int u = 0; u < 8; ++u) g8[u] = 0.f;
+#pragma unroll
+                        for (int e = 0; e < a0 + 8; ++e) {
+                            const float4 m0 = *reinterpret_cast<const float4*>(mv + e * kCols + a0);
+                            const float4 m1 = *reinterpret_cast<const float4*>(mv + e * kCols + a0 + 4);
+                            g8[0] = fmaf(acc[e], m0.x, g8[0]);
+                            g8[1] = fmaf(acc[e], m0.y, g8[1]);
+                            g8[2] = fmaf(acc[e], m0.z, g8[2]);
+                            g8[3] = fmaf(acc[e], m0.w, g8[3]);
+                            g8[4] = fmaf(acc[e], m1.x, g8[4]);
+                            g8[5] = fmaf(acc[e], m1.y, g8[5]);
+                            g8[6] = fmaf(acc[e], m1.z, g8[6]);
+                            g8[7] = fmaf(acc[e], m1.w, g8[7]);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int a = a0 + u;
+                            if (a < nacc) {
+                                *reinterpret_cast<float*>(ktile + (a >> 5) * kAOp +
+                                                          tc::sw128_off((uint32_t)rloc, (uint32_t)(a & 31))) = g8[u];
+                                sq = fmaf(g8[u], g8[u], sq);
+                            }
+                        }
                     }
                 }
                 nd = fmax(d_old - (double)sq, 0.0);
@@ -378,8 +425,8 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
                     const RoundView* st, float* __restrict__ Kc) {
     if (st->done || st->nacc == 0) return;
     const int nacc = st->nacc;
-    extern __shared__ __align__(16) float ksm[];
-    constexpr int dp = kFeatChunk + 4;   // 16-byte aligned rows
+    extern __shared__ float ksm[];
+    constexpr int dp = kFeatChunk + 1;
     float* xr = ksm;                 // 128 x dp
     float* xq = ksm + kRows * dp;    // 64 x dp
     const int64_t row0 = (int64_t)blockIdx.x * kRows;
@@ -393,37 +440,27 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
     for (int c0 = 0; c0 < d; c0 += kFeatChunk) {
         const int w = min(kFeatChunk, d - c0);
         __syncthreads();
-        const int w4 = (w + 3) & ~3;   // staged width, zero-padded to a multiple of 4
-        for (int e = threadIdx.x; e < kRows * w4; e += 256) {
-            const int rr = e / w4, kk = e - rr * w4;
+        for (int e = threadIdx.x; e < kRows * w; e += 256) {
+            const int rr = e / w, kk = e - rr * w;
             const int64_t i = row0 + rr;
-            xr[rr * dp + kk] = (i < N && kk < w) ? X[i * d + c0 + kk] : 0.f;
+            xr[rr * dp + kk] = (i < N) ? X[i * d + c0 + kk] : 0.f;
         }
-        for (int e = threadIdx.x; e < kCols * w4; e += 256) {
-            const int q = e / w4, kk = e - q * w4;
-            xq[q * dp + kk] = (q < nacc && kk < w) ? X[sacc[q] * d + c0 + kk] : 0.f;
+        for (int e = threadIdx.x; e < kCols * w; e += 256) {
+            const int q = e / w, kk = e - q * w;
+            xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + c0 + kk] : 0.f;
         }
         __syncthreads();
-        // four features per 16-byte load; padded features are zero in both
-        // operands and add nothing (0 - 0 squared), so the sum and its order
-        // over the real features are unchanged
-        for (int k4 = 0; k4 < w4; k4 += 4) {
-            float4 vr[8], vq[4];
+        for (int kk = 0; kk < w; ++kk) {
+            float vr[8], vq[4];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) vr[a] = *reinterpret_cast<const float4*>(xr + (ty + 16 * a) * dp + k4);
+            for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) vq[c] = *reinterpret_cast<const float4*>(xq + (tx + 16 * c) * dp + k4);
+            for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
 #pragma unroll
             for (int a = 0; a < 8; ++a)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    float t = vr[a].x - vq[c].x;
-                    acc[a][c] = fmaf(t, t, acc[a][c]);
-                    t = vr[a].y - vq[c].y;
-                    acc[a][c] = fmaf(t, t, acc[a][c]);
-                    t = vr[a].z - vq[c].z;
-                    acc[a][c] = fmaf(t, t, acc[a][c]);
-                    t = vr[a].w - vq[c].w;
+                    const float t = vr[a] - vq[c];
                     acc[a][c] = fmaf(t, t, acc[a][c]);
                 }
         }
@@ -545,7 +582,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     }
     {
         ProfScope ps(ctx, "rp_update_kcols", s);
-        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 4) * sizeof(float);
+        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 1) * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
         update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
         KEVD_LAUNCH(ctx);
