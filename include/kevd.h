@@ -254,6 +254,16 @@ int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision,
                        int64_t N, int64_t k, int64_t ldF, const double* s,
                        double* G, void* stream);
 
+/* Both Grams of the bistochastic EVD in one pass over F: G = F^T diag(s)^2 F
+ * and G2 = F^T diag(s2)^2 F (the Atil and Btil accumulations of
+ * ks_kevd.cu:1091-1159 and :1627-1685, which the reference runs as two
+ * passes).  For KEVD_MIXED each F tile is loaded once and feeds both; the
+ * results equal two kevd_weighted_gram calls bit for bit.  Arguments as for
+ * kevd_weighted_gram. */
+int kevd_weighted_gram2(kevd_ctx* ctx, const void* F, int32_t precision,
+                        int64_t N, int64_t k, int64_t ldF, const double* s,
+                        const double* s2, double* G, double* G2, void* stream);
+
 /* Bistochastic EVD of Khat = F F^T.  F: device N x ldF (double or float by
  * precision).  lam: host, k eigenvalues ascending.  U: device, N x k_out
  * float row-major, columns ascending (the last is the leading eigenvector),

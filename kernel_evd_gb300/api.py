@@ -374,6 +374,24 @@ def weighted_gram(ctx: Context, F: torch.Tensor, s: torch.Tensor, k: int | None 
     return G.T.contiguous()   # column-major storage -> row-major view
 
 
+def weighted_gram2(ctx: Context, F: torch.Tensor, s: torch.Tensor, s2: torch.Tensor,
+                   k: int | None = None) -> tuple[torch.Tensor, torch.Tensor]:
+    """(F^T diag(s)^2 F, F^T diag(s2)^2 F) in one pass over F (FP32 F: one tensor-core kernel)."""
+    if not (F.is_cuda and F.dtype in (torch.float32, torch.float64) and F.stride(1) == 1):
+        raise ValueError("F must be a CUDA float32/float64 tensor with unit column stride")
+    _need_cuda(s, torch.float64, "s")
+    _need_cuda(s2, torch.float64, "s2")
+    p = KEVD_FP64 if F.dtype == torch.float64 else KEVD_MIXED
+    N = F.shape[0]
+    if k is None:
+        k = F.shape[1]
+    G = torch.empty((k, k), dtype=torch.float64, device=F.device)
+    G2 = torch.empty((k, k), dtype=torch.float64, device=F.device)
+    ctx._check(ctx.lib.kevd_weighted_gram2(ctx.h, _ptr(F), p, N, k, F.stride(0), _ptr(s), _ptr(s2), _ptr(G),
+                                           _ptr(G2), _stream()))
+    return G.T.contiguous(), G2.T.contiguous()
+
+
 class NystromModel:
     """Resident landmarks + eigenfunction coefficients for out-of-sample states."""
 

@@ -305,6 +305,12 @@ int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision, int64_t 
     return run_weighted_gram(ctx, F, precision, N, k, ldF, s, G, as_stream(stream));
 }
 
+int kevd_weighted_gram2(kevd_ctx* ctx, const void* F, int32_t precision, int64_t N, int64_t k, int64_t ldF,
+                        const double* s, const double* s2, double* G, double* G2, void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_weighted_gram2(ctx, F, precision, N, k, ldF, s, s2, G, G2, as_stream(stream));
+}
+
 __global__ void cast_d2f_kernel(const double* __restrict__ a, int64_t rows, int64_t cols,
                                 int64_t lda, float* __restrict__ b, int64_t ldb) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols;

@@ -27,6 +27,8 @@ namespace kevd {
 
 int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s, double* G,
                 cudaStream_t st);
+int run_gram2_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s,
+                 const double* s2, double* G, double* G2, cudaStream_t st);
 int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
                       cudaStream_t st);
 
@@ -905,8 +907,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
         // FP32 factor: 3xTF32 tcgen05 Gram with FP64 accumulation across row chunks
         ev_rsqrt_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(qtil, w2, N);
         KEVD_LAUNCH(ctx);
-        KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, dinv, A, s));
-        KEVD_TRY(run_gram_tc(ctx, FT, ldT, N, k, w2, B, s));
+        KEVD_TRY(run_gram2_tc(ctx, FT, ldT, N, k, dinv, w2, A, B, s));
     } else {
         ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
         KEVD_LAUNCH(ctx);
@@ -1058,6 +1059,20 @@ int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, in
     KEVD_TRY(gram<double>(ctx, (const double*)F, ldF, N, k, w2, G, st));
     KEVD_CUDA(ctx, cudaStreamSynchronize(st));
     return KEVD_OK;
+}
+
+int run_weighted_gram2(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
+                       const double* s_dev, const double* s2_dev, double* G, double* G2, cudaStream_t st) {
+    if (!F || !s_dev || !s2_dev || !G || !G2 || N < 1 || k < 1 || ldF < k)
+        return set_error(ctx, KEVD_ERR_ARG, "weighted_gram2: bad arguments");
+    if (precision == KEVD_MIXED) {
+        float* FT = nullptr;
+        int64_t ldT = 0;
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, st));
+        return run_gram2_tc(ctx, FT, ldT, N, k, s_dev, s2_dev, G, G2, st);
+    }
+    KEVD_TRY(run_weighted_gram(ctx, F, precision, N, k, ldF, s_dev, G, st));
+    return run_weighted_gram(ctx, F, precision, N, k, ldF, s2_dev, G2, st);
 }
 
 int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k,

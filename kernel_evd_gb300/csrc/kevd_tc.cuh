@@ -242,6 +242,14 @@ __host__ __device__ constexpr uint32_t sw128_off(uint32_t row, uint32_t k) {
     return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + (k & 3u) * 4u;
 }
 
+// *p += v in global memory without waiting for the old value (red.global.add,
+// FP64, round to nearest).  Reductions from one thread to one address take
+// effect in program order, so a per-thread sequence of flushes into its own
+// partial sums gives the same value as plain read-modify-writes.
+__device__ __forceinline__ void red_add(double* p, double v) {
+    asm volatile("red.relaxed.gpu.global.add.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
 // The tf32 value the tensor core reads from an FP32 operand: its low 13
 // mantissa bits are ignored (truncation toward zero), so x - tf32_trunc(x) is
 // exact in FP32 and is what a one-operand read drops.

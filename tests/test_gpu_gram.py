@@ -32,6 +32,28 @@ def test_gram_tc_fp32_factor(ctx, N, k, ld):
     np.testing.assert_allclose(G, G.T, rtol=0, atol=0)
 
 
+@pytest.mark.parametrize("N,k,ld", [(5000, 300, 300), (4097, 128, 128), (100, 2, 2), (33, 129, 132),
+                                    (70000, 260, 260)])
+def test_gram2_tc_one_pass(ctx, N, k, ld):
+    """Both Grams in one pass over F: the same values as two single-Gram calls,
+    bit for bit (same split, MMA order and FP64 flushes per output tile)."""
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(7 * N + k)
+    Fb = rng.standard_normal((N, ld)).astype(np.float32)
+    Fb[:, : k // 3] = np.abs(Fb[:, : k // 3]) + 0.5
+    s = rng.uniform(0.5, 2.0, N)
+    s2 = rng.uniform(0.1, 3.0, N)
+    Ft = torch.from_numpy(Fb).cuda()
+    Ft = Ft[:, :k] if ld != k else Ft
+    st, s2t = torch.from_numpy(s).cuda(), torch.from_numpy(s2).cuda()
+    G, G2 = api.weighted_gram2(ctx, Ft, st, s2t, k=k)
+    assert torch.equal(G, api.weighted_gram(ctx, Ft, st, k=k))
+    assert torch.equal(G2, api.weighted_gram(ctx, Ft, s2t, k=k))
+    R2 = _ref(Fb[:, :k], s2)
+    scale = np.sqrt(np.outer(np.diag(R2), np.diag(R2)))
+    assert (np.abs(G2.cpu().numpy() - R2) / scale).max() < 3e-5
+
+
 def test_gram_fp64_factor(ctx):
     from kernel_evd_gb300 import api
     rng = np.random.default_rng(3)
