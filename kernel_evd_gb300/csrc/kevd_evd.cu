@@ -200,8 +200,8 @@ __global__ void ev_square_kernel(const double* __restrict__ x, double* __restric
         y[i] = x[i] * x[i];
 }
 
-__global__ void ev_trace_shift_kernel(double* __restrict__ A, int64_t k, double* __restrict__ out) {
-    // one CTA: out[0] = tr(A), out[1] = shift; A += shift I
+__global__ void ev_trace_shift_kernel(double* __restrict__ A, int64_t k, double* __restrict__ out, double c) {
+    // one CTA: out[0] = tr(A), out[1] = shift = c u tr(A); A += shift I
     __shared__ double red[1024];
     double s = 0.0;
     for (int64_t i = threadIdx.x; i < k; i += blockDim.x) s += A[i * k + i];
@@ -212,7 +212,7 @@ __global__ void ev_trace_shift_kernel(double* __restrict__ A, int64_t k, double*
         __syncthreads();
     }
     const double tr = red[0];
-    const double sh = DBL_EPSILON * tr;
+    const double sh = c * DBL_EPSILON * tr;
     for (int64_t i = threadIdx.x; i < k; i += blockDim.x) A[i * k + i] += sh;
     if (threadIdx.x == 0) {
         out[0] = tr;
@@ -924,8 +924,6 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     }
 
     // dense 1: shift, Cholesky A + sI = L L^T
-    ev_trace_shift_kernel<<<1, 1024, 0, s>>>(A, k, trsh);
-    KEVD_LAUNCH(ctx);
     KEVD_SOLVER(ctx, cusolverDnSetStream(ctx->solver, s));
     KEVD_BLAS(ctx, cublasSetStream(ctx->blas, s));
     int lwork = 0, lwork2 = 0;
@@ -937,9 +935,32 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     double* work = arena_get<double>(ctx, "ev.work", (size_t)std::max(lwork, lwork2) + 1, &st);
     if (st != KEVD_OK) return st;
     {
+        // s = u tr(A) (ks_kevd.cu:1447-1499).  The tensor-core Grams of an FP32
+        // factor carry about 1e-5 relative error, which can leave a numerically
+        // rank-deficient A indefinite by more than u tr(A); there potrf is
+        // retried from a saved A with the shift raised 1e3-fold per attempt (the
+        // leading eigenpairs are refined against F in FP64 afterwards).  The FP64
+        // factor keeps the single attempt.
         ProfScope p1(ctx, "dense_potrf", s);
-        KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A, (int)k, work,
-                                          lwork, flags + 2));
+        const int attempts = (sizeof(T) == 4) ? 4 : 1;
+        if (attempts > 1)
+            KEVD_CUDA(ctx, cudaMemcpyAsync(W, A, (size_t)k * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        double c = 1.0;
+        for (int a = 0; a < attempts; ++a, c *= 1e3) {
+            if (a > 0) {
+                KEVD_CUDA(ctx, cudaMemcpyAsync(A, W, (size_t)k * k * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                KEVD_CUDA(ctx, cudaMemsetAsync(flags + 2, 0, sizeof(int), s));
+            }
+            ev_trace_shift_kernel<<<1, 1024, 0, s>>>(A, k, trsh, c);
+            KEVD_LAUNCH(ctx);
+            KEVD_SOLVER(ctx, cusolverDnDpotrf(ctx->solver, CUBLAS_FILL_MODE_LOWER, (int)k, A, (int)k, work,
+                                              lwork, flags + 2));
+            if (a + 1 < attempts) {
+                KEVD_CUDA(ctx, cudaMemcpyAsync(hflags + 2, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+                KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+                if (hflags[2] == 0) break;
+            }
+        }
     }
     // dense 2: W = L^T B L
     const double one = 1.0;
