@@ -304,7 +304,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         int64_t g = 0;
         int64_t kit = 0;
         bool ok = true;
-        __shared__ double wsum[4];
+        __shared__ double wsum[2][4];
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
             const int64_t row0 = rb * kRows;
             const int64_t i = row0 + rloc;
@@ -351,9 +351,10 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
                 }
                 // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
-                // chains, two 16-byte broadcast loads of L_i^{-1} per term); each
-                // G[a] sums e = 0..a in increasing order (the zero terms above the
-                // diagonal leave it unchanged); G -> own tile row
+                // chains; the two 16-byte broadcast loads of L_i^{-1} for term e+2
+                // are issued before the FMAs of term e); each G[a] sums e = 0..a in
+                // increasing order (the zero terms above the diagonal leave it
+                // unchanged); G -> own row of the tile
                 float sq = 0.f;
 #pragma unroll
                 for (int a0 = 0; a0 < kCols; a0 += 8) {
@@ -361,10 +362,19 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         float g8[8];
 #pragma unroll
                         for (int u = 0; u < 8; ++u) g8[u] = 0.f;
+                        float4 n0 = *reinterpret_cast<const float4*>(mv + a0);
+                        float4 n1 = *reinterpret_cast<const float4*>(mv + a0 + 4);
+                        float4 p0 = *reinterpret_cast<const float4*>(mv + kCols + a0);
+                        float4 p1 = *reinterpret_cast<const float4*>(mv + kCols + a0 + 4);
 #pragma unroll
                         for (int e = 0; e < a0 + 8; ++e) {
-                            const float4 m0 = *reinterpret_cast<const float4*>(mv + e * kCols + a0);
-                            const float4 m1 = *reinterpret_cast<const float4*>(mv + e * kCols + a0 + 4);
+                            const float4 m0 = n0, m1 = n1;
+                            n0 = p0;
+                            n1 = p1;
+                            if (e + 2 < a0 + 8) {
+                                p0 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0);
+                                p1 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0 + 4);
+                            }
                             g8[0] = fmaf(acc[e], m0.x, g8[0]);
                             g8[1] = fmaf(acc[e], m0.y, g8[1]);
                             g8[2] = fmaf(acc[e], m0.z, g8[2]);
@@ -388,27 +398,37 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 nd = fmax(d_old - (double)sq, 0.0);
                 dvec[i] = nd;
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");   // G rows in the tile
-            // coalesced store of the new columns: warp q writes rows q, q+4, ...
+            __syncwarp();   // this warp's 32 rows of G in the tile
+            // coalesced store of the new columns: warp q writes its own rows
+            // 32q .. 32q+31, so no other warp has to be waited for
             if (ok) {
-                const int64_t nrows = min((int64_t)kRows, N - row0);
-                for (int rr = q; rr < nrows; rr += 4) {
-                    float* frow = F + (row0 + rr) * ldF + r;
-                    for (int a = lane; a < nacc; a += 32)
-                        frow[a] = *reinterpret_cast<const float*>(
-                            ktile + (a >> 5) * kAOp + tc::sw128_off((uint32_t)rr, (uint32_t)(a & 31)));
+                // lane owns columns lane and lane + 32; eight rows per batch so
+                // the shared loads of a batch are in flight together
+                const int nr = (int)min((int64_t)32, N - row0 - 32 * q);
+                float* fbase = F + (row0 + 32 * q) * ldF + r;
+                const bool c1 = lane < nacc, c2 = lane + 32 < nacc;
+#pragma unroll 8
+                for (int rr = 0; rr < 32; ++rr) {
+                    if (rr < nr) {
+                        const uint32_t row = (uint32_t)(32 * q + rr);
+                        const float v1 = *reinterpret_cast<const float*>(ktile + tc::sw128_off(row, (uint32_t)lane));
+                        const float v2 =
+                            *reinterpret_cast<const float*>(ktile + kAOp + tc::sw128_off(row, (uint32_t)lane));
+                        if (c1) fbase[(int64_t)rr * ldF + lane] = v1;
+                        if (c2) fbase[(int64_t)rr * ldF + lane + 32] = v2;
+                    }
                 }
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");   // tile consumed
-            tc::mbar_arrive(&bar->kempty);
+            __syncwarp();
+            tc::mbar_arrive(&bar->kempty);   // this thread is done with the tile
             ++kit;
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
-            if (lane == 0) wsum[q] = nd;
+            double* ws = wsum[kit & 1];   // alternate buffers: one barrier per row block
+            if (lane == 0) ws[q] = nd;
             asm volatile("bar.sync 1, 128;" ::: "memory");
-            if (rloc == 0) dblk[rb] = (wsum[0] + wsum[1]) + (wsum[2] + wsum[3]);
-            asm volatile("bar.sync 1, 128;" ::: "memory");
+            if (rloc == 0) dblk[rb] = (ws[0] + ws[1]) + (ws[2] + ws[3]);
         }
     }
     tc::tc_fence_before();
