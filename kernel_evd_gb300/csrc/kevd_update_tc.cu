@@ -10,10 +10,10 @@
 //
 // Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
 // lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
-// stage accumulates hi_a hi_b + hi_a lo_b + lo_a hi_b; every two stages use a
-// fresh TMEM partial (24 MMA updates), and the epilogue sums the partials in
-// FP32 registers with round-to-nearest, so the tensor-core accumulator's
-// rounding bias never builds up over r.
+// stage accumulates hi_a hi_b + lo_a hi_b and, in a second accumulator,
+// hi_a lo_b; every four stages use a fresh TMEM partial (32 MMA updates), and
+// the epilogue sums the partials in FP32 registers with round-to-nearest, so
+// the tensor-core accumulator's rounding bias never builds up over r.
 //
 // CTA (448 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
@@ -50,22 +50,28 @@ constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
 // Pipeline shape (tuning parameters; Tensor Memory holds kBufs partial buffers
-// and kStages a-slots of 64 columns each, 512 columns in all)
+// of 128 columns and kStages a-slots of 64 columns, 512 columns in all)
 #ifndef KEVD_UPD_STAGES
 #define KEVD_UPD_STAGES 4
 #endif
 #ifndef KEVD_UPD_BUFS
-#define KEVD_UPD_BUFS 4
+#define KEVD_UPD_BUFS 2
 #endif
 #ifndef KEVD_UPD_PER_PARTIAL
-#define KEVD_UPD_PER_PARTIAL 2
+#define KEVD_UPD_PER_PARTIAL 4
 #endif
 constexpr int kStages = KEVD_UPD_STAGES;
 constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
-constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of 64 columns
+constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of kPartCols columns
 constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulated per TMEM partial
-constexpr uint32_t kTmemA = kBufs * 64;   // a-slots after the partials, 64 per stage (hi 32, lo 32)
-static_assert(kBufs * 64 + kStages * 64 <= 512, "Tensor Memory holds 512 columns");
+// A partial buffer holds two 64-column accumulators side by side: columns
+// [0,64) take hi_a hi_b + lo_a hi_b, columns [64,128) take hi_a lo_b (one
+// N = 128 MMA against the b-hi and b-lo tiles, which lie back to back in
+// shared memory as one 128-row operand, plus one N = 64 MMA: 8 MMAs per stage
+// instead of 12)
+constexpr int kPartCols = 2 * kCols;
+constexpr uint32_t kTmemA = kBufs * kPartCols;   // a-slots after the partials, 64 per stage (hi 32, lo 32)
+static_assert(kBufs * kPartCols + kStages * 64 <= 512, "Tensor Memory holds 512 columns");
 constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
@@ -198,6 +204,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // descriptor, is a compile-time index into registers filled once.
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
+            constexpr uint32_t idesc2 = tc::idesc_tf32(kRows, kPartCols);
             const uint32_t bh_base = tc::desc_lo_sw128(tc::smem_u32(base + kAOp));   // slot 0's b-hi tile
             uint64_t dbh[kStages][kKs / 8], dbl[kStages][kKs / 8];
 #pragma unroll
@@ -225,7 +232,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     const bool first = (s % kPerPartial) == 0;
                     const bool last = (s % kPerPartial) == kPerPartial - 1 || s == n_st - 1;
                     const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * 64u, alo = ahi + 32u;
-                    const uint32_t dt = tbase + (uint32_t)(tb * kCols);
+                    const uint32_t dt = tbase + (uint32_t)(tb * kPartCols);
                     const uint32_t acc0 = first ? 0u : 1u;
                     if ((first && !tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs)) ||
                         !tc::mbar_wait(&bar->cvt_full[sl], use & 1u, kTimeoutNs)) {
@@ -235,9 +242,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     tc::tc_fence_after();
 #pragma unroll
                     for (int j = 0; j < kKs / 8; ++j) {
-                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, j > 0 ? 1u : acc0);
-                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbl[sl][j], idesc, 1u);
-                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc, 1u);
+                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the first half
+                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc2, j > 0 ? 1u : acc0);
+                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[sl]);
                     if (last) {
@@ -323,13 +330,15 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
                 tc::tc_fence_after();
                 float v[32];
-                const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kCols);
+                const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kPartCols);
+                // 32 columns at a time (register budget of 448 threads): the main
+                // sums, then the hi_a lo_b sums of the same columns
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {   // one half at a time (register budget of 448 threads)
-                    tc::tmem_ld32(ta + 32u * h, v);
+                for (int h = 0; h < 4; ++h) {
+                    tc::tmem_ld32(ta + (uint32_t)((h & 1) * 32 + (h >> 1) * kCols), v);
                     tc::tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) acc[32 * h + j] += v[j];
+                    for (int j = 0; j < 32; ++j) acc[32 * (h & 1) + j] += v[j];
                 }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
