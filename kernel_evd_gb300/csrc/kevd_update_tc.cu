@@ -70,6 +70,8 @@ constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulate
 // shared memory as one 128-row operand, plus one N = 64 MMA: 8 MMAs per stage
 // instead of 12)
 constexpr int kPartCols = 2 * kCols;
+static_assert((kBufs & (kBufs - 1)) == 0 && (kPerPartial & (kPerPartial - 1)) == 0,
+              "partial-buffer count and stages per partial are powers of two");
 constexpr uint32_t kTmemA = kBufs * kPartCols;   // a-slots after the partials, 64 per stage (hi 32, lo 32)
 static_assert(kBufs * kPartCols + kStages * 64 <= 512, "Tensor Memory holds 512 columns");
 constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
@@ -206,35 +208,37 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
             constexpr uint32_t idesc2 = tc::idesc_tf32(kRows, kPartCols);
             const uint32_t bh_base = tc::desc_lo_sw128(tc::smem_u32(base + kAOp));   // slot 0's b-hi tile
-            uint64_t dbh[kStages][kKs / 8], dbl[kStages][kKs / 8];
+            uint64_t dbh[kStages][kKs / 8];   // b-hi and b-lo tiles as one 128-row operand
 #pragma unroll
             for (int sl = 0; sl < kStages; ++sl)
 #pragma unroll
                 for (int j = 0; j < kKs / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
                     const uint32_t bh = bh_base + (uint32_t)sl * (uint32_t)(kStageBytes >> 4);
                     dbh[sl][j] = tc::desc_sw128_from_lo(bh + 2u * j);
-                    dbl[sl][j] = tc::desc_sw128_from_lo(bh + (uint32_t)(kBOp >> 4) + 2u * j);
                     tc::reg_pin(dbh[sl][j]);
-                    tc::reg_pin(dbl[sl][j]);
                 }
             const int64_t my_blocks = (nblk - blockIdx.x + gridDim.x - 1) / gridDim.x;
             const int64_t total = my_blocks * n_st;
-            int s = 0;            // stage within the current row block
-            int64_t pg = 0;       // partial buffers used so far
+            // per-stage bookkeeping in 32-bit counters (the issuing thread runs
+            // it between two MMA bursts, so every dependent instruction counts)
+            uint32_t s = 0;            // stage within the current row block
+            uint32_t pg = 0;           // partial buffers used so far
+            const uint32_t last_s = (uint32_t)n_st - 1u;
             bool ok = true;
             for (int64_t g0 = 0; g0 < total && ok; g0 += kStages) {
                 const uint32_t use = (uint32_t)(g0 / kStages);
 #pragma unroll
                 for (int sl = 0; sl < kStages; ++sl) {
                     if (g0 + sl >= total) break;
-                    const int tb = (int)(pg % kBufs);
-                    const uint32_t tuse = (uint32_t)(pg / kBufs);
-                    const bool first = (s % kPerPartial) == 0;
-                    const bool last = (s % kPerPartial) == kPerPartial - 1 || s == n_st - 1;
+                    const uint32_t tb = pg & (uint32_t)(kBufs - 1);
+                    const uint32_t tpar = ((pg / (uint32_t)kBufs) & 1u) ^ 1u;
+                    const uint32_t sp = s & (uint32_t)(kPerPartial - 1);
+                    const bool first = sp == 0u;
+                    const bool last = sp == (uint32_t)(kPerPartial - 1) || s == last_s;
                     const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * 64u, alo = ahi + 32u;
-                    const uint32_t dt = tbase + (uint32_t)(tb * kPartCols);
+                    const uint32_t dt = tbase + tb * (uint32_t)kPartCols;
                     const uint32_t acc0 = first ? 0u : 1u;
-                    if ((first && !tc::mbar_wait(&bar->acce[tb], (tuse & 1u) ^ 1u, kTimeoutNs)) ||
+                    if ((first && !tc::mbar_wait(&bar->acce[tb], tpar, kTimeoutNs)) ||
                         !tc::mbar_wait(&bar->cvt_full[sl], use & 1u, kTimeoutNs)) {
                         ok = false;
                         break;
@@ -251,7 +255,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         tc::mma_commit(&bar->accf[tb]);
                         ++pg;
                     }
-                    if (++s == n_st) s = 0;
+                    s = (s == last_s) ? 0u : s + 1u;
                 }
             }
             if (!ok) atomicExch(err, 12);
