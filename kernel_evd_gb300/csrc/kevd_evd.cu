@@ -18,6 +18,7 @@
 // FP64; FP32 factors accumulate FP32 partials over 1024-row chunks that are
 // then added in FP64.
 #include "kevd_internal.cuh"
+#include "kevd_tc.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -390,7 +391,7 @@ evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
 // U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32)
 __global__ void __launch_bounds__(256)
 evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ Z, int m,
-             const double* __restrict__ dinv, float* __restrict__ U) {
+             const double* __restrict__ dinv, float* __restrict__ U, float* __restrict__ Y) {
     __shared__ __align__(16) float Zs[128][32];
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     float acc[32];
@@ -428,67 +429,111 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
     if (i >= N) return;
     const double di = dinv[i];
 #pragma unroll
-    for (int q = 0; q < 32; ++q)
-        if (q < m) U[i * m + q] = (float)((double)acc[q] * di);
+    for (int q = 0; q < 32; ++q) {
+        const float u = (float)((double)acc[q] * di);
+        if (q < m) U[i * m + q] = u;
+        // Y = Dtil^{-1} U of the rounded U, 32 columns (zero beyond m), for the
+        // Rayleigh-Ritz T1 pass
+        if (Y) Y[i * 32 + q] = (q < m) ? (float)((double)u * di) : 0.f;
+    }
 }
 
-// Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] U[i][q] dinv_i over this
-// CTA's rows, for a block of 64 columns j.  128 threads, thread (jg, qg) owns
-// columns j = 4 jg..4 jg+3 and q = 4 qg..4 qg+3: per row one 16-byte load of
-// F and one of the weights feed 16 FMAs.  FP32 products and 8-row FP32
-// partials (round to nearest: their errors are unbiased and average out in
-// H); the partials are added with compensation over the CTA's row range.
+// Rayleigh-Ritz T1 partials: T1[j][q] = sum_i FT[j][i] Y[i][q] over this CTA's
+// rows, Y = Dtil^{-1} U rounded to FP32 (N x 32, written by evt_u_kernel), for a
+// block of 64 columns j.  128 threads, thread (jg, qg) owns columns 4 jg..4 jg+3
+// and q = 4 qg..4 qg+3.  Tiles of 64 rows are staged with 16-byte cp.async into
+// a double buffer (the next tile is in flight while this one is used): F as
+// [column][row] with the 16-byte chunk index of a column XOR-ed with
+// (column >> 1) & 7 (the four columns a warp reads at once land in four
+// different bank groups), Y as [row][q].  FP32 products and 8-row FP32 partials
+// (round to nearest: their errors are unbiased and average out in H); the
+// partials are added with compensation over the CTA's row range.
+constexpr int kT1Rows = 64;
+constexpr size_t kT1Smem = 2 * (size_t)(64 * kT1Rows + kT1Rows * 32) * sizeof(float);
 __global__ void __launch_bounds__(128)
-evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ U, int m,
-              const double* __restrict__ dinv, int64_t rows_per, double* __restrict__ partial) {
-    constexpr int kP = 68;   // row pitch: 16-byte aligned rows
-    __shared__ __align__(16) float Fs[64][kP];   // [row i][column j]
-    __shared__ __align__(16) float Ws[64][32];   // [row i][q]
+evt_t1_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ Y, int m,
+              int64_t rows_per, double* __restrict__ partial) {
+    extern __shared__ __align__(16) float t1sm[];
     const int tid = threadIdx.x;
     const int jg = tid >> 3, qg = tid & 7;
     const int64_t j0 = (int64_t)blockIdx.x * 64;
     const int64_t r0 = (int64_t)blockIdx.y * rows_per;
     const int64_t r1 = min(N, r0 + rows_per);
+    const int64_t n_t = (r1 > r0) ? (r1 - r0 + kT1Rows - 1) / kT1Rows : 0;
+    auto fbuf = [&](int b) { return t1sm + (size_t)b * (64 * kT1Rows + kT1Rows * 32); };
+    auto stage = [&](int64_t t, int b) {
+        float* Fs = fbuf(b);
+        float* Ws = Fs + 64 * kT1Rows;
+        const int64_t i0 = r0 + t * kT1Rows;
+        for (int e = tid; e < 64 * 16 + kT1Rows * 8; e += 128) {
+            if (e < 64 * 16) {
+                const int jj = e >> 4, c = e & 15;   // column jj, rows 4c..4c+3
+                const int64_t j = j0 + jj, i = i0 + 4 * c;
+                const bool ok = (j < k) && (i < r1);
+                const float* src = ok ? FT + j * ldT + i : FT;
+                tc::cp_async16(Fs + jj * kT1Rows + 4 * (c ^ ((jj >> 1) & 7)), src, ok ? 16u : 0u);
+            } else {
+                const int e2 = e - 64 * 16;
+                const int ii = e2 >> 3, c = e2 & 7;   // row ii, q 4c..4c+3
+                const int64_t i = i0 + ii;
+                const bool ok = i < r1;
+                tc::cp_async16(Ws + ii * 32 + 4 * c, ok ? Y + i * 32 + 4 * c : Y, ok ? 16u : 0u);
+            }
+        }
+    };
     float ks[4][4], kc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) ks[a][b] = kc[a][b] = 0.f;
-    for (int64_t i0 = r0; i0 < r1; i0 += 64) {
-        __syncthreads();
-        for (int e = tid; e < 64 * 64; e += 128) {
-            const int jj = e >> 6, ii = e & 63;   // consecutive threads: consecutive rows (coalesced)
-            const int64_t j = j0 + jj, i = i0 + ii;
-            Fs[ii][jj] = (j < k && i < r1) ? FT[j * ldT + i] : 0.f;
-        }
-        for (int e = tid; e < 64 * 32; e += 128) {
-            const int ii = e >> 5, q = e & 31;
-            const int64_t i = i0 + ii;
-            Ws[ii][q] = (i < r1 && q < m) ? (float)((double)U[i * m + q] * dinv[i]) : 0.f;
+    if (n_t > 0) stage(0, 0);
+    tc::cp_async_commit();
+    for (int64_t t = 0; t < n_t; ++t) {
+        if (t + 1 < n_t) {
+            stage(t + 1, (int)((t + 1) & 1));
+            tc::cp_async_commit();
+            tc::cp_async_wait<1>();
+        } else {
+            tc::cp_async_wait<0>();
         }
         __syncthreads();
+        const float* Fs = fbuf((int)(t & 1));
+        const float* Ws = Fs + 64 * kT1Rows;
 #pragma unroll 1
-        for (int i8 = 0; i8 < 64; i8 += 8) {
+        for (int i8 = 0; i8 < kT1Rows; i8 += 8) {
             float p[4][4];
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
                 for (int b = 0; b < 4; ++b) p[a][b] = 0.f;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const float4 f = *reinterpret_cast<const float4*>(&Fs[i8 + u][4 * jg]);
-                const float4 w = *reinterpret_cast<const float4*>(&Ws[i8 + u][4 * qg]);
-                const float fv[4] = {f.x, f.y, f.z, f.w}, wv[4] = {w.x, w.y, w.z, w.w};
+            for (int h = 0; h < 2; ++h) {
+                const int rc = (i8 >> 2) + h;   // 16-byte chunk of rows 4 rc..4 rc+3
+                float fv[4][4], wv[4][4];
 #pragma unroll
-                for (int a = 0; a < 4; ++a)
+                for (int a = 0; a < 4; ++a) {
+                    const int jj = 4 * jg + a;
+                    const float4 f = *reinterpret_cast<const float4*>(Fs + jj * kT1Rows + 4 * (rc ^ ((jj >> 1) & 7)));
+                    fv[a][0] = f.x; fv[a][1] = f.y; fv[a][2] = f.z; fv[a][3] = f.w;
+                }
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) p[a][b] = fmaf(fv[a], wv[b], p[a][b]);
+                for (int u = 0; u < 4; ++u) {
+                    const float4 w = *reinterpret_cast<const float4*>(Ws + (4 * rc + u) * 32 + 4 * qg);
+                    wv[u][0] = w.x; wv[u][1] = w.y; wv[u][2] = w.z; wv[u][3] = w.w;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) p[a][b] = fmaf(fv[a][u], wv[u][b], p[a][b]);
             }
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
                 for (int b = 0; b < 4; ++b) kahan_add(ks[a][b], kc[a][b], p[a][b]);
         }
+        __syncthreads();
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -513,8 +558,11 @@ constexpr int kHmRows = 64;
 __global__ void __launch_bounds__(128)
 evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const float* __restrict__ T1hl,
               int m, const float* __restrict__ U, const double* __restrict__ qinv, double* __restrict__ partial) {
-    __shared__ __align__(16) float Fs[32][kHmRows];   // [column j of the chunk][row i]
-    __shared__ __align__(16) float Ts[2][32][32];     // hi, lo of a 32-column chunk of T1
+    // double buffer of (F chunk [column j][row i], T1 hi/lo chunk), 16-byte
+    // cp.async copies: the next (tile, column chunk) step is in flight while
+    // this one is used
+    __shared__ __align__(16) float Fsb[2][32][kHmRows];
+    __shared__ __align__(16) float Tsb[2][2][32][32];
     __shared__ float Ws[kHmRows][33];
     const int tid = threadIdx.x;
     const int ig = tid >> 3, qg = tid & 7;
@@ -522,34 +570,55 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
 #pragma unroll
     for (int r = 0; r < 8; ++r) h64[r] = m64[r] = 0.0;
     const int64_t n_tiles = (N + kHmRows - 1) / kHmRows;
+    const int nch = (int)((k + 31) / 32);
+    auto stage = [&](int64_t t, int c, int b) {
+        const int64_t i0 = t * kHmRows, j0 = (int64_t)c * 32;
+        for (int e = tid; e < 32 * (kHmRows / 4) + 64 * 8; e += 128) {
+            if (e < 32 * (kHmRows / 4)) {
+                const int jj = e / (kHmRows / 4), rc = e % (kHmRows / 4);   // column jj, rows 4 rc..4 rc+3
+                const int64_t j = j0 + jj, i = i0 + 4 * rc;
+                const bool ok = (j < k) && (i < N);   // FT rows are padded to a multiple of 4 with zeros
+                tc::cp_async16(&Fsb[b][jj][4 * rc], ok ? FT + j * ldT + i : FT, ok ? 16u : 0u);
+            } else {
+                const int e2 = e - 32 * (kHmRows / 4);
+                const int r2 = e2 >> 3, c4 = e2 & 7;   // T1hl row 2 j + (hi, lo), q 4 c4..4 c4+3
+                const int jj = r2 >> 1, hl = r2 & 1;
+                const int64_t j = j0 + jj;
+                const bool ok = j < k;
+                tc::cp_async16(&Tsb[b][hl][jj][4 * c4], ok ? T1hl + (2 * j + hl) * 32 + 4 * c4 : T1hl, ok ? 16u : 0u);
+            }
+        }
+    };
+    int b = 0;
+    if ((int64_t)blockIdx.x < n_tiles) stage(blockIdx.x, 0, 0);
+    tc::cp_async_commit();
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const int64_t i0 = t * kHmRows;
         float ws[4][4], wc[4][4];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) ws[a][b] = wc[a][b] = 0.f;
-        for (int64_t j0 = 0; j0 < k; j0 += 32) {
-            __syncthreads();
-            for (int e = tid; e < 32 * kHmRows; e += 128) {
-                const int jj = e / kHmRows, ii = e - jj * kHmRows;   // coalesced along rows
-                const int64_t j = j0 + jj, i = i0 + ii;
-                Fs[jj][ii] = (j < k && i < N) ? FT[j * ldT + i] : 0.f;
-            }
-            for (int e = tid; e < 32 * 32; e += 128) {
-                const int jj = e >> 5, q = e & 31;
-                const int64_t j = j0 + jj;
-                Ts[0][jj][q] = (j < k) ? T1hl[(2 * j) * 32 + q] : 0.f;
-                Ts[1][jj][q] = (j < k) ? T1hl[(2 * j + 1) * 32 + q] : 0.f;
+            for (int bb = 0; bb < 4; ++bb) ws[a][bb] = wc[a][bb] = 0.f;
+        for (int c = 0; c < nch; ++c) {
+            const int64_t nt = (c + 1 < nch) ? t : t + gridDim.x;
+            const int nc = (c + 1 < nch) ? c + 1 : 0;
+            if (nt < n_tiles) {
+                stage(nt, nc, b ^ 1);
+                tc::cp_async_commit();
+                tc::cp_async_wait<1>();
+            } else {
+                tc::cp_async_wait<0>();
             }
             __syncthreads();
+            float (*Fs)[kHmRows] = Fsb[b];
+            float (*Ts)[32][32] = Tsb[b];
 #pragma unroll 1
             for (int j8 = 0; j8 < 32; j8 += 8) {
                 float p[4][4];
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) p[a][b] = 0.f;
+                    for (int bb = 0; bb < 4; ++bb) p[a][bb] = 0.f;
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     const float4 f = *reinterpret_cast<const float4*>(&Fs[j8 + u][4 * ig]);
@@ -560,13 +629,15 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int b = 0; b < 4; ++b) p[a][b] = fmaf(fv[a], hv[b], fmaf(fv[a], lv[b], p[a][b]));
+                        for (int bb = 0; bb < 4; ++bb) p[a][bb] = fmaf(fv[a], hv[bb], fmaf(fv[a], lv[bb], p[a][bb]));
                 }
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) kahan_add(ws[a][b], wc[a][b], p[a][b]);
+                    for (int bb = 0; bb < 4; ++bb) kahan_add(ws[a][bb], wc[a][bb], p[a][bb]);
             }
+            __syncthreads();
+            b ^= 1;
         }
         __syncthreads();
 #pragma unroll
@@ -574,9 +645,9 @@ evt_hm_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, c
             const int64_t i = i0 + 4 * ig + a;
             const float sq = (i < N) ? (float)sqrt(qinv[i]) : 0.f;
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int q = 4 * qg + b;
-                Ws[4 * ig + a][q] = (q < m) ? (ws[a][b] - wc[a][b]) * sq : 0.f;
+            for (int bb = 0; bb < 4; ++bb) {
+                const int q = 4 * qg + bb;
+                Ws[4 * ig + a][q] = (q < m) ? (ws[a][bb] - wc[a][bb]) * sq : 0.f;
             }
         }
         __syncthreads();
@@ -665,7 +736,7 @@ __global__ void rr_rotate_kernel(float* __restrict__ U, int64_t N, int m, const 
 
 // On the column-major FP32 factor FT (k x ldT).
 static int rayleigh_ritz(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, int m, float* U,
-                         const double* dinv, const double* qinv, double* lam_top, cudaStream_t s) {
+                         const float* Y, const double* qinv, double* lam_top, cudaStream_t s) {
     ProfScope ps(ctx, "ev_ritz", s);
     int st = KEVD_OK;
     const int ny = (int)std::min<int64_t>((N + 8191) / 8192, (int64_t)ctx->num_sms * 2);
@@ -679,7 +750,8 @@ static int rayleigh_ritz(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N,
     double* w = arena_get<double>(ctx, "rr.w", 64, &st);
     int* info = arena_get<int>(ctx, "rr.info", 1, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "rayleigh_ritz: out of device memory");
-    evt_t1_kernel<<<dim3(ceil_div(k, 64), ny), 128, 0, s>>>(FT, ldT, N, k, U, m, dinv, rows_per, tpart);
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&evt_t1_kernel), kT1Smem));
+    evt_t1_kernel<<<dim3(ceil_div(k, 64), ny), 128, kT1Smem, s>>>(FT, ldT, N, k, Y, m, rows_per, tpart);
     KEVD_LAUNCH(ctx);
     rr_sum_kernel<<<ceil_div(k * m, 256), 256, 0, s>>>(tpart, ny, k * m, T1);
     KEVD_LAUNCH(ctx);
@@ -1029,11 +1101,14 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     KEVD_BLAS(ctx, cublasDtrsm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
                                CUBLAS_DIAG_NON_UNIT, (int)k, k_out, &one, A, (int)k, Z, (int)k));
     // pass 4: U = Dtil^{-1} F Z
+    float* Yrr = nullptr;   // Dtil^{-1} U for the Rayleigh-Ritz T1 pass (FP32 factor)
     {
         ProfScope ps(ctx, "ev_u", s);
-        if (sizeof(T) == 4 && k_out <= 32)
-            evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U);
-        else
+        if (sizeof(T) == 4 && k_out <= 32) {
+            Yrr = arena_get<float>(ctx, "ev.Yrr", (size_t)N * 32, &st);
+            if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+            evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U, Yrr);
+        } else
             ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
         KEVD_LAUNCH(ctx);
     }
@@ -1046,7 +1121,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     if (sizeof(T) == 4 && hflags[2] == 0 && hflags[3] == 0 && k_out <= 32) {
         // FP32 factor: refine the leading k_out eigenpairs by Rayleigh-Ritz in FP64
         double top[32];
-        KEVD_TRY(rayleigh_ritz(ctx, FT, ldT, N, k, k_out, U, dinv, qinv, top, s));
+        KEVD_TRY(rayleigh_ritz(ctx, FT, ldT, N, k, k_out, U, Yrr, qinv, top, s));
         if (lam_h)
             for (int j = 0; j < k_out; ++j) lam_h[k - k_out + j] = top[j];
     }
