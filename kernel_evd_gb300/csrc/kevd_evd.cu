@@ -407,10 +407,17 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
         __syncthreads();
         if (i < N) {
             const int jn = (int)min((int64_t)128, k - j0);
+            // the four F values of the next step are loaded before this step's
+            // FMAs (columns past jn read as zero; Zs is zero there too)
+            float fn[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) fn[u] = (u < jn) ? FT[(j0 + u) * ldT + i] : 0.f;
             for (int jj = 0; jj < jn; jj += 4) {
                 float f[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) f[u] = (jj + u < jn) ? FT[(j0 + jj + u) * ldT + i] : 0.f;
+                for (int u = 0; u < 4; ++u) f[u] = fn[u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) fn[u] = (jj + 4 + u < jn) ? FT[(j0 + jj + 4 + u) * ldT + i] : 0.f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const float4* zr = reinterpret_cast<const float4*>(Zs[jj + u]);

@@ -82,6 +82,7 @@ constexpr int kThreads = 448;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = kMaxFeatures;
 constexpr int kFeatChunk = 64;      // features staged at a time by update_kcols_kernel
+constexpr int kGPitch = kCols + 1;  // row pitch of the new-column staging buffer (conflict-free by row and column)
 
 struct Bars {
     uint64_t tma_full[kStages];
@@ -127,7 +128,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
     // K(R, S_i) tile: two 128 x 32 SWIZZLE_128B halves (TMA), then G in place
     uint8_t* ktile = base + (size_t)kStages * kStageBytes;
     float* mv = reinterpret_cast<float*>(ktile + 2 * kAOp);                      // kCols x kCols
-    Bars* bar = reinterpret_cast<Bars*>(mv + kCols * kCols);
+    float* gbuf = mv + kCols * kCols;                                            // kRows x kGPitch: new columns
+    Bars* bar = reinterpret_cast<Bars*>(gbuf + kRows * kGPitch);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // L_i^{-1} (FP32) for the epilogue, transposed: mv[q][a] = L_i^{-1}[a][q]
@@ -352,7 +354,8 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 ok = false;
             }
             double nd = d_old;
-            if (ok && i < N) {
+            const bool live = ok && i < N;
+            if (live) {
                 // T = K(i, S_i) - P  (K(:, S_i) by update_kcols_kernel, TMA tile in smem)
 #pragma unroll
                 for (int c4 = 0; c4 < kCols / 4; ++c4) {
@@ -363,11 +366,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
                     acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
                 }
+            }
+            tc::mbar_arrive(&bar->kempty);   // this thread is done with the K tile: the next one may land
+            if (live) {
                 // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
                 // chains; the two 16-byte broadcast loads of L_i^{-1} for term e+2
                 // are issued before the FMAs of term e); each G[a] sums e = 0..a in
                 // increasing order (the zero terms above the diagonal leave it
-                // unchanged); G -> own row of the tile
+                // unchanged); G -> own row of the staging buffer
                 float sq = 0.f;
 #pragma unroll
                 for (int a0 = 0; a0 < kCols; a0 += 8) {
@@ -401,8 +407,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         for (int u = 0; u < 8; ++u) {
                             const int a = a0 + u;
                             if (a < nacc) {
-                                *reinterpret_cast<float*>(ktile + (a >> 5) * kAOp +
-                                                          tc::sw128_off((uint32_t)rloc, (uint32_t)(a & 31))) = g8[u];
+                                gbuf[rloc * kGPitch + a] = g8[u];
                                 sq = fmaf(g8[u], g8[u], sq);
                             }
                         }
@@ -411,7 +416,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 nd = fmax(d_old - (double)sq, 0.0);
                 dvec[i] = nd;
             }
-            __syncwarp();   // this warp's 32 rows of G in the tile
+            __syncwarp();   // this warp's 32 rows of G staged
             // coalesced store of the new columns: warp q writes its own rows
             // 32q .. 32q+31, so no other warp has to be waited for
             if (ok) {
@@ -423,17 +428,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 #pragma unroll 8
                 for (int rr = 0; rr < 32; ++rr) {
                     if (rr < nr) {
-                        const uint32_t row = (uint32_t)(32 * q + rr);
-                        const float v1 = *reinterpret_cast<const float*>(ktile + tc::sw128_off(row, (uint32_t)lane));
-                        const float v2 =
-                            *reinterpret_cast<const float*>(ktile + kAOp + tc::sw128_off(row, (uint32_t)lane));
+                        const float* grow = gbuf + (32 * q + rr) * kGPitch;
+                        const float v1 = grow[lane], v2 = grow[lane + 32];
                         if (c1) fbase[(int64_t)rr * ldF + lane] = v1;
                         if (c2) fbase[(int64_t)rr * ldF + lane + 32] = v2;
                     }
                 }
             }
             __syncwarp();
-            tc::mbar_arrive(&bar->kempty);   // this thread is done with the tile
             ++kit;
             // block sum of the new d over the 128 epilogue threads
 #pragma unroll
@@ -553,7 +555,9 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 }  // namespace
 
-constexpr size_t kUpdSmem = (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + sizeof(Bars) + 1024;
+constexpr size_t kUpdSmem =
+    (size_t)kStages * kStageBytes + 2 * kAOp + kCols * kCols * 4 + kRows * kGPitch * 4 + sizeof(Bars) + 1024;
+static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 
 // Whether the tensor-core update can run for this factor layout.
