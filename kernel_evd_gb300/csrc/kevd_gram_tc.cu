@@ -688,22 +688,44 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// FT[c * ldT + i] = F[i * ldF + c]: 32 x 32 tiles through shared memory.
-__global__ void transpose_kernel(const float* __restrict__ F, int64_t ldF, int64_t N, int64_t k,
-                                 float* __restrict__ FT, int64_t ldT) {
-    __shared__ float t[32][33];
-    const int64_t n_ti = (N + 31) / 32, n_tc = (k + 31) / 32;
+// FT[c * ldT + i] = F[i * ldF + c]: 64 x 64 tiles through shared memory, read
+// and written in 16-byte pieces where a piece lies inside the matrix and its
+// row stride allows (F rows: ldF % 4 == 0; FT rows: ldT % 4 == 0 always), else
+// element by element.
+__global__ void __launch_bounds__(256) transpose_kernel(const float* __restrict__ F, int64_t ldF, int64_t N,
+                                                        int64_t k, float* __restrict__ FT, int64_t ldT) {
+    __shared__ float t[64][65];
+    const int64_t n_ti = (N + 63) / 64, n_tc = (k + 63) / 64;
+    const bool vec_in = (ldF % 4) == 0 && ((uintptr_t)F % 16) == 0;
+    const bool vec_out = (ldT % 4) == 0 && ((uintptr_t)FT % 16) == 0;
+    const int tid = threadIdx.x;
     for (int64_t tile = blockIdx.x; tile < n_ti * n_tc; tile += gridDim.x) {
-        const int64_t i0 = (tile % n_ti) * 32, c0 = (tile / n_ti) * 32;
+        const int64_t i0 = (tile % n_ti) * 64, c0 = (tile / n_ti) * 64;
         __syncthreads();
-        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-            const int64_t i = i0 + r, c = c0 + threadIdx.x;
-            t[r][threadIdx.x] = (i < N && c < k) ? F[i * ldF + c] : 0.f;
+        for (int e = tid; e < 64 * 16; e += 256) {
+            const int r = e >> 4, c4 = (e & 15) * 4;   // row r, columns c4..c4+3 of the tile
+            const int64_t i = i0 + r, c = c0 + c4;
+            if (i < N && vec_in && c + 3 < k) {
+                const float4 v = *reinterpret_cast<const float4*>(F + i * ldF + c);
+                t[r][c4] = v.x; t[r][c4 + 1] = v.y; t[r][c4 + 2] = v.z; t[r][c4 + 3] = v.w;
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) t[r][c4 + u] = (i < N && c + u < k) ? F[i * ldF + c + u] : 0.f;
+            }
         }
         __syncthreads();
-        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-            const int64_t c = c0 + r, i = i0 + threadIdx.x;
-            if (c < k && i < ldT) FT[c * ldT + i] = t[threadIdx.x][r];
+        for (int e = tid; e < 64 * 16; e += 256) {
+            const int cc = e >> 4, r4 = (e & 15) * 4;   // FT row c0 + cc, rows i0 + r4..+3
+            const int64_t c = c0 + cc, i = i0 + r4;
+            if (c >= k) continue;
+            if (vec_out && i + 3 < ldT) {
+                *reinterpret_cast<float4*>(FT + c * ldT + i) =
+                    make_float4(t[r4][cc], t[r4 + 1][cc], t[r4 + 2][cc], t[r4 + 3][cc]);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (i + u < ldT) FT[c * ldT + i + u] = t[r4 + u][cc];
+            }
         }
     }
 }
@@ -714,9 +736,9 @@ __global__ void transpose_kernel(const float* __restrict__ F, int64_t ldF, int64
 int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
                       cudaStream_t st) {
     ProfScope ps(ctx, "ev_transpose", st);
-    const int64_t tiles = ((N + 31) / 32) * ((k + 31) / 32);
-    const int grid = (int)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16);
-    transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(F, ldF, N, k, FT, ldT);
+    const int64_t tiles = ((N + 63) / 64) * ((k + 63) / 64);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 8);
+    transpose_kernel<<<grid, 256, 0, st>>>(F, ldF, N, k, FT, ldT);
     KEVD_LAUNCH(ctx);
     return KEVD_OK;
 }

@@ -267,7 +267,8 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
                  int64_t* __restrict__ sacc, int64_t* __restrict__ piv,
                  int32_t* __restrict__ hm) {
     if (st->done) return;
-    extern __shared__ double H[];         // b x b
+    extern __shared__ double H[];         // b x b, then the b x b inverse being formed
+    double* MS = H + b * b;
     __shared__ double H0[kMaxBlock];
     __shared__ int accpos[kMaxBlock];
     __shared__ int s_dec, s_m;
@@ -276,7 +277,8 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
     const int nz = (int)((r + kColChunk - 1) / kColChunk);
     for (int e = tid; e < b * b; e += blockDim.x) {
         double v = kss[e];
-        for (int z = 0; z < nz; ++z) v -= hpart[(int64_t)z * b * b + e];
+#pragma unroll 8
+        for (int z = 0; z < nz; ++z) v -= hpart[(int64_t)z * b * b + e];   // loads ahead, subtractions in order
         H[e] = v;
     }
     __syncthreads();
@@ -309,22 +311,26 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
         }
     }
     const int nacc = s_m;
-    // forward substitution, one column per thread
-    for (int e = tid; e < b * b; e += blockDim.x) minv[e] = 0.0;
+    // forward substitution, one column per thread, in shared memory (the
+    // sequential dot products read what the same thread wrote a step earlier)
+    for (int e = tid; e < b * b; e += blockDim.x) MS[e] = 0.0;
     __syncthreads();
     if (tid < nacc) {
         const int t = tid;
         const int at = accpos[t];
-        minv[t * b + t] = 1.0 / H[at * b + at];
+        MS[t * b + t] = 1.0 / H[at * b + at];
         for (int a = t + 1; a < nacc; ++a) {
             const int aa = accpos[a];
             double s = 0.0;
-            for (int e = t; e < a; ++e) s += H[aa * b + accpos[e]] * minv[e * b + t];
-            minv[a * b + t] = -s / H[aa * b + aa];
+            for (int e = t; e < a; ++e) s += H[aa * b + accpos[e]] * MS[e * b + t];
+            MS[a * b + t] = -s / H[aa * b + aa];
         }
     }
     __syncthreads();
-    for (int e = tid; e < b * b; e += blockDim.x) minv_f[e] = (float)minv[e];
+    for (int e = tid; e < b * b; e += blockDim.x) {
+        minv[e] = MS[e];
+        minv_f[e] = (float)MS[e];
+    }
     if (tid < nacc) {
         const int64_t sp = props[accpos[tid]];
         sacc[tid] = sp;
@@ -564,7 +570,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     rp_init_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dvec, dblk, N, nblk, rs);
     KEVD_LAUNCH(ctx);
 
-    const size_t fsm = (size_t)b * b * sizeof(double);
+    const size_t fsm = (size_t)2 * b * b * sizeof(double);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_factor_kernel), (int)std::max(fsm, (size_t)1024)));
     const size_t usm = update_smem<T>(d);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_update_kernel<T>), (int)usm));
