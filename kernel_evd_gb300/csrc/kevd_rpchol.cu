@@ -36,6 +36,8 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
 
 constexpr int kRowBlock = 128;   // rows per update CTA (= rows per d partial sum)
 constexpr int kMaxBlock = 64;    // proposals per round supported by the SIMT update
+constexpr int kFactorThreads = 256;   // rp_factor_kernel: 16 x 16 threads over the trailing update
+static_assert(kFactorThreads == 256 && kMaxBlock * kMaxBlock % kFactorThreads == 0, "factor thread layout");
 constexpr int kColChunk = 32;    // F columns per hgram CTA
 constexpr int kFeat = 64;        // features staged at a time by the SIMT update
 constexpr int kSampleThreads = 1024;
@@ -267,30 +269,53 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
                  int64_t* __restrict__ sacc, int64_t* __restrict__ piv,
                  int32_t* __restrict__ hm) {
     if (st->done) return;
-    extern __shared__ double H[];         // b x b, then the b x b inverse being formed
+    extern __shared__ double H[];         // b x b, the b x b inverse being formed, the compacted factor
     double* MS = H + b * b;
+    double* LC = MS + b * b;
     __shared__ double H0[kMaxBlock];
+    __shared__ double us[kMaxBlock];      // the round's acceptance uniforms
     __shared__ int accpos[kMaxBlock];
     __shared__ int s_dec, s_m;
     const int tid = threadIdx.x;
     const int64_t r = st->rank;
     const int nz = (int)((r + kColChunk - 1) / kColChunk);
-    for (int e = tid; e < b * b; e += blockDim.x) {
-        double v = kss[e];
-#pragma unroll 8
-        for (int z = 0; z < nz; ++z) v -= hpart[(int64_t)z * b * b + e];   // loads ahead, subtractions in order
-        H[e] = v;
+    {
+        // 256 threads x 16 elements (b <= 64): the 16 chains of a thread advance
+        // together over the column chunks, so 16 loads are in flight per step;
+        // each element still subtracts its chunks in increasing order
+        constexpr int kPer = kMaxBlock * kMaxBlock / 256;
+        double v[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int e = tid + 256 * j;
+            v[j] = (e < b * b) ? kss[e] : 0.0;
+        }
+        for (int z = 0; z < nz; ++z) {
+            const double* hz = hpart + (int64_t)z * b * b;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int e = tid + 256 * j;
+                if (e < b * b) v[j] -= hz[e];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int e = tid + 256 * j;
+            if (e < b * b) H[e] = v[j];
+        }
     }
     __syncthreads();
-    for (int p = tid; p < b; p += blockDim.x) H0[p] = H[p * b + p];
+    for (int p = tid; p < b; p += blockDim.x) {
+        H0[p] = H[p * b + p];
+        us[p] = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + p] : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)p);
+    }
     if (tid == 0) s_m = 0;
     __syncthreads();
     const int64_t cap = k_max - r;
     for (int i = 0; i < b; ++i) {
         __syncthreads();  // everyone has consumed the previous decision
         if (tid == 0) {
-            const double u = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + i]
-                                      : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)i);
+            const double u = us[i];
             const double hii = H[i * b + i];
             const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol);
             s_dec = acc;
@@ -302,28 +327,30 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
             __syncthreads();
             for (int j = i + tid; j < b; j += blockDim.x) H[j * b + i] *= f;
             __syncthreads();
-            const int w = b - (i + 1);
-            for (int e = tid; e < w * w; e += blockDim.x) {
-                const int jj = i + 1 + e / w, kk = i + 1 + e % w;
-                if (jj >= kk) H[jj * b + kk] -= H[jj * b + i] * H[kk * b + i];
-            }
+            // trailing update of the lower triangle, 16 x 16 threads over (jj, kk)
+            for (int jj = i + 1 + (tid >> 4); jj < b; jj += 16)
+                for (int kk = i + 1 + (tid & 15); kk <= jj; kk += 16) H[jj * b + kk] -= H[jj * b + i] * H[kk * b + i];
             __syncthreads();
         }
     }
     const int nacc = s_m;
     // forward substitution, one column per thread, in shared memory (the
     // sequential dot products read what the same thread wrote a step earlier)
-    for (int e = tid; e < b * b; e += blockDim.x) MS[e] = 0.0;
+    // on the compacted factor LC (no index indirection inside the chains)
+    for (int e = tid; e < b * b; e += blockDim.x) {
+        MS[e] = 0.0;
+        const int a = e / b, c = e - a * b;
+        LC[e] = (a < nacc && c < nacc) ? H[accpos[a] * b + accpos[c]] : 0.0;
+    }
     __syncthreads();
     if (tid < nacc) {
         const int t = tid;
-        const int at = accpos[t];
-        MS[t * b + t] = 1.0 / H[at * b + at];
+        MS[t * b + t] = 1.0 / LC[t * b + t];
         for (int a = t + 1; a < nacc; ++a) {
-            const int aa = accpos[a];
+            const double* la = LC + a * b;
             double s = 0.0;
-            for (int e = t; e < a; ++e) s += H[aa * b + accpos[e]] * MS[e * b + t];
-            MS[a * b + t] = -s / H[aa * b + aa];
+            for (int e = t; e < a; ++e) s += la[e] * MS[e * b + t];
+            MS[a * b + t] = -s / la[a];
         }
     }
     __syncthreads();
@@ -570,7 +597,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     rp_init_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dvec, dblk, N, nblk, rs);
     KEVD_LAUNCH(ctx);
 
-    const size_t fsm = (size_t)2 * b * b * sizeof(double);
+    const size_t fsm = (size_t)3 * b * b * sizeof(double);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_factor_kernel), (int)std::max(fsm, (size_t)1024)));
     const size_t usm = update_smem<T>(d);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_update_kernel<T>), (int)usm));
@@ -597,7 +624,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
         }
         {
             ProfScope ps(ctx, "rp_factor", s);
-            rp_factor_kernel<<<1, 256, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
+            rp_factor_kernel<<<1, kFactorThreads, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
                                                  p->k_max, props, rs, minv, minv_f, sacc, piv, hm);
             KEVD_LAUNCH(ctx);
         }
