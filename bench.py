@@ -588,20 +588,30 @@ def main():
     acc = fac.accepted
     r_old = np.concatenate([[0], np.cumsum(acc)[:-1]])
     upd_bytes = float(np.sum(N * (4.0 * r_old + 4.0 * acc + 4.0 * d + 16.0)))
-    gram_flops = float(N) * k * (k + 1)     # one Gram launch: lower triangle incl. diagonal, 2 flops per MAC
+    # one launch forms both EVD Grams: two lower triangles incl. the diagonal, 2 flops per MAC
+    gram_flops = 2.0 * float(N) * k * (k + 1)
+    # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000 (round 5)
+    # read + wrote 538.6 MB against 542.4 MB of algorithmic bytes; traffic grows with N r, so the
+    # full-size figure is the algorithmic bytes scaled by that ratio
+    upd_traffic_ratio = 538.6 / 542.4
     roof = {}
     if "rp_update" in prof:
         t = prof["rp_update"][0] / args.steps / 1e3
         nl = max(1, prof["rp_update"][1] // args.steps)   # per step; rounds with nacc = 0 return at once
         roof["rp_update"] = {"bound": "hbm", "achieved": upd_bytes / t / 1e9, "peak": hbm, "unit": "GB/s",
-                             "frac": upd_bytes / t / 1e9 / hbm, "traffic": None,
-                             "bytes_per_launch": upd_bytes / nl, "note": src}
+                             "frac": upd_bytes / t / 1e9 / hbm,
+                             "traffic": upd_bytes / nl * upd_traffic_ratio,
+                             "bytes_per_launch": upd_bytes / nl,
+                             "note": src + "; traffic scaled from the ncu capture at N = 300,000 (DRAM / algorithmic "
+                                     "bytes = 0.993)"}
     if "gram_tc" in prof:
         t = prof["gram_tc"][0] / max(1, prof["gram_tc"][1])   # ms per launch
         t = t / 1e3
         roof["gram_tc"] = {"bound": "tensor", "achieved": gram_flops / t / 1e12, "peak": tc, "unit": "TFLOP/s",
                            "frac": gram_flops / t / 1e12 / tc, "traffic": None, "flops_per_launch": gram_flops,
-                           "note": src + " bf16 dense; useful flops (4xTF32 issues 4x this at the TF32 rate)"}
+                           "issued_tf32_tflops": 3.0 * gram_flops / t / 1e12,
+                           "note": src + " bf16 dense; useful flops of both Grams (3xTF32 issues 3x this at the "
+                                   "TF32 rate, half the bf16 rate)"}
     dom = max(prof, key=lambda k_: prof[k_][0]) if prof else None
     roofline = roof.get(dom) or (next(iter(roof.values())) if roof else None)
     if roofline is not None:
