@@ -254,6 +254,24 @@ int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision,
                        int64_t N, int64_t k, int64_t ldF, const double* s,
                        double* G, void* stream);
 
+/* Kuramoto-Sivashinsky trajectories on the GPU: the synthetic data of the
+ * workloads, by the scheme of the reference's generator (ks_datagen.py:21-101:
+ * ETDRK4 in FP64 on real-FFT coefficients, quadratic term dealiased by the 3/2
+ * rule).  n_traj trajectories of one grid size M (a power of two, 4 .. 128).
+ * Trajectory t starts from the M/2+1 rfft
+ * coefficients vhat0[t] (complex, interleaved re/im), steps with the ETDRK4
+ * coefficients coef[t] (6 x (M/2+1): E, E2, Q, f1, f2, f3) and the dealiased
+ * -1/2 d/dx factor g[t] (complex, interleaved), discards n_warm steps and writes
+ * n_snap[t] states of M floats (time-major) to the device buffer out[t].  coef,
+ * g, vhat0, n_snap and out are host arrays of n_traj entries each; the call
+ * returns when the trajectories are written.  precision: KEVD_FP64 steps in
+ * FP64 as the reference does (slow on the GB300's FP64 pipe); KEVD_MIXED steps in
+ * FP32, about 20x faster, statistically the same attractor but a different
+ * chaotic trajectory after a few Lyapunov times. */
+int kevd_ks_generate(kevd_ctx* ctx, int32_t n_traj, int32_t M, int32_t precision, const double* coef,
+                     const double* g, const double* vhat0, int64_t n_warm,
+                     const int64_t* n_snap, float* const* out, void* stream);
+
 /* Both Grams of the bistochastic EVD in one pass over F: G = F^T diag(s)^2 F
  * and G2 = F^T diag(s2)^2 F (the Atil and Btil accumulations of
  * ks_kevd.cu:1091-1159 and :1627-1685, which the reference runs as two

@@ -101,6 +101,7 @@ SIGNATURES = {
                                         C.POINTER(EvdInfo), C.POINTER(EvdDump), _P]),
     "kevd_weighted_gram": (C.c_int, [_P, _P, _I32, _I64, _I64, _I64, _P, _P, _P]),
     "kevd_weighted_gram2": (C.c_int, [_P, _P, _I32, _I64, _I64, _I64, _P, _P, _P, _P, _P]),
+    "kevd_ks_generate": (C.c_int, [_P, _I32, _I32, _I32, _P, _P, _P, _I64, _P, _P, _P]),
     "kevd_factor_from_linv": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I64, _P, _I32, _P, _I64, _P]),
     "kevd_factor_from_pivots": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I64, _I32, _P, _I64, _P]),
     "kevd_nystrom_prepare": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I32, _I64, _P, _I64, _I32,

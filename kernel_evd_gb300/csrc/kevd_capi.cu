@@ -305,6 +305,13 @@ int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision, int64_t 
     return run_weighted_gram(ctx, F, precision, N, k, ldF, s, G, as_stream(stream));
 }
 
+int kevd_ks_generate(kevd_ctx* ctx, int32_t n_traj, int32_t M, int32_t precision, const double* coef,
+                     const double* g, const double* vhat0, int64_t n_warm, const int64_t* n_snap, float* const* out,
+                     void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_ks_generate(ctx, n_traj, M, precision, coef, g, vhat0, n_warm, n_snap, out, as_stream(stream));
+}
+
 int kevd_weighted_gram2(kevd_ctx* ctx, const void* F, int32_t precision, int64_t N, int64_t k, int64_t ldF,
                         const double* s, const double* s2, double* G, double* G2, void* stream) {
     KEVD_CHECK_CTX(ctx);

@@ -193,6 +193,9 @@ int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N,
                          kevd_evd_dump* dump, cudaStream_t s);
 int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
                       const double* s_dev, double* G, cudaStream_t st);
+int run_ks_generate(kevd_ctx* ctx, int32_t n_traj, int32_t M, int32_t precision, const double* coef,
+                    const double* g, const double* vhat0, int64_t n_warm, const int64_t* n_snap,
+                    float* const* out, cudaStream_t s);
 int run_weighted_gram2(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
                        const double* s_dev, const double* s2_dev, double* G, double* G2, cudaStream_t st);
 int run_gather_rows(kevd_ctx* ctx, const void* F, int precision, int64_t ldF, const int64_t* idx,
