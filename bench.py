@@ -590,7 +590,7 @@ def main():
     upd_bytes = float(np.sum(N * (4.0 * r_old + 4.0 * acc + 4.0 * d + 16.0)))
     # one launch forms both EVD Grams: two lower triangles incl. the diagonal, 2 flops per MAC
     gram_flops = 2.0 * float(N) * k * (k + 1)
-    # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000 (round 5)
+    # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000
     # read + wrote 538.6 MB against 542.4 MB of algorithmic bytes; traffic grows with N r, so the
     # full-size figure is the algorithmic bytes scaled by that ratio
     upd_traffic_ratio = 538.6 / 542.4

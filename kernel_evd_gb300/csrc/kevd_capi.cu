@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(256) nystrom_eval_kernel(const float* __restri
     float* ys = reinterpret_cast<float*>(zc + kNyLm * kc);  // 32 x dp (one feature chunk)
     float* xc = ys + kNyRows * dp;                       // 32 x dp
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const float fscale = (float)scale;
+    const ScalePair fscale = split_scale(scale);
     const int64_t row0 = (int64_t)blockIdx.x * kNyRows;
     // with one feature chunk the query rows are staged once for all landmarks
     const bool one_chunk = d <= kNyFeat;
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(256) nystrom_eval_kernel(const float* __restri
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i)
-            kv[(ty + 8 * i) * (kNyLm + 1) + tx] = (j0 + tx < r) ? (double)expf(-fscale * dist[i]) : 0.0;
+            kv[(ty + 8 * i) * (kNyLm + 1) + tx] = (j0 + tx < r) ? (double)kexp_scaled(dist[i], fscale) : 0.0;
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < kNyMaxOut; ++q) {

@@ -12,10 +12,11 @@
 // Memory; the dropped parts (lo_a lo_b, the truncation of the lo reads) are
 // below 2^-20 of each product and shrink its magnitude by about 5e-7 on
 // average.  The tensor-core accumulator rounds each update with a one-sided
-// bias, so the FP32 partial is kept short: every 1024 rows it is added into
+// bias, so the FP32 partial is kept short: every 2048 rows it is added into
 // an FP64 tile in global memory and the long sum over N rows is FP64 (the
 // Gram accumulators of the reference are FP64, ks_kevd.cu:1152-1158).  The
-// relative error of a Gram entry is about 1e-5; eigenvalues are then refined
+// relative error of a Gram entry is about 4e-5 (1024-row partials halve it
+// and cost 14 % more time at N = 2M, k = 2000); eigenvalues are then refined
 // in FP64 by Rayleigh-Ritz (kevd_evd.cu).
 //
 // CTA roles (448 threads):
@@ -59,7 +60,7 @@ constexpr int kStages = 4;
 constexpr int kPrefetch = 0;          // stages of F prefetched into L2 ahead of the ring (0: off;
                                       // at N = 2M, k = 2000 a 6-stage prefetch cost 1.8x: it
                                       // broke the L2 sharing of panels between CTAs)
-constexpr int kFlushStages = 32;       // 1024 rows per FP32 TMEM partial
+constexpr int kFlushStages = 64;       // 2048 rows per FP32 TMEM partial
 constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
 constexpr int kStageBytes = 3 * kOpBytes;   // a (raw), b hi, b lo
 constexpr int kEpiWarps = 4;        // warps 0-3

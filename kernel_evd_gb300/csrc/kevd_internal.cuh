@@ -161,6 +161,30 @@ inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// The kernel scale 1/(Nq eps) of an FP32 kernel evaluation as an FP32 pair
+// hi + lo (hi = fl32(s)).  Rounding s to FP32 alone moves eps by up to 6e-8
+// relative for every entry of K alike, which shifts the spectrum
+// systematically; the pair keeps s to about 2^-48.
+struct ScalePair {
+    float hi, lo;
+};
+__host__ __device__ inline ScalePair split_scale(double s) {
+    const float hi = (float)s;
+    return {hi, (float)(s - (double)hi)};
+}
+
+// exp(-s x) in FP32 for a squared distance x >= 0 and s = hi + lo: with
+// a = fl(hi x), the product's rounding error (exact, by fma) and lo x form
+// a_lo, and e^{-(a + a_lo)} = e^{-a} (1 - a_lo) to first order (|a_lo| is
+// below 2^-22 a, so the dropped term a_lo^2/2 is below 2^-44 a^2 of the
+// value).  The entry then carries only the rounding of x and of expf.
+__device__ __forceinline__ float kexp_scaled(float x, ScalePair s) {
+    const float a = __fmul_rn(s.hi, x);
+    const float a_lo = fmaf(s.lo, x, fmaf(s.hi, x, -a));
+    const float e = expf(-a);
+    return fmaf(-e, a_lo, e);
+}
+
 // ---- stage entry points implemented in the .cu files (C++ linkage) --------
 int launch_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M, int64_t Nq,
                        float* X, cudaStream_t s);

@@ -456,7 +456,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
                 T kv = 0;
                 if (c < nacc) {
                     if (sizeof(T) == 8) kv = (T)exp(-scale * (double)acc[i][j]);
-                    else kv = (T)expf(-(float)scale * (float)acc[i][j]);
+                    else kv = (T)kexp_scaled((float)acc[i][j], split_scale(scale));
                 }
                 Tm[(ty + 16 * i) * (kMaxBlock + 1) + c] = kv;
             }

@@ -453,10 +453,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 }
 
 // K(:, S_i) for the round, FP32 from direct differences: Kc[i][c], 64 columns
-// per row (zero beyond nacc).  CTA = 128 rows x 64 pivots; thread (ty, tx) of
-// 16 x 16 computes rows ty + 16a (a < 8) and columns tx + 16b (b < 4).
+// per row (zero beyond nacc); the scale enters as an FP32 pair (kexp_scaled).
+// CTA = 128 rows x 64 pivots; thread (ty, tx) of 16 x 16 computes rows
+// ty + 16a (a < 8) and columns tx + 16b (b < 4).
 __global__ void __launch_bounds__(256)
-update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, const int64_t* __restrict__ sacc,
+update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, ScalePair scale, const int64_t* __restrict__ sacc,
                     const RoundView* st, float* __restrict__ Kc) {
     if (st->done || st->nacc == 0) return;
     const int nacc = st->nacc;
@@ -507,7 +508,7 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, float scale, 
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const int col = tx + 16 * c;
-            Kc[i * kCols + col] = (col < nacc) ? expf(-scale * acc[a][c]) : 0.f;
+            Kc[i * kCols + col] = (col < nacc) ? kexp_scaled(acc[a][c], scale) : 0.f;
         }
     }
 }
@@ -621,7 +622,8 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
         ProfScope ps(ctx, "rp_update_kcols", s);
         const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 1) * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
-        update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, (float)scale, sacc, rv, Kc);
+        update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, split_scale(scale), sacc, rv,
+                                                                             Kc);
         KEVD_LAUNCH(ctx);
     }
     {

@@ -34,13 +34,6 @@ int launch_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M, 
     return KEVD_OK;
 }
 
-template <typename T>
-__device__ inline T kexp(T x);
-template <>
-__device__ inline double kexp<double>(double x) { return exp(x); }
-template <>
-__device__ inline float kexp<float>(float x) { return expf(x); }
-
 constexpr int kBlkFeat = 128;   // features staged at a time
 
 // One CTA computes a 32 x 32 tile; thread (tx, ty) computes rows ty + 8j.
@@ -87,7 +80,12 @@ __global__ void __launch_bounds__(256) kernel_block_kernel(
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int64_t r = r_base + ty + 8 * j;
-        if (r < nrows) out[r * ld + c] = kexp<T>(-(T)scale * acc[j]);
+        if (r < nrows) {
+            if constexpr (sizeof(T) == 8)
+                out[r * ld + c] = exp(-scale * (double)acc[j]);
+            else
+                out[r * ld + c] = kexp_scaled((float)acc[j], split_scale(scale));
+        }
     }
 }
 
