@@ -612,10 +612,10 @@ def main():
                            "issued_tf32_tflops": 3.0 * gram_flops / t / 1e12,
                            "note": src + " bf16 dense; useful flops of both Grams (3xTF32 issues 3x this at the "
                                    "TF32 rate, half the bf16 rate)"}
-    dom = max(prof, key=lambda k_: prof[k_][0]) if prof else None
-    roofline = roof.get(dom) or (next(iter(roof.values())) if roof else None)
-    if roofline is not None:
-        roofline = dict(roofline, kernel=dom)
+    # the kernel with the most time among those with a roofline model (the residual
+    # update at N = 2M; at small N the dense k x k solvers lead and have none)
+    dom = max(roof, key=lambda k_: prof[k_][0]) if roof else None
+    roofline = dict(roof[dom], kernel=dom) if dom else None
     # --- CPU baseline on rank 0 (bounded sample)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
