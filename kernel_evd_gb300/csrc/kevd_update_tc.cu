@@ -19,7 +19,7 @@
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
 //              and the pre-split S_i tiles (bulk copy)
 //   warp 1     TMEM allocation and the single MMA-issuing thread (A from
-//              Tensor Memory, B from shared memory); a stage's 12 MMAs are
+//              Tensor Memory, B from shared memory); a stage's 8 MMAs are
 //              issued back to back from descriptors computed before its wait
 //              (a 128 x 64 x 8 kind::tf32 MMA takes 48 cycles that way on
 //              GB300, and each dependent instruction between two MMAs adds
@@ -30,7 +30,7 @@
 //              lo parts into the stage's Tensor Memory a-slot (tcgen05.st)
 //   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
 // Ring of 4 stages (shared-memory tiles + Tensor Memory a-slots of 64 columns)
-// and 4 TMEM partial buffers of 64 columns, handed over with mbarriers; every
+// and 2 TMEM partial buffers of 128 columns, handed over with mbarriers; every
 // wait is bounded (error flag on timeout).  The F tile never goes back to
 // shared memory split, so per stage the shared-memory traffic is the TMA write,
 // one read by the converters and the MMA's B reads.
