@@ -591,9 +591,9 @@ def main():
     # one launch forms both EVD Grams: two lower triangles incl. the diagonal, 2 flops per MAC
     gram_flops = 2.0 * float(N) * k * (k + 1)
     # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000
-    # read + wrote 538.6 MB against 542.4 MB of algorithmic bytes; traffic grows with N r, so the
+    # read + wrote 540.6 MB against 542.4 MB of algorithmic bytes; traffic grows with N r, so the
     # full-size figure is the algorithmic bytes scaled by that ratio
-    upd_traffic_ratio = 538.6 / 542.4
+    upd_traffic_ratio = 540.6 / 542.4
     roof = {}
     if "rp_update" in prof:
         t = prof["rp_update"][0] / args.steps / 1e3
@@ -603,7 +603,7 @@ def main():
                              "traffic": upd_bytes / nl * upd_traffic_ratio,
                              "bytes_per_launch": upd_bytes / nl,
                              "note": src + "; traffic scaled from the ncu capture at N = 300,000 (DRAM / algorithmic "
-                                     "bytes = 0.993)"}
+                                     "bytes = 0.997)"}
     if "gram_tc" in prof:
         t = prof["gram_tc"][0] / max(1, prof["gram_tc"][1])   # ms per launch
         t = t / 1e3
