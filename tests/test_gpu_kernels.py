@@ -40,6 +40,28 @@ def test_kernel_block(ctx, states, prec, tol):
                                rtol=0, atol=tol)
 
 
+def test_kernel_block_mixed_scale_unbiased(ctx, states):
+    """The FP32 kernel block carries no systematic error from rounding the scale to
+    FP32. The scale sits 0.45 ulp from its FP32 value (relative 3.4e-8). Every entry
+    with K > 1e-3 gives a relative error rel ~ -arg * delta (arg = scale * d^2), and
+    the least-squares delta stays below 1e-8; with fl32(scale) alone it is -3.0e-8
+    (a NumPy emulation of the FP32 arithmetic gives -3.0e-8 and 5e-10)."""
+    from kernel_evd_gb300 import api
+    rng = np.random.default_rng(5)
+    cols = rng.choice(states.shape[0], 600, replace=False)
+    s0 = np.float32(0.025)
+    sc = float(s0) + 0.45 * float(np.spacing(s0))
+    K = api.kernel_block(ctx, torch.from_numpy(states).cuda(), sc, torch.from_numpy(cols).cuda(),
+                         precision="mixed").cpu().numpy().astype(np.float64)
+    ref = kernel.kblock(states.astype(np.float64), np.arange(states.shape[0]), cols, sc)
+    m = ref > 1e-3
+    arg = -np.log(ref[m])
+    rel = (K[m] - ref[m]) / ref[m]
+    delta = -(rel * arg).sum() / (arg * arg).sum()
+    assert m.sum() > 100_000
+    assert abs(delta) < 1e-8, delta
+
+
 @pytest.mark.parametrize("N", [1, 2, 127, 128, 129, 1000])
 def test_calibrate_matches_oracle(ctx, states, N):
     from kernel_evd_gb300 import api
