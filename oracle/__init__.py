@@ -1,9 +1,10 @@
 """CPU oracle for the kernel low-rank pipeline (FP64 NumPy restatement).
 
 This package is TEST INFRASTRUCTURE.  Only ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` may import it, and only as the checker
-(or the timed CPU baseline); the product path in ``kernel_evd_gb300`` never
-imports, links or executes anything here.
+and the CPU-baseline legs of ``bench.py`` may import it, and only as the
+reference the GPU results are compared with (or as the timed CPU baseline); the
+product path in ``kernel_evd_gb300`` never imports, links or executes anything
+here.
 
 Modules and the reference code they restate:
 
