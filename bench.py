@@ -68,6 +68,17 @@ def dist_info():
     return ws, rank, local
 
 
+def max_over_ranks(vals, dist=None, device="cuda"):
+    """Each value's maximum over all ranks: N replicas finish when the slowest one
+    does, so the whole job's time per step is the largest rank time."""
+    if dist is None:
+        return [float(v) for v in vals]
+    import torch
+    t = torch.tensor([float(v) for v in vals], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
 def sample_pairs(N: int, n_pairs: int, seed: int = 0):
     rng = np.random.default_rng(seed)
     i = rng.integers(0, N, n_pairs, dtype=np.int64)
@@ -646,13 +657,7 @@ def main():
     if args.serve_seconds > 0:
         phase("serving", serving_phase, ctx, X, Xd, scale, args)
     # --- max over ranks
-    val = ms / 1e3
-    if dist is not None:
-        t = torch.tensor([val, e2e_ms / 1e3], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        val, e2e_s = float(t[0]), float(t[1])
-    else:
-        e2e_s = e2e_ms / 1e3
+    val, e2e_s = max_over_ranks([ms / 1e3, e2e_ms / 1e3], dist)
     if rank == 0:
         line = {"metric": METRIC, "value": val, "unit": "s", "n_gpus": n_gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": val * 1e3, "higher_is_better": False,
