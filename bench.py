@@ -53,12 +53,21 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--cal-n", type=int, default=200_000, help="states in the calibration measurement (0: skip)")
     ap.add_argument("--c4-datasets", type=int, default=48, help="datasets in the batched phase (0: skip)")
+    ap.add_argument("--no-c1", action="store_true", help="skip the N = 20,000 plain FP64 phase")
     ap.add_argument("--no-autotune", action="store_true", help="skip the block-size autotuner (profiling runs)")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the serving window (0: no serving phase)")
     ap.add_argument("--fact-rate", type=float, default=20.0, help="factorization requests per second")
     ap.add_argument("--query-rate", type=float, default=2000.0, help="query batches per second")
     return ap.parse_args()
+
+
+def workload_config(args, N, d, n_gpus):
+    """The workload as both arms name it (identical dicts)."""
+    return {"workload": f"block RPCholesky + bistochastic EVD, N={N}, d={d}, k={args.k}, b={args.b}, "
+                        f"top {args.kout}",
+            "l2": "inputs larger than L2 (X 512 MB, F 16 GB)",
+            "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"}
 
 
 def dist_info():
@@ -202,6 +211,69 @@ def calibration_phase(ctx, Xd, args, sm_mhz):
             "vs_fp64": {"rows": n64, "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
                         "scales_compared": int(mask.sum()), "same_selected_eps": sel32["idmax"] == sel64["idmax"],
                         "fp64_pass_s": t64}}
+
+
+def c1_phase(ctx, X, args):
+    """The plain FP64 configuration at N = 20,000: the first 20,000 states of the
+    benchmark trajectory (KS L = 22, d = 64, seed 0), eps by the 41-value
+    calibration procedure (exact median over all pairs), unblocked RPCholesky
+    (b = 1) to rank 500, bistochastic EVD, top 32.  GPU time (CUDA events) of
+    calibration, factorisation and EVD; parity with the FP64 oracle run of the same
+    low-rank pipeline (same Philox draws: pivots, trace error, top-32 eigenvalues);
+    and the dense FP64 EVD of the reference's CPU oracle program (ks_reference.py,
+    restated with a blocked kernel build) timed on the host cores, with the
+    low-rank eigenpairs compared against it."""
+    import torch
+    from kernel_evd_gb300 import api
+    from oracle import dense, evd, rpchol
+    n, k, top = 20_000, 500, 32
+    Xs = np.ascontiguousarray(X[:n])
+    Xd = torch.from_numpy(Xs).cuda()
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    eps, med, _ = calibrate_eps(ctx, Xd, n)            # warm-up of the calibration kernels
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    eps, med, _ = calibrate_eps(ctx, Xd, n)
+    ev[1].record(stream)
+    scale = 1.0 / eps
+    g = api.rpcholesky(ctx, Xd, scale, k_max=k, block=1, seed=1234, precision="fp64")
+    ev[2].record(stream)
+    e = api.bistochastic_evd(ctx, g.factor, k_out=top)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    t_cal, t_rp, t_evd = (ev[i].elapsed_time(ev[i + 1]) / 1e3 for i in range(3))
+    U = e.U.cpu().numpy().astype(np.float64)
+    # FP64 oracle of the same low-rank pipeline
+    t0 = time.time()
+    ref = rpchol.rpcholesky(Xs.astype(np.float64), scale, k, 1, seed=1234)
+    eo = evd.evd_from_factor(ref["F"], top)
+    t_oracle = time.time() - t0
+    piv_equal = bool(np.array_equal(g.piv, ref["piv"]))
+    lam_rel = np.abs(e.lam[-top:] - eo["lam"][-top:]) / np.abs(eo["lam"][-top:])
+    # dense FP64 EVD (the reference's CPU path) on the host cores
+    t0 = time.time()
+    wd, Vd = dense.dense_evd(Xs.astype(np.float64), scale, top=top)
+    t_dense = time.time() - t0
+    lam_lr = e.lam[-top:][::-1]
+    Ul = U[:, ::-1]
+    c = np.abs(np.einsum("ij,ij->j", Ul, Vd)) / (np.linalg.norm(Ul, axis=0) * np.linalg.norm(Vd, axis=0))
+    ang = np.arccos(np.clip(c, 0.0, 1.0))
+    return {"workload": f"N={n}, d=64, eps by 41-value calibration, b=1, k={k}, top {top}, plain FP64",
+            "eps": eps, "median_sqdist": med,
+            "gpu_seconds": {"calibration": t_cal, "rpcholesky": t_rp, "evd": t_evd, "total": t_cal + t_rp + t_evd},
+            "rank": int(g.rank), "trace_error": float(g.trace_error),
+            "vs_oracle_same_draws": {"pivots_bit_exact": piv_equal,
+                                     "trace_error_rel": abs(g.trace_error - ref["err"][-1]) / ref["err"][-1],
+                                     "top_eig_rel_err_max": float(lam_rel.max()), "oracle_seconds": t_oracle},
+            "vs_dense": {"top_eig_abs_err_leading8": [float(x) for x in np.abs(lam_lr - wd)[:8]],
+                         "top_eig_abs_err_max": float(np.abs(lam_lr - wd).max()),
+                         "eigvec_angle_leading4_rad": [float(x) for x in ang[:4]],
+                         "lam_dense_leading4": [float(x) for x in wd[:4]]},
+            "cpu_dense_evd": {"seconds": t_dense, "cores": os.cpu_count(), "kind": "port",
+                              "what": "ks_reference.py dense FP64 EVD restated (blocked K, vector diagonals), "
+                                      "scipy eigh top 32",
+                              "openblas_threads": os.environ.get("OPENBLAS_NUM_THREADS", "default")}}
 
 
 def batched_phase(ctx, args):
@@ -428,19 +500,24 @@ def serving_phase(ctx, X, Xd, scale, args):
 
 
 def reference_arm(args, n_gpus):
+    """The CPU implementation of the pipeline (the FP64 NumPy/OpenBLAS oracle
+    port: stored-factor block RPCholesky + bistochastic EVD) on a row sample of
+    the workload with all host threads.  Its states come from the oracle's own
+    ETDRK4 generator (the reference generator's scheme, pinned to its output),
+    so this arm maps none of this repository's libraries."""
     ws, rank, _ = dist_info()
     if rank != 0:
         return
-    from oracle import baseline
-    X, _ = make_workload(args.n)
+    from oracle import baseline, calibrate, ks
+    n_s = min(args.cpu_rows, args.n)
+    X = ks.seeded_mode(max(n_s, min(args.n, 20_000)), M=64, L=22.0, seed=0, warm_time=1000.0,
+                       dt=0.25).astype(np.float32)
     # eps: the same procedure in NumPy on the first 20,000 states
-    from oracle import calibrate
     Xs = X[: min(args.n, 20_000)].astype(np.float64)
     med = calibrate.median_sqdist_exact(Xs)
     eps_s = calibrate.log_sweep(med, 41)
     T = calibrate.pair_sums(Xs, 1.0 / eps_s)
     eps = calibrate.select(eps_s, T, Xs.shape[0])[3]
-    n_s = min(args.cpu_rows, args.n)
     times = []
     for _ in range(max(1, args.steps)):
         t = baseline.timed_pipeline(X[:n_s], 1.0 / eps, args.k, args.b, args.kout)
@@ -452,9 +529,10 @@ def reference_arm(args, n_gpus):
               f"{os.environ.get('OPENBLAS_NUM_THREADS', 'default')}")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": n_gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic KS states (L=22, seed 0)",
-            "config": {"workload": f"block RPCholesky + bistochastic EVD, N={args.n}, d=64, k={args.k}, "
-                                   f"b={args.b}, top {args.kout}", "eps": eps},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic KS states (L=22, d=64, seed 0; oracle ETDRK4 generator)",
+            "config": workload_config(args, args.n, 64, n_gpus),
+            "calibration_eps": {"eps": eps, "median_sqdist": med, "calibration_rows": int(Xs.shape[0])},
             "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -648,6 +726,8 @@ def main():
 
     if args.cal_n > 0:
         phase("calibration", calibration_phase, ctx, Xd, args, (clocks or {}).get("sm_mhz"))
+    if not args.no_c1 and rank == 0:
+        phase("c1", c1_phase, ctx, X, args)
     # --- serving loop under load (after the timed regions; frees the step's buffers first)
     del F, U
     torch.cuda.empty_cache()
@@ -663,21 +743,23 @@ def main():
                 "warmup": args.warmup, "ms_per_step": val * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor / f64 pivot, diag, kxk",
                 "data": "synthetic KS states (L=22, d=64, seed 0; host ETDRK4 generator)",
-                "config": {"workload": f"block RPCholesky + bistochastic EVD, N={N}, d={d}, k={args.k}, "
-                                       f"b={args.b}, top {args.kout}, mixed precision",
-                           "eps": eps, "median_sqdist": med, "calibration_rows": n_cal,
-                           "block_autotune": {"chosen": int(tuned["block"]),
-                                              "ms_per_column": tuned["ms_per_column"]} if tuned else None,
-                           "l2": "inputs larger than L2 (X 512 MB, F 16 GB)",
-                           "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"},
-                "rank": int(fac.rank), "rounds": int(fac.rounds), "trace_error": fac.trace_error,
-                "lam_top": float(lam_mixed[-1]),
+                "config": workload_config(args, N, d, n_gpus),
                 "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(N * d * 4),
                         "d2h_bytes_per_step": int(N * args.kout * 4)},
                 "gpu_launches": int(launches // args.steps) * args.steps,
-                "roofline": roofline, "roofline_by_kernel": roof, "kernels": kernels,
-                "clocks": clocks, "cpu_baseline": cpu, "datagen_s": gen_s}
-        line.update(result)
+                "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu,
+                "calibration_eps": {"eps": eps, "median_sqdist": med, "calibration_rows": n_cal},
+                "block_autotune": {"chosen": int(tuned["block"]), "ms_per_column": tuned["ms_per_column"]}
+                if tuned else None,
+                "roofline_by_kernel": roof, "kernels": kernels, "datagen_s": gen_s}
+        # measurement blocks, then the accuracy of the timed run last (the end of
+        # the line is what a truncated log keeps)
+        for key in ("calibration", "batched", "serving", "c1"):
+            if key in result:
+                line[key] = result[key]
+        line["accuracy"] = {"rank": int(fac.rank), "rounds": int(fac.rounds), "trace_error": fac.trace_error,
+                            "lam_top": float(lam_mixed[-1]), "fp64": result.get("fp64"),
+                            "same_pivots_fp64": result.get("same_pivots_fp64")}
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:

@@ -77,6 +77,14 @@ int kevd_profile_read(kevd_ctx* ctx, int idx, char* name, int name_len,
                       double* total_ms, int64_t* count);
 int64_t kevd_launch_count(const kevd_ctx* ctx);
 
+/* Issue-rate probe for roofline denominators (no reference counterpart; a
+ * measurement aid).  kind 0: MUFU ex2 evaluations per second; 1: FP32 FMAs
+ * per second; 2: FP64 FMAs per second; 3: FP32 FMAs per second issued as
+ * packed pairs (fma.rn.f32x2, two per instruction); each from independent dependency
+ * chains over every SM, at the clock the GPU runs during the call.  ms: the
+ * best of three timed launches.  Synchronises the stream. */
+int kevd_peak_rate(kevd_ctx* ctx, int32_t kind, double* ops_per_s, double* ms, void* stream);
+
 /* ---- sample views ------------------------------------------------------ */
 
 /* Materialise the delay-embedded samples of the reference programs as rows.
@@ -114,15 +122,19 @@ int kevd_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                         const double* scales, int32_t n_scales, double* sums,
                         void* stream);
 
-/* kevd_calibrate for callers that cannot allocate device memory (inside a CUDA
- * graph capture or a stream callback, under a device-memory pool they do not
- * own, or after an allocation freeze).  No reference counterpart.  Needs no
- * context and allocates nothing: its scratch is a fixed device array of about
- * 160 KB that every GPU loading the library keeps until exit.  Limits:
- * n_scales <= 64 (KEVD_ERR_ARG beyond).  The first call on a device resolves
- * the array's device address with that device current, so make it before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race.
- * X: device; scales, sums: host. */
+/* kevd_calibrate for callers that cannot call cudaMalloc: a process whose
+ * device memory is fully reserved by a pool it does not own (another
+ * framework's caching allocator, or a host application that gives the plugin
+ * a fixed budget), or a service that forbids allocation once it has started.
+ * No reference counterpart.  Needs no context and allocates nothing: its
+ * scratch is a fixed device array of about 160 KB that every GPU loading the
+ * library keeps until exit.  Limits: n_scales <= 64 (KEVD_ERR_ARG beyond).
+ * The first call on a device (and on each further context of that device)
+ * resolves the array's device address with that device current; make that
+ * first call before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race.  The call synchronises the stream.  A CUDA error
+ * already pending on the calling thread is reported as KEVD_ERR_CUDA, left in
+ * place, and nothing is enqueued.  X: device; scales, sums: host. */
 int kevd_calibrate_noalloc(const float* X, int64_t N, int32_t d,
                            const double* scales, int32_t n_scales,
                            double* sums, void* stream);
@@ -165,9 +177,14 @@ int kevd_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
 
 typedef struct {
     int64_t k_max;          /* factor capacity (target rank)                 */
-    int32_t block;          /* proposals per round b, 1..64                   */
+    int32_t block;          /* proposals per round b, 1..512 (the reference's
+                               BLK; rounds accepting more than 64 columns
+                               update them in passes of 64)                   */
     int32_t max_rounds;     /* round limit                                    */
-    double tol;             /* rejection tolerance (reference: 1e-10)         */
+    double tol;             /* rejection tolerance (reference: 1e-10); the
+                               mixed form also rejects H_ii <= 16 x 2^-24 K_ii
+                               (FP32 rounding level of the factor) and stops
+                               once the trace error is at or below that level */
     double err_target;      /* stop once trace error <= this (0: never)       */
     uint64_t seed;          /* Philox key when uniforms == NULL               */
     const double* uniforms; /* host, optional: max_rounds x 2 x block draws in

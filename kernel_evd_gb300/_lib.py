@@ -85,6 +85,7 @@ SIGNATURES = {
     "kevd_profile_enable": (C.c_int, [_P, C.c_int]),
     "kevd_profile_read": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_int, C.POINTER(_D), C.POINTER(_I64)]),
     "kevd_launch_count": (_I64, [_P]),
+    "kevd_peak_rate": (C.c_int, [_P, _I32, C.POINTER(_D), C.POINTER(_D), _P]),
     "kevd_hankel_rows": (C.c_int, [_P, _P, _I64, _I64, _I64, _P, _P]),
     "kevd_kernel_block": (C.c_int, [_P, _P, _I64, _I32, _D, _P, _I64, _I64, _P, _I64, _I32, _P, _I64, _P]),
     "kevd_calibrate": (C.c_int, [_P, _P, _I64, _I32, _P, _I32, _P, _P]),

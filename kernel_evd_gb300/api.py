@@ -550,6 +550,15 @@ def profile_read(ctx: Context) -> dict:
     return out
 
 
+def peak_rate(ctx: Context, kind: str) -> dict:
+    """Measured issue rate: kind "ex2" (MUFU ex2/s), "fp32_fma", "fp64_fma" or
+    "fp32x2_fma" (FMA/s; the last issued as packed FP32 pairs)."""
+    k = {"ex2": 0, "fp32_fma": 1, "fp64_fma": 2, "fp32x2_fma": 3}[kind]
+    rate, ms = C.c_double(), C.c_double()
+    ctx._check(ctx.lib.kevd_peak_rate(ctx.h, k, C.byref(rate), C.byref(ms), _stream()))
+    return {"ops_per_s": rate.value, "ms": ms.value}
+
+
 def launch_count(ctx: Context) -> int:
     """Kernels launched by this library through ctx so far."""
     return int(ctx.lib.kevd_launch_count(ctx.h))

@@ -15,6 +15,8 @@
 // in a fixed order, so the result is deterministic.
 #include "kevd_internal.cuh"
 
+#include <cuda.h>
+
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -295,17 +297,18 @@ int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double*
 }
 
 // ---- calibration without allocation -------------------------------------
-// Some callers cannot allocate device memory at all: code running inside a
-// CUDA graph capture or another library's stream callback, processes whose
-// device memory is fully reserved by a pool they do not own, and hosts that
-// forbid allocation after start-up.  For them the pair-sum sweep has a variant
-// whose scratch (per-CTA FP64 partials, the device copy of the scales and the
-// reduced sums) lives in fixed file-scope device arrays instead of workspace
-// buffers.  Limits: at most kNaMaxScales scales per call and a grid of at most
-// kNaGrid CTAs (about 160 KB held by every GPU that loads the library, until
-// the process exits).  Each call overwrites every entry it reads, so no entry
-// has to start at zero; calls share the arrays, so calls that overlap on the
-// GPU (different streams, or several host threads) race.
+// Some callers cannot allocate device memory: processes whose device memory is
+// fully reserved by a pool they do not own (another framework's caching
+// allocator, a host application that hands the plugin a fixed budget), and
+// services that forbid allocation once they have started.  For them the
+// pair-sum sweep has a variant whose scratch (per-CTA FP64 partials, the
+// device copy of the scales and the reduced sums) lives in fixed file-scope
+// device arrays instead of workspace buffers.  Limits: at most kNaMaxScales
+// scales per call and a grid of at most kNaGrid CTAs (about 160 KB held by
+// every GPU that loads the library, until the process exits).  Each call
+// overwrites every entry it reads, so no entry has to start at zero; calls
+// share the arrays, so calls that overlap on the GPU (different streams, or
+// several host threads) race.
 constexpr int kNaMaxScales = 64;
 constexpr int kNaGrid = 304;
 static __device__ __align__(256) double g_na_partial[kNaGrid * kNaMaxScales];
@@ -318,30 +321,49 @@ struct NoAllocScratch {
     double* sums = nullptr;
 };
 
-// Device addresses of the arrays, resolved once per device with that device
-// current (a host-side use of the symbols would be a host stand-in, not a
-// device address).
+// The current CUDA context, through the driver entry point (no link against
+// the driver library): the module holding the arrays is loaded once per
+// context, so their device addresses are only valid in the context that
+// resolved them.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+static CtxGetCurrentFn ctx_get_current() {
+    static const CtxGetCurrentFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            return reinterpret_cast<CtxGetCurrentFn>(p);
+        return (CtxGetCurrentFn) nullptr;
+    }();
+    return fn;
+}
+
+// Device addresses of the arrays, resolved with cudaGetSymbolAddress once per
+// device and context, with that device current (a host-side use of the
+// symbols is a host stand-in, not a device address).  A caller that switches
+// to another context on the same device (cuCtxCreate) gets them resolved
+// again for that context.
 static int noalloc_scratch(NoAllocScratch* out) {
     constexpr int kMaxDevices = 64;
     static std::mutex mu;
-    static bool ready[kMaxDevices] = {};
+    static CUcontext owner[kMaxDevices] = {};
     static NoAllocScratch table[kMaxDevices];
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        cudaGetLastError();
-        return KEVD_ERR_CUDA;
-    }
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return KEVD_ERR_CUDA;
+    CUcontext cur = nullptr;
+    const CtxGetCurrentFn get = ctx_get_current();
+    if (get && get(&cur) != CUDA_SUCCESS) cur = nullptr;
     std::lock_guard<std::mutex> lock(mu);
-    if (!ready[dev]) {
+    if (owner[dev] == nullptr || owner[dev] != cur) {
         NoAllocScratch t;
         if (cudaGetSymbolAddress((void**)&t.partial, g_na_partial) != cudaSuccess ||
             cudaGetSymbolAddress((void**)&t.scales, g_na_scales) != cudaSuccess ||
-            cudaGetSymbolAddress((void**)&t.sums, g_na_sums) != cudaSuccess) {
-            cudaGetLastError();
+            cudaGetSymbolAddress((void**)&t.sums, g_na_sums) != cudaSuccess)
             return KEVD_ERR_CUDA;
-        }
+        // the first symbol access made the context current if none was
+        if (get && cur == nullptr && get(&cur) != CUDA_SUCCESS) cur = nullptr;
         table[dev] = t;
-        ready[dev] = true;
+        owner[dev] = cur;
     }
     *out = table[dev];
     return KEVD_OK;
@@ -353,15 +375,23 @@ int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales
         return KEVD_ERR_ARG;
     for (int j = 0; j < n_scales; ++j)
         if (!(scales[j] > 0.0)) return KEVD_ERR_ARG;
+    // An error left pending by earlier work on this thread would make this
+    // call's launch check ambiguous: report it and leave it in place.
+    if (cudaPeekAtLastError() != cudaSuccess) return KEVD_ERR_CUDA;
     NoAllocScratch sc;
-    const int rc = noalloc_scratch(&sc);
-    if (rc != KEVD_OK) return rc;
+    if (noalloc_scratch(&sc) != KEVD_OK) {
+        cudaGetLastError();   // this call's own failure
+        return KEVD_ERR_CUDA;
+    }
     float hc[kNaMaxScales];
     for (int j = 0; j < n_scales; ++j) hc[j] = (float)(scales[j] * 1.4426950408889634);
     const int64_t nt = (N + kCalTile - 1) / kCalTile;
     const int64_t n_tiles = nt * (nt + 1) / 2;
     const int grid = (int)std::min<int64_t>(n_tiles, kNaGrid);
     const size_t smem = calib_smem(d);
+    // hc lives on this stack frame: the copy is complete (pageable source) or
+    // staged before cudaMemcpyAsync returns, and the stream is synchronised
+    // below before the frame goes away
     if (cudaMemcpyAsync(sc.scales, hc, n_scales * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         raise_smem_limit(reinterpret_cast<const void*>(&calibrate_tiles_kernel), (int)smem) !=
             cudaSuccess) {
@@ -370,10 +400,10 @@ int run_calibrate_noalloc(const float* X, int64_t N, int d, const double* scales
     }
     calibrate_tiles_kernel<<<grid, 256, smem, s>>>(X, N, d, sc.scales, n_scales, n_tiles, sc.partial);
     reduce_partials_kernel<<<1, kCalMaxScales, 0, s>>>(sc.partial, grid, n_scales, sc.sums);
-    if (cudaGetLastError() != cudaSuccess ||
+    if (cudaPeekAtLastError() != cudaSuccess ||
         cudaMemcpyAsync(sums, sc.sums, n_scales * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
+        cudaGetLastError();   // nothing was pending on entry: the error is this call's
         return KEVD_ERR_CUDA;
     }
     return KEVD_OK;

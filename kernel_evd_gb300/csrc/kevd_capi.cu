@@ -188,6 +188,11 @@ int kevd_profile_read(kevd_ctx* ctx, int idx, char* name, int name_len, double* 
 
 int64_t kevd_launch_count(const kevd_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int kevd_peak_rate(kevd_ctx* ctx, int32_t kind, double* ops_per_s, double* ms, void* stream) {
+    KEVD_CHECK_CTX(ctx);
+    return run_peak_rate(ctx, kind, ops_per_s, ms, as_stream(stream));
+}
+
 int kevd_hankel_rows(kevd_ctx* ctx, const float* u, int64_t Ndata, int64_t M, int64_t Nq, float* X,
                      void* stream) {
     KEVD_CHECK_CTX(ctx);

@@ -222,6 +222,7 @@ int run_ks_generate(kevd_ctx* ctx, int32_t n_traj, int32_t M, int32_t precision,
                     float* const* out, cudaStream_t s);
 int run_weighted_gram2(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k, int64_t ldF,
                        const double* s_dev, const double* s2_dev, double* G, double* G2, cudaStream_t st);
+int run_peak_rate(kevd_ctx* ctx, int kind, double* rate, double* ms, cudaStream_t s);
 int run_gather_rows(kevd_ctx* ctx, const void* F, int precision, int64_t ldF, const int64_t* idx,
                     int64_t n, int64_t ncols, double* out, cudaStream_t s);
 

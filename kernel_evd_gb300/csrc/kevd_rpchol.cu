@@ -29,18 +29,31 @@
 
 namespace kevd {
 
-bool update_tc_supported(const float* F, int64_t ldF, int d, int b);
+bool update_tc_supported(const float* F, int64_t ldF, int d);
 int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_max, const float* X, int d,
                      double scale, const int64_t* sacc, const float* minv_f, int b, const void* round_state,
                      double* dvec, double* dblk, int* err, cudaStream_t s);
 
 constexpr int kRowBlock = 128;   // rows per update CTA (= rows per d partial sum)
-constexpr int kMaxBlock = 64;    // proposals per round supported by the SIMT update
+constexpr int kMaxBlock = 512;   // proposals per round (the reference's default BLK, ks_arpclm.cu:38)
+constexpr int kGroup = 64;       // accepted columns per update pass: a round with more runs several passes
+constexpr int kSmallBlock = 64;  // rounds up to this size factor their block in shared memory
 constexpr int kFactorThreads = 256;   // rp_factor_kernel: 16 x 16 threads over the trailing update
-static_assert(kFactorThreads == 256 && kMaxBlock * kMaxBlock % kFactorThreads == 0, "factor thread layout");
+constexpr int kBigFactorThreads = 1024;   // rp_factor_big_kernel: 32 x 32 threads
+static_assert(kFactorThreads == 256 && kSmallBlock * kSmallBlock % kFactorThreads == 0, "factor thread layout");
 constexpr int kColChunk = 32;    // F columns per hgram CTA
 constexpr int kFeat = 64;        // features staged at a time by the SIMT update
 constexpr int kSampleThreads = 1024;
+
+// Acceptance floor of the mixed form, relative to K(S',S')_ii (= 1 for the
+// Gaussian kernel).  In the mixed form H = K(S',S') - F(S',:) F(S',:)^T is
+// formed from the FP32 factor, whose rounding leaves noise of a few 1e-7 in
+// H_ii; a proposal whose H_ii is at that level would be accepted on noise and
+// give a column of noise / sqrt(noise).  The mixed form therefore rejects
+// H_ii <= 16 u32 K_ii (u32 = 2^-24, about 9.5e-7) and stops once the trace
+// error, the mean residual diagonal, has fallen below the same level.  The
+// FP64 form keeps the reference's tolerance alone (ks_arpclm.cu:329-331).
+constexpr double kMixedFloor = 16.0 / 16777216.0;
 
 struct RoundState {
     int64_t rank;    // columns of F written
@@ -90,7 +103,7 @@ rp_sample_kernel(const double* __restrict__ d, const double* __restrict__ dblk, 
                  int64_t nblk, int round, int b, uint64_t seed,
                  const double* __restrict__ uniforms, int64_t* __restrict__ props,
                  RoundState* st, int64_t k_max, int max_rounds, double err_target,
-                 double* __restrict__ err) {
+                 double err_floor, double* __restrict__ err) {
     __shared__ double incl[kSampleThreads];
     __shared__ int s_stop;
     if (st->done) return;
@@ -113,7 +126,8 @@ rp_sample_kernel(const double* __restrict__ d, const double* __restrict__ dblk, 
         if (round > 0) err[round - 1] = e;
         st->total = total;
         const bool stop = (round >= max_rounds) || (st->rank >= k_max) ||
-                          (err_target > 0.0 && round > 0 && e <= err_target);
+                          (err_target > 0.0 && round > 0 && e <= err_target) ||
+                          (err_floor > 0.0 && round > 0 && e <= err_floor);
         if (stop) {
             st->done = 1;
             st->rounds = round;
@@ -192,6 +206,13 @@ rp_sample_kernel(const double* __restrict__ d, const double* __restrict__ dblk, 
 }
 
 // ---- proposal block: F(S',c-chunk) F(S',c-chunk)^T and K(S',S') -----------
+constexpr int kHgramStageRows = 128;
+template <typename T>
+static size_t hgram_smem(int b) {
+    const size_t f = (size_t)b * (kColChunk + 1) * sizeof(T);
+    const size_t x = b <= kHgramStageRows ? (size_t)b * 129 * sizeof(float) : 0;
+    return std::max(f, x);
+}
 template <typename T>
 __global__ void __launch_bounds__(256)
 rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ X, int d,
@@ -199,8 +220,7 @@ rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ 
                 const RoundState* st, double* __restrict__ hpart, double* __restrict__ kss) {
     if (st->done) return;
     // one buffer, used either for an F column chunk or for the X rows of S'
-    __shared__ __align__(16) unsigned char raw[kMaxBlock * 129 * sizeof(float)];
-    static_assert(kMaxBlock * (kColChunk + 1) * sizeof(double) <= sizeof(raw), "hgram smem");
+    extern __shared__ __align__(16) unsigned char raw[];
     T* fs = reinterpret_cast<T*>(raw);
     float* xs = reinterpret_cast<float*>(raw);
     const int tid = threadIdx.x;
@@ -226,9 +246,10 @@ rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ 
         // K(S', S') in FP64, rows split over the remaining CTAs
         const int nk = gridDim.x - n_split;
         const int part = blockIdx.x - n_split;
-        // rows of S' staged in shared memory up to 128 features, read from
-        // global memory (L2-resident, b rows) beyond; same summation order
-        const bool staged = d <= 128;
+        // rows of S' staged in shared memory up to 128 features and 128
+        // proposals, read from global memory (L2-resident, b rows) beyond;
+        // same summation order
+        const bool staged = d <= 128 && b <= kHgramStageRows;
         if (staged)
             for (int e = tid; e < b * d; e += 256) {
                 const int p = e / d, k = e - p * d;
@@ -264,7 +285,7 @@ rp_hgram_kernel(const T* __restrict__ F, int64_t ldF, const float* __restrict__ 
 __global__ void __launch_bounds__(256)
 rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpart, int b,
                  int round, uint64_t seed, const double* __restrict__ uniforms, double tol,
-                 int64_t k_max, const int64_t* __restrict__ props, RoundState* st,
+                 double floor_rel, int64_t k_max, const int64_t* __restrict__ props, RoundState* st,
                  double* __restrict__ minv, float* __restrict__ minv_f,
                  int64_t* __restrict__ sacc, int64_t* __restrict__ piv,
                  int32_t* __restrict__ hm) {
@@ -272,9 +293,10 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
     extern __shared__ double H[];         // b x b, the b x b inverse being formed, the compacted factor
     double* MS = H + b * b;
     double* LC = MS + b * b;
-    __shared__ double H0[kMaxBlock];
-    __shared__ double us[kMaxBlock];      // the round's acceptance uniforms
-    __shared__ int accpos[kMaxBlock];
+    __shared__ double H0[kSmallBlock];
+    __shared__ double us[kSmallBlock];    // the round's acceptance uniforms
+    __shared__ double kfl[kSmallBlock];   // acceptance floor per proposal (0 in the FP64 form)
+    __shared__ int accpos[kSmallBlock];
     __shared__ int s_dec, s_m;
     const int tid = threadIdx.x;
     const int64_t r = st->rank;
@@ -283,7 +305,7 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
         // 256 threads x 16 elements (b <= 64): the 16 chains of a thread advance
         // together over the column chunks, so 16 loads are in flight per step;
         // each element still subtracts its chunks in increasing order
-        constexpr int kPer = kMaxBlock * kMaxBlock / 256;
+        constexpr int kPer = kSmallBlock * kSmallBlock / 256;
         double v[kPer];
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
@@ -307,6 +329,7 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
     __syncthreads();
     for (int p = tid; p < b; p += blockDim.x) {
         H0[p] = H[p * b + p];
+        kfl[p] = floor_rel * kss[p * b + p];
         us[p] = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + p] : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)p);
     }
     if (tid == 0) s_m = 0;
@@ -317,7 +340,7 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
         if (tid == 0) {
             const double u = us[i];
             const double hii = H[i * b + i];
-            const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol);
+            const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol) && (hii > kfl[i]);
             s_dec = acc;
             if (acc) accpos[s_m++] = i;
         }
@@ -371,9 +394,113 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
     }
 }
 
+// Accept / reject, Cholesky and inverse for 64 < b <= kMaxBlock: the steps and
+// the per-element operation order of rp_factor_kernel, with H, the compacted
+// factor LC and the inverse MS in a global workspace (b^2 doubles each,
+// L2-resident) instead of shared memory, and 32 x 32 threads over the
+// trailing update.  __syncthreads orders the CTA's global accesses as it does
+// its shared ones.
+__global__ void __launch_bounds__(kBigFactorThreads)
+rp_factor_big_kernel(const double* __restrict__ kss, const double* __restrict__ hpart, int b,
+                     int round, uint64_t seed, const double* __restrict__ uniforms, double tol,
+                     double floor_rel, int64_t k_max, const int64_t* __restrict__ props, RoundState* st,
+                     double* __restrict__ minv, float* __restrict__ minv_f,
+                     int64_t* __restrict__ sacc, int64_t* __restrict__ piv,
+                     int32_t* __restrict__ hm, double* H, double* MS, double* LC) {
+    if (st->done) return;
+    __shared__ double H0[kMaxBlock];
+    __shared__ double us[kMaxBlock];
+    __shared__ double kfl[kMaxBlock];
+    __shared__ int accpos[kMaxBlock];
+    __shared__ int s_dec, s_m;
+    const int tid = threadIdx.x;
+    const int nt = blockDim.x;
+    const int64_t r = st->rank;
+    const int nz = (int)((r + kColChunk - 1) / kColChunk);
+    for (int e = tid; e < b * b; e += nt) {
+        double v = kss[e];
+        for (int z = 0; z < nz; ++z) v -= hpart[(int64_t)z * b * b + e];
+        H[e] = v;
+    }
+    __syncthreads();
+    for (int p = tid; p < b; p += nt) {
+        H0[p] = H[p * b + p];
+        kfl[p] = floor_rel * kss[p * b + p];
+        us[p] = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + p] : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)p);
+    }
+    if (tid == 0) s_m = 0;
+    __syncthreads();
+    const int64_t cap = k_max - r;
+    for (int i = 0; i < b; ++i) {
+        __syncthreads();
+        if (tid == 0) {
+            const double u = us[i];
+            const double hii = H[i * b + i];
+            const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol) && (hii > kfl[i]);
+            s_dec = acc;
+            if (acc) accpos[s_m++] = i;
+        }
+        __syncthreads();
+        if (s_dec) {
+            const double f = 1.0 / sqrt(H[i * b + i]);
+            __syncthreads();
+            for (int j = i + tid; j < b; j += nt) H[j * b + i] *= f;
+            __syncthreads();
+            for (int jj = i + 1 + (tid >> 5); jj < b; jj += 32)
+                for (int kk = i + 1 + (tid & 31); kk <= jj; kk += 32) H[jj * b + kk] -= H[jj * b + i] * H[kk * b + i];
+            __syncthreads();
+        }
+    }
+    const int nacc = s_m;
+    for (int e = tid; e < b * b; e += nt) {
+        MS[e] = 0.0;
+        const int a = e / b, c = e - a * b;
+        LC[e] = (a < nacc && c < nacc) ? H[accpos[a] * b + accpos[c]] : 0.0;
+    }
+    __syncthreads();
+    if (tid < nacc) {
+        const int t = tid;
+        MS[t * b + t] = 1.0 / LC[t * b + t];
+        for (int a = t + 1; a < nacc; ++a) {
+            const double* la = LC + a * b;
+            double sum = 0.0;
+            for (int e = t; e < a; ++e) sum += la[e] * MS[e * b + t];
+            MS[a * b + t] = -sum / la[a];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < b * b; e += nt) {
+        minv[e] = MS[e];
+        minv_f[e] = (float)MS[e];
+    }
+    if (tid < nacc) {
+        const int64_t sp = props[accpos[tid]];
+        sacc[tid] = sp;
+        piv[r + tid] = sp;
+    }
+    if (tid == 0) {
+        st->r_old = r;
+        st->nacc = nacc;
+        st->rank = r + nacc;
+        hm[round] = nacc;
+    }
+}
+
 // ---- residual update over all row blocks -----------------------------------
 // CTA = 128 rows x up to 64 accepted columns; thread (ty, tx) of 16 x 16 owns
 // rows ty + 16i (i < 8) and columns tx + 16j (j < 4).
+//
+// A round that accepts more than 64 columns is updated in passes of 64
+// (group g = columns r + 64g ...).  With L_i = [[L00, 0], [L10, L11]] the new
+// columns satisfy G0 = T0 L00^{-T} and G1 = (T1 - G0 L10^T) L11^{-T}; pass g
+// therefore runs the one-group update against the factor's first r + 64g
+// columns (which include the previous passes' output, whose rows at S_g are
+// L10) with the pivots of group g and the diagonal block g of L_i^{-1}.
+__device__ __forceinline__ bool group_view(int64_t r_old, int nacc_all, int group, int64_t& r, int& nacc) {
+    r = r_old + (int64_t)kGroup * group;
+    nacc = min(kGroup, nacc_all - kGroup * group);
+    return nacc > 0;
+}
 template <typename T>
 struct UpdSmem {
     static constexpr int KC = 32;
@@ -384,25 +511,31 @@ __global__ void __launch_bounds__(256)
 rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, int64_t N, int d,
                  double scale, const int64_t* __restrict__ sacc, const double* __restrict__ minv,
                  const float* __restrict__ minv_f, int b, const RoundState* st,
-                 double* __restrict__ dvec, double* __restrict__ dblk) {
+                 double* __restrict__ dvec, double* __restrict__ dblk, int group) {
     if (st->done) return;
-    const int nacc = st->nacc;
-    if (nacc == 0) return;
-    const int64_t r = st->r_old;
+    int64_t r;
+    int nacc;
+    if (!group_view(st->r_old, st->nacc, group, r, nacc)) return;
+    {   // this pass's pivots and diagonal block of L_i^{-1} (leading dimension b)
+        const int64_t o = (int64_t)kGroup * group;
+        sacc += o;
+        minv += o * b + o;
+        minv_f += o * b + o;
+    }
     constexpr int KC = UpdSmem<T>::KC;
     extern __shared__ __align__(16) unsigned char smraw[];
     // region 1 (phase A: X rows, kFeat features at a time; phase B: F tiles),
     // then Tm, then Minv
     constexpr int dp = kFeat + 1;
-    const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
-    const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (KC + 1) * sizeof(T);
+    const size_t reg1_a = (size_t)(kRowBlock + kGroup) * dp * sizeof(float);
+    const size_t reg1_b = (size_t)(kRowBlock + kGroup) * (KC + 1) * sizeof(T);
     const size_t reg1 = (reg1_a > reg1_b ? reg1_a : reg1_b + 0);
     float* xr = reinterpret_cast<float*>(smraw);
     float* xs = xr + kRowBlock * dp;
     T* At = reinterpret_cast<T*>(smraw);
     T* Bt = At + kRowBlock * (KC + 1);
     T* Tm = reinterpret_cast<T*>(smraw + ((reg1 + 15) / 16) * 16);   // 128 x (64+1)
-    T* Mv = Tm + kRowBlock * (kMaxBlock + 1);                         // 64 x (64+1)
+    T* Mv = Tm + kRowBlock * (kGroup + 1);                         // 64 x (64+1)
     __shared__ double rowsq_s[kRowBlock];
 
     const int tid = threadIdx.x;
@@ -413,7 +546,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
     // phase A: K(R, S_i) into Tm
     for (int e = tid; e < nacc * nacc; e += 256) {
         const int a = e / nacc, q = e - a * nacc;
-        Mv[a * (kMaxBlock + 1) + q] = sizeof(T) == 8 ? (T)minv[a * b + q] : (T)minv_f[a * b + q];
+        Mv[a * (kGroup + 1) + q] = sizeof(T) == 8 ? (T)minv[a * b + q] : (T)minv_f[a * b + q];
     }
     {
         T acc[8][4];
@@ -438,7 +571,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
 #pragma unroll
                 for (int i = 0; i < 8; ++i) vr[i] = (T)xr[(ty + 16 * i) * dp + k];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) vs[j] = (T)xs[min(tx + 16 * j, kMaxBlock - 1) * dp + k];
+                for (int j = 0; j < 4; ++j) vs[j] = (T)xs[min(tx + 16 * j, kGroup - 1) * dp + k];
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -458,7 +591,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
                     if (sizeof(T) == 8) kv = (T)exp(-scale * (double)acc[i][j]);
                     else kv = (T)kexp_scaled((float)acc[i][j], split_scale(scale));
                 }
-                Tm[(ty + 16 * i) * (kMaxBlock + 1) + c] = kv;
+                Tm[(ty + 16 * i) * (kGroup + 1) + c] = kv;
             }
     }
     __syncthreads();
@@ -475,7 +608,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
             const int rr = e / KC, c = e - rr * KC;
             At[rr * (KC + 1) + c] = (rr < nrows && c < nc) ? F[(row0 + rr) * ldF + c0 + c] : (T)0;
         }
-        for (int e = tid; e < kMaxBlock * KC; e += 256) {
+        for (int e = tid; e < kGroup * KC; e += 256) {
             const int q = e / KC, c = e - q * KC;
             Bt[q * (KC + 1) + c] = (q < nacc && c < nc) ? F[sacc[q] * ldF + c0 + c] : (T)0;
         }
@@ -498,7 +631,7 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) Tm[(ty + 16 * i) * (kMaxBlock + 1) + tx + 16 * j] -= acc[i][j];
+        for (int j = 0; j < 4; ++j) Tm[(ty + 16 * i) * (kGroup + 1) + tx + 16 * j] -= acc[i][j];
     __syncthreads();
     // phase D: G = Tm Minv^T
     T g[8][4];
@@ -509,11 +642,11 @@ rp_update_kernel(T* __restrict__ F, int64_t ldF, const float* __restrict__ X, in
     for (int e = 0; e < nacc; ++e) {
         T vt[8], vm[4];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) vt[i] = Tm[(ty + 16 * i) * (kMaxBlock + 1) + e];
+        for (int i = 0; i < 8; ++i) vt[i] = Tm[(ty + 16 * i) * (kGroup + 1) + e];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int a = tx + 16 * j;
-            vm[j] = (a < nacc) ? Mv[a * (kMaxBlock + 1) + e] : (T)0;
+            vm[j] = (a < nacc) ? Mv[a * (kGroup + 1) + e] : (T)0;
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i)
@@ -557,11 +690,11 @@ template <typename T>
 static size_t update_smem(int d) {
     (void)d;
     const int dp = kFeat + 1;
-    const size_t reg1_a = (size_t)(kRowBlock + kMaxBlock) * dp * sizeof(float);
-    const size_t reg1_b = (size_t)(kRowBlock + kMaxBlock) * (UpdSmem<T>::KC + 1) * sizeof(T);
+    const size_t reg1_a = (size_t)(kRowBlock + kGroup) * dp * sizeof(float);
+    const size_t reg1_b = (size_t)(kRowBlock + kGroup) * (UpdSmem<T>::KC + 1) * sizeof(T);
     const size_t reg1 = ((std::max(reg1_a, reg1_b) + 15) / 16) * 16;
-    return reg1 + (size_t)kRowBlock * (kMaxBlock + 1) * sizeof(T) +
-           (size_t)kMaxBlock * (kMaxBlock + 1) * sizeof(T);
+    return reg1 + (size_t)kRowBlock * (kGroup + 1) * sizeof(T) +
+           (size_t)kGroup * (kGroup + 1) * sizeof(T);
 }
 
 template <typename T>
@@ -570,6 +703,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                        double* err_h, int32_t* hm_h, kevd_rpchol_result* res, cudaStream_t s,
                        RpcholDeferred* defer = nullptr) {
     const int b = p->block;
+    const double floor_rel = sizeof(T) == 4 ? kMixedFloor : 0.0;
     const int64_t nblk = (N + kRowBlock - 1) / kRowBlock;
     const int n_split = (int)((p->k_max + kColChunk - 1) / kColChunk);
     const int n_kss = 8;
@@ -597,13 +731,23 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     rp_init_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dvec, dblk, N, nblk, rs);
     KEVD_LAUNCH(ctx);
 
-    const size_t fsm = (size_t)3 * b * b * sizeof(double);
-    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_factor_kernel), (int)std::max(fsm, (size_t)1024)));
+    const bool big = b > kSmallBlock;
+    const size_t fsm = big ? 0 : (size_t)3 * b * b * sizeof(double);
+    double* hbig = nullptr;   // H, the compacted factor and the inverse of a large block
+    if (big) {
+        hbig = arena_get<double>(ctx, "rp.hbig", (size_t)3 * b * b, &st);
+        if (st != KEVD_OK) return st;
+    } else {
+        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_factor_kernel), (int)std::max(fsm, (size_t)1024)));
+    }
+    const size_t hsm = hgram_smem<T>(b);
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_hgram_kernel<T>), (int)hsm));
+    const int n_groups = (b + kGroup - 1) / kGroup;
     const size_t usm = update_smem<T>(d);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_update_kernel<T>), (int)usm));
     int* done_h = static_cast<int*>(ctx->pinned);
     // FP32 factors take the tensor-core residual update when the layout allows TMA
-    const bool use_tc = sizeof(T) == 4 && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d, b);
+    const bool use_tc = sizeof(T) == 4 && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d);
     int* tc_err = arena_get<int>(ctx, "rp.tcerr", 1, &st);
     if (st != KEVD_OK) return st;
     KEVD_CUDA(ctx, cudaMemsetAsync(tc_err, 0, sizeof(int), s));
@@ -613,19 +757,26 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
             ProfScope ps(ctx, "rp_sample", s);
             rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, round, b, p->seed,
                                                           unif, props, rs, p->k_max, p->max_rounds,
-                                                          p->err_target, err);
+                                                          p->err_target, floor_rel, err);
             KEVD_LAUNCH(ctx);
         }
         {
             ProfScope ps(ctx, "rp_hgram", s);
-            rp_hgram_kernel<T><<<n_split + n_kss, 256, 0, s>>>(F, ldF, X, d, scale, props, b,
-                                                             n_split, rs, hpart, kss);
+            rp_hgram_kernel<T><<<n_split + n_kss, 256, hsm, s>>>(F, ldF, X, d, scale, props, b,
+                                                               n_split, rs, hpart, kss);
             KEVD_LAUNCH(ctx);
         }
         {
             ProfScope ps(ctx, "rp_factor", s);
-            rp_factor_kernel<<<1, kFactorThreads, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
-                                                 p->k_max, props, rs, minv, minv_f, sacc, piv, hm);
+            if (big)
+                rp_factor_big_kernel<<<1, kBigFactorThreads, 0, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
+                                                                      floor_rel, p->k_max, props, rs, minv, minv_f,
+                                                                      sacc, piv, hm, hbig, hbig + (size_t)b * b,
+                                                                      hbig + (size_t)2 * b * b);
+            else
+                rp_factor_kernel<<<1, kFactorThreads, fsm, s>>>(kss, hpart, b, round, p->seed, unif, p->tol,
+                                                                floor_rel, p->k_max, props, rs, minv, minv_f, sacc,
+                                                                piv, hm);
             KEVD_LAUNCH(ctx);
         }
         if (use_tc) {
@@ -633,9 +784,11 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
                                       minv_f, b, rs, dvec, dblk, tc_err, s));
         } else {
             ProfScope ps(ctx, "rp_update", s);
-            rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv,
-                                                           minv_f, b, rs, dvec, dblk);
-            KEVD_LAUNCH(ctx);
+            for (int g = 0; g < n_groups; ++g) {
+                rp_update_kernel<T><<<(int)nblk, 256, usm, s>>>(F, ldF, X, N, d, scale, sacc, minv,
+                                                               minv_f, b, rs, dvec, dblk, g);
+                KEVD_LAUNCH(ctx);
+            }
         }
         if (!defer && (round & 3) == 3) {
             KEVD_CUDA(ctx, cudaMemcpyAsync(done_h, &rs->done, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -646,7 +799,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     // closing sampler call: records the last round's error and the stop
     rp_sample_kernel<<<1, kSampleThreads, 0, s>>>(dvec, dblk, N, nblk, std::min(round, p->max_rounds),
                                                   0, p->seed, unif, props, rs, p->k_max,
-                                                  std::min(round, p->max_rounds), p->err_target, err);
+                                                  std::min(round, p->max_rounds), p->err_target, floor_rel, err);
     KEVD_LAUNCH(ctx);
     if (defer) {
         // capture-safe: results go to pinned host memory, read after the stream completes

@@ -451,7 +451,7 @@ int kevd_server_submit_factorization(kevd_server* s, const float* X, int64_t N, 
                                      int64_t k, int32_t block, int32_t k_out, uint64_t seed, int32_t precision,
                                      int64_t* request_id) {
     if (!s || !X || !request_id || N < 2 || d < 1 || d > kMaxFeatures || !(scale > 0.0) || k < 1 || k > N || block < 1 ||
-        block > 64 || k_out < 1 || k_out > kQueryMaxOut || k_out > k ||
+        block > 512 || k_out < 1 || k_out > kQueryMaxOut || k_out > k ||
         (precision != KEVD_FP64 && precision != KEVD_MIXED))
         return KEVD_ERR_ARG;
     const size_t footprint = factorization_footprint(N, d, k, k_out, precision);

@@ -10,12 +10,13 @@
 //
 // Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
 // lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
-// stage accumulates hi_a hi_b + lo_a hi_b and, in a second accumulator,
-// hi_a lo_b; every two stages use a fresh TMEM partial (16 MMA updates), and
-// the epilogue sums the partials in FP32 registers with round-to-nearest, so
-// the tensor-core accumulator's rounding bias never builds up over r.  (Four
-// stages per partial are 10 % faster at N = 2M, k = 2000 but leave a top-32
-// eigenvalue error of 2e-8 against FP64 on the same pivots; two leave 1.2e-8.)
+// stage accumulates hi_a hi_b in one accumulator and the two small terms
+// hi_a lo_b + lo_a hi_b in a second one; every stage uses a fresh TMEM partial
+// (four MMA updates of the large accumulator), and the epilogue sums the
+// partials in FP32 registers with round-to-nearest, so the tensor-core
+// accumulator's one-sided rounding never builds up over r.  (Measured top-32
+// eigenvalue error against FP64 on the same pivots at N = 2M, k = 2000: four
+// stages per partial 2.0e-8, two 1.2e-8, one 8.2e-9 at 5 % more update time.)
 //
 // CTA (448 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
@@ -60,17 +61,17 @@ constexpr int kKs = 32;             // F columns per stage
 #define KEVD_UPD_BUFS 2
 #endif
 #ifndef KEVD_UPD_PER_PARTIAL
-#define KEVD_UPD_PER_PARTIAL 2
+#define KEVD_UPD_PER_PARTIAL 1
 #endif
 constexpr int kStages = KEVD_UPD_STAGES;
 constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
 constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of kPartCols columns
 constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulated per TMEM partial
 // A partial buffer holds two 64-column accumulators side by side: columns
-// [0,64) take hi_a hi_b + lo_a hi_b, columns [64,128) take hi_a lo_b (one
+// [0,64) take hi_a hi_b, columns [64,128) take hi_a lo_b + lo_a hi_b (one
 // N = 128 MMA against the b-hi and b-lo tiles, which lie back to back in
-// shared memory as one 128-row operand, plus one N = 64 MMA: 8 MMAs per stage
-// instead of 12)
+// shared memory as one 128-row operand, plus one N = 64 MMA into the second
+// half: 8 MMAs per stage instead of 12)
 constexpr int kPartCols = 2 * kCols;
 static_assert((kBufs & (kBufs - 1)) == 0 && (kPerPartial & (kPerPartial - 1)) == 0,
               "partial-buffer count and stages per partial are powers of two");
@@ -113,15 +114,25 @@ struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
     double total;
 };
 
+// Update pass g of a round that accepted more than kCols columns: columns
+// r_old + kCols g .. against the factor's first r_old + kCols g columns (the
+// same split as the SIMT update in kevd_rpchol.cu).  False when the pass has
+// no column.
+__device__ __forceinline__ bool pass_view(const RoundView* st, int group, int64_t& r, int& nacc) {
+    if (st->done) return false;
+    r = st->r_old + (int64_t)kCols * group;
+    nacc = min(kCols, st->nacc - kCols * group);
+    return nacc > 0;
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmk,
                  float* __restrict__ F, int64_t ldF, int64_t N, const float* __restrict__ minv_f, int b,
                  const uint8_t* __restrict__ bprep, const RoundView* st, double* __restrict__ dvec,
-                 double* __restrict__ dblk, int* __restrict__ err) {
-    if (st->done) return;
-    const int nacc = st->nacc;
-    if (nacc == 0) return;
-    const int64_t r = st->r_old;
+                 double* __restrict__ dblk, int* __restrict__ err, int group) {
+    int64_t r;
+    int nacc;
+    if (!pass_view(st, group, r, nacc)) return;
     const int n_st = (int)((r + kKs - 1) / kKs);
     const int64_t nblk = (N + kRows - 1) / kRows;
 
@@ -250,9 +261,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     tc::tc_fence_after();
 #pragma unroll
                     for (int j = 0; j < kKs / 8; ++j) {
-                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the first half
+                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the
+                        // second half, so the first half takes one (large) update per
+                        // k-step and the small terms accumulate at their own scale
                         tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc2, j > 0 ? 1u : acc0);
-                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt + (uint32_t)kCols, alo + 8u * j, dbh[sl][j], idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[sl]);
                     if (last) {
@@ -457,48 +470,81 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 // K(:, S_i) for the round, FP32 from direct differences: Kc[i][c], 64 columns
 // per row (zero beyond nacc); the scale enters as an FP32 pair (kexp_scaled).
 // CTA = 128 rows x 64 pivots; thread (ty, tx) of 16 x 16 computes rows
-// ty + 16a (a < 8) and columns tx + 16b (b < 4).
+// ty + 16a (a < 8) and columns tx + 16c (c < 4).  Features are staged 64 at
+// a time with a row pitch of 68 floats, so a thread reads four features of a
+// row in one 16-byte shared load (8 + 4 loads per four features for 256 FP32
+// operations) and the pivot loads of a quarter warp fall in distinct banks;
+// each squared distance still sums its features in increasing order (the
+// zero padding of a ragged last chunk adds exact zeros).
+constexpr int kKcPitch = kFeatChunk + 4;
+
 __global__ void __launch_bounds__(256)
 update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, ScalePair scale, const int64_t* __restrict__ sacc,
-                    const RoundView* st, float* __restrict__ Kc) {
-    if (st->done || st->nacc == 0) return;
-    const int nacc = st->nacc;
-    extern __shared__ float ksm[];
-    constexpr int dp = kFeatChunk + 1;
-    float* xr = ksm;                 // 128 x dp
-    float* xq = ksm + kRows * dp;    // 64 x dp
+                    const RoundView* st, float* __restrict__ Kc, int group) {
+    int64_t r_unused;
+    int nacc;
+    if (!pass_view(st, group, r_unused, nacc)) return;
+    sacc += (int64_t)kCols * group;
+    extern __shared__ __align__(16) float ksm[];
+    float* xr = ksm;                      // 128 x kKcPitch
+    float* xq = ksm + kRows * kKcPitch;   // 64 x kKcPitch
     const int64_t row0 = (int64_t)blockIdx.x * kRows;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const bool vec = (d & 3) == 0 && ((uintptr_t)X & 15) == 0;   // rows start on 16-byte boundaries
     float acc[8][4];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[a][c] = 0.f;
-    // features kFeatChunk at a time, summed in increasing order
     for (int c0 = 0; c0 < d; c0 += kFeatChunk) {
         const int w = min(kFeatChunk, d - c0);
+        const int w4 = (w + 3) & ~3;
         __syncthreads();
-        for (int e = threadIdx.x; e < kRows * w; e += 256) {
-            const int rr = e / w, kk = e - rr * w;
-            const int64_t i = row0 + rr;
-            xr[rr * dp + kk] = (i < N) ? X[i * d + c0 + kk] : 0.f;
-        }
-        for (int e = threadIdx.x; e < kCols * w; e += 256) {
-            const int q = e / w, kk = e - q * w;
-            xq[q * dp + kk] = (q < nacc) ? X[sacc[q] * d + c0 + kk] : 0.f;
+        if (vec) {
+            const int nq = w4 >> 2;
+            for (int e = threadIdx.x; e < (kRows + kCols) * nq; e += 256) {
+                const int rr = e / nq, k4 = (e - rr * nq) << 2;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (rr < kRows) {
+                    const int64_t i = row0 + rr;
+                    if (i < N) v = __ldg(reinterpret_cast<const float4*>(X + i * d + c0 + k4));
+                    *reinterpret_cast<float4*>(xr + rr * kKcPitch + k4) = v;
+                } else {
+                    const int q = rr - kRows;
+                    if (q < nacc) v = __ldg(reinterpret_cast<const float4*>(X + sacc[q] * d + c0 + k4));
+                    *reinterpret_cast<float4*>(xq + q * kKcPitch + k4) = v;
+                }
+            }
+        } else {
+            for (int e = threadIdx.x; e < (kRows + kCols) * w4; e += 256) {
+                const int rr = e / w4, kk = e - rr * w4;
+                if (rr < kRows) {
+                    const int64_t i = row0 + rr;
+                    xr[rr * kKcPitch + kk] = (i < N && kk < w) ? X[i * d + c0 + kk] : 0.f;
+                } else {
+                    const int q = rr - kRows;
+                    xq[q * kKcPitch + kk] = (q < nacc && kk < w) ? X[sacc[q] * d + c0 + kk] : 0.f;
+                }
+            }
         }
         __syncthreads();
-        for (int kk = 0; kk < w; ++kk) {
-            float vr[8], vq[4];
+        for (int kk = 0; kk < w4; kk += 4) {
+            float4 vr[8], vq[4];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) vr[a] = xr[(ty + 16 * a) * dp + kk];
+            for (int a = 0; a < 8; ++a) vr[a] = *reinterpret_cast<const float4*>(xr + (ty + 16 * a) * kKcPitch + kk);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) vq[c] = xq[(tx + 16 * c) * dp + kk];
+            for (int c = 0; c < 4; ++c) vq[c] = *reinterpret_cast<const float4*>(xq + (tx + 16 * c) * kKcPitch + kk);
 #pragma unroll
             for (int a = 0; a < 8; ++a)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
-                    const float t = vr[a] - vq[c];
+                    float t = vr[a].x - vq[c].x;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].y - vq[c].y;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].z - vq[c].z;
+                    acc[a][c] = fmaf(t, t, acc[a][c]);
+                    t = vr[a].w - vq[c].w;
                     acc[a][c] = fmaf(t, t, acc[a][c]);
                 }
         }
@@ -519,10 +565,11 @@ update_kcols_kernel(const float* __restrict__ X, int64_t N, int d, ScalePair sca
 // stage s -> [hi: 64 rows x 32 cols][lo], K-major SW128 (rows >= nacc and
 // columns >= r are zero).
 __global__ void update_prep_kernel(const float* __restrict__ F, int64_t ldF, const int64_t* __restrict__ sacc,
-                                   const RoundView* st, int n_stages_max, uint8_t* __restrict__ bprep) {
-    if (st->done || st->nacc == 0) return;
-    const int nacc = st->nacc;
-    const int64_t r = st->r_old;
+                                   const RoundView* st, int n_stages_max, uint8_t* __restrict__ bprep, int group) {
+    int64_t r;
+    int nacc;
+    if (!pass_view(st, group, r, nacc)) return;
+    sacc += (int64_t)kCols * group;
     const int n_st = (int)((r + kKs - 1) / kKs);
     const int64_t total = (int64_t)n_st * kCols * kKs;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -564,8 +611,8 @@ static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 static_assert(kUpdSmem <= 227 * 1024, "shared memory per CTA");
 
 // Whether the tensor-core update can run for this factor layout.
-bool update_tc_supported(const float* F, int64_t ldF, int d, int b) {
-    return get_encode() != nullptr && (ldF % 4) == 0 && ((uintptr_t)F % 16) == 0 && d <= kMaxD && b <= kCols &&
+bool update_tc_supported(const float* F, int64_t ldF, int d) {
+    return get_encode() != nullptr && (ldF % 4) == 0 && ((uintptr_t)F % 16) == 0 && d <= kMaxD &&
            ldF * 4 < (1ll << 40);
 }
 
@@ -593,6 +640,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
         last_N = N;
     }
     const int n_stages_max = (int)((k_max + kKs - 1) / kKs);
+    const int n_groups = (b + kCols - 1) / kCols;
     int rc = KEVD_OK;
     uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
@@ -620,28 +668,31 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
             last_KN = N;
         }
     }
-    {
-        ProfScope ps(ctx, "rp_update_kcols", s);
-        const size_t ksm = (size_t)(kRows + kCols) * (kFeatChunk + 1) * sizeof(float);
-        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
-        update_kcols_kernel<<<(int)((N + kRows - 1) / kRows), 256, ksm, s>>>(X, N, d, split_scale(scale), sacc, rv,
-                                                                             Kc);
-        KEVD_LAUNCH(ctx);
-    }
-    {
-        ProfScope ps(ctx, "rp_update_prep", s);
-        update_prep_kernel<<<std::max(1, std::min(n_stages_max * 8, ctx->num_sms * 4)), 256, 0, s>>>(
-            F, ldF, sacc, rv, n_stages_max, bprep);
-        KEVD_LAUNCH(ctx);
-    }
+    const size_t ksm = (size_t)(kRows + kCols) * kKcPitch * sizeof(float);
+    KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_kcols_kernel), (int)ksm));
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&update_tc_kernel), (int)kUpdSmem));
     const int64_t nblk = (N + kRows - 1) / kRows;
     const int grid = (int)std::min<int64_t>(nblk, ctx->num_sms);
-    {
-        ProfScope ps(ctx, "rp_update", s);
-        update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, tmk, F, ldF, N, minv_f, b, bprep, rv, dvec, dblk,
-                                                          err);
-        KEVD_LAUNCH(ctx);
+    // one pass per 64 accepted columns (passes beyond the round's count return at once)
+    for (int g = 0; g < n_groups; ++g) {
+        const float* minv_g = minv_f + (size_t)kCols * g * b + (size_t)kCols * g;
+        {
+            ProfScope ps(ctx, "rp_update_kcols", s);
+            update_kcols_kernel<<<(int)nblk, 256, ksm, s>>>(X, N, d, split_scale(scale), sacc, rv, Kc, g);
+            KEVD_LAUNCH(ctx);
+        }
+        {
+            ProfScope ps(ctx, "rp_update_prep", s);
+            update_prep_kernel<<<std::max(1, std::min(n_stages_max * 8, ctx->num_sms * 4)), 256, 0, s>>>(
+                F, ldF, sacc, rv, n_stages_max, bprep, g);
+            KEVD_LAUNCH(ctx);
+        }
+        {
+            ProfScope ps(ctx, "rp_update", s);
+            update_tc_kernel<<<grid, kThreads, kUpdSmem, s>>>(tmap, tmk, F, ldF, N, minv_g, b, bprep, rv, dvec, dblk,
+                                                              err, g);
+            KEVD_LAUNCH(ctx);
+        }
     }
     return KEVD_OK;
 }

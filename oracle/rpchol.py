@@ -60,13 +60,22 @@ def reject_and_factor(H: np.ndarray, ua: np.ndarray, tol: float, cap: int):
     Lc = L[np.ix_(acc, acc)]
     n = acc.size
     Minv = np.zeros((n, n))
-    for t in range(n):
-        Minv[t, t] = 1.0 / Lc[t, t]
-        for a in range(t + 1, n):
-            s = 0.0
-            for e in range(t, a):
-                s += Lc[a, e] * Minv[e, t]
-            Minv[a, t] = -s / Lc[a, a]
+    if n <= 64:
+        # column-wise forward substitution, each sum in increasing e
+        for t in range(n):
+            Minv[t, t] = 1.0 / Lc[t, t]
+            for a in range(t + 1, n):
+                s = 0.0
+                for e in range(t, a):
+                    s += Lc[a, e] * Minv[e, t]
+                Minv[a, t] = -s / Lc[a, a]
+    else:
+        # the same substitution a row at a time (sums in BLAS order: equal to
+        # the column-wise form up to rounding; the zeros above the diagonal of
+        # Minv add nothing)
+        for a in range(n):
+            Minv[a, :a] = -(Lc[a, :a] @ Minv[:a, :a]) / Lc[a, a]
+            Minv[a, a] = 1.0 / Lc[a, a]
     return acc, Lc, Minv
 
 

@@ -26,7 +26,8 @@ def _gpu(ctx, X, **kw):
     return api.rpcholesky(ctx, torch.from_numpy(np.ascontiguousarray(X)).cuda(), SCALE, **kw)
 
 
-@pytest.mark.parametrize("N,k,b", [(5000, 200, 1), (5000, 300, 16), (4999, 400, 64), (777, 150, 32)])
+@pytest.mark.parametrize("N,k,b", [(5000, 200, 1), (5000, 300, 16), (4999, 400, 64), (777, 150, 32),
+                                   (5000, 600, 128), (5000, 800, 256), (5000, 900, 512)])
 def test_fp64_pivots_bit_exact(ctx, states, N, k, b):
     X = states[:N]
     seed = 1000 + b
@@ -81,7 +82,7 @@ def test_mixed_trace_error_close_to_fp64(ctx, states):
     assert abs(direct - g.trace_error) <= 1e-5 * max(1.0, g.trace_error)
 
 
-@pytest.mark.parametrize("N,b", [(5000, 64), (3001, 17), (640, 1)])
+@pytest.mark.parametrize("N,b", [(5000, 64), (3001, 17), (640, 1), (5000, 128), (4000, 256)])
 def test_mixed_factor_columns_match_oracle(ctx, states, N, b):
     """With the same draws, the FP32 factor (tensor-core residual update) agrees
     with the FP64 oracle column by column while the pivot sequences agree."""
@@ -90,9 +91,13 @@ def test_mixed_factor_columns_match_oracle(ctx, states, N, b):
     ref = rpchol.rpcholesky(X.astype(np.float64), SCALE, k, b, seed=77)
     g = _gpu(ctx, X, k_max=k, block=b, seed=77, precision="mixed")
     same = int(np.argmax(g.piv != ref["piv"])) if np.any(g.piv != ref["piv"]) else min(g.rank, ref["piv"].size)
-    assert same >= min(k, 2 * b)
+    # a larger block accepts more proposals per round after many Schur updates,
+    # whose residuals lie nearer the acceptance threshold (FP32 rounding of H
+    # can flip a decision sooner) and nearer the FP32 floor (a column divides
+    # by sqrt(H_ii) >= 1e-3, so its error can reach 1e-7 / 1e-3)
+    assert same >= min(k, 2 * b if b <= 64 else b)
     F = g.factor.double().cpu().numpy()[:, :same]
-    np.testing.assert_allclose(F, ref["F"][:, :same], rtol=0, atol=2e-5)
+    np.testing.assert_allclose(F, ref["F"][:, :same], rtol=0, atol=2e-5 if b <= 64 else 2e-4)
 
 
 def test_linv_matches_oracle(ctx, states):
@@ -109,7 +114,7 @@ def test_bad_arguments(ctx, states):
     from kernel_evd_gb300 import KevdError, api
     X = torch.from_numpy(states[:100].copy()).cuda()
     with pytest.raises(KevdError) as e:
-        api.rpcholesky(ctx, X, SCALE, k_max=10, block=65, precision="fp64")
+        api.rpcholesky(ctx, X, SCALE, k_max=10, block=513, precision="fp64")
     assert e.value.name == "KEVD_ERR_ARG"
     with pytest.raises(KevdError):
         api.rpcholesky(ctx, X, SCALE, k_max=10, block=4, precision="fp64",
@@ -122,7 +127,7 @@ def test_batched_factorisations_match_single(ctx, use_graph):
     graph: each job equals the single-job factorisation (same pivots, same
     trace error, same factor columns)."""
     from kernel_evd_gb300 import api
-    shapes = [(3000, 64, 256, 32), (1200, 32, 100, 16), (5000, 128, 320, 64), (800, 64, 64, 32)]
+    shapes = [(3000, 64, 256, 32), (1200, 32, 100, 16), (5000, 128, 320, 64), (800, 64, 64, 32), (4000, 64, 400, 128)]
     Xs, scales = [], []
     for q, (n, m, k, b) in enumerate(shapes):
         Xn = ks.seeded_mode(n, M=m, seed=10 + q, warm_time=60.0).astype(np.float32)
@@ -130,7 +135,7 @@ def test_batched_factorisations_match_single(ctx, use_graph):
         scales.append(1.0 / (0.5 * m))
     ks_ = [s[2] for s in shapes]
     bs = [s[3] for s in shapes]
-    got = api.rpcholesky_batched(ctx, Xs, scales, ks_, bs, seeds=[7, 8, 9, 10], use_graph=use_graph)
+    got = api.rpcholesky_batched(ctx, Xs, scales, ks_, bs, seeds=[7, 8, 9, 10, 11], use_graph=use_graph)
     for q in range(len(shapes)):
         ref = api.rpcholesky(ctx, Xs[q], scales[q], k_max=ks_[q], block=bs[q], seed=7 + q, precision="mixed")
         assert got[q].rank == ref.rank
