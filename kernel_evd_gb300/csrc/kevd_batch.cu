@@ -15,6 +15,7 @@
 // synchronisation or allocation once the queue is uploaded, so it can be
 // captured in a CUDA graph and replayed.
 #include "kevd_internal.cuh"
+#include "kevd_pairtile.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -27,8 +28,6 @@ namespace {
 constexpr int kTile = 128;
 constexpr int kMaxScalesB = 64;
 constexpr int kMaxDB = 1024;
-constexpr int kFC = 64;            // feature chunk staged in shared memory
-constexpr int kFP = kFC + 1;
 
 struct JobDesc {
     const float* X;
@@ -62,23 +61,14 @@ __device__ __forceinline__ void tile_ij(int64_t t, int64_t& ti, int64_t& tj) {
     tj = t - i * (i + 1) / 2;
 }
 
-__device__ __forceinline__ void stage_chunk(const float* __restrict__ X, int64_t N, int d, int64_t r0, int c0, int w,
-                                            float* dst) {
-    for (int e = threadIdx.x; e < kTile * w; e += blockDim.x) {
-        const int rr = e / w, kk = e - rr * w;
-        const int64_t r = r0 + rr;
-        dst[rr * kFP + kk] = (r < N) ? X[r * d + c0 + kk] : 0.f;
-    }
-}
-
 __global__ void __launch_bounds__(256, 2)
 calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict__ items, int item_base,
                        int n_items, const float* __restrict__ c2all, int* __restrict__ counter,
                        double* __restrict__ partial) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     float* xi = sm;
-    float* xj = sm + kTile * kFP;
-    float* cs = xj + kTile * kFP;            // kMaxScalesB
+    float* xj = sm + kPtTile * kPtPitch;
+    float* cs = xj + kPtTile * kPtPitch;     // kMaxScalesB
     float* red = cs + kMaxScalesB;           // 8 warps x kMaxScalesB
     __shared__ int cur;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -98,31 +88,7 @@ calibrate_queue_kernel(const JobDesc* __restrict__ jobs, const Item* __restrict_
             int64_t ti, tj;
             tile_ij(t, ti, tj);
             float D[8][8];
-#pragma unroll
-            for (int a = 0; a < 8; ++a)
-#pragma unroll
-                for (int b = 0; b < 8; ++b) D[a][b] = 0.f;
-            for (int c0 = 0; c0 < d; c0 += kFC) {
-                const int w = min(kFC, d - c0);
-                __syncthreads();
-                stage_chunk(jb.X, jb.N, d, ti * kTile, c0, w, xi);
-                stage_chunk(jb.X, jb.N, d, tj * kTile, c0, w, xj);
-                __syncthreads();
-                for (int k = 0; k < w; ++k) {
-                    float vi[8], vj[8];
-#pragma unroll
-                    for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * kFP + k];
-#pragma unroll
-                    for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * kFP + k];
-#pragma unroll
-                    for (int a = 0; a < 8; ++a)
-#pragma unroll
-                        for (int b = 0; b < 8; ++b) {
-                            const float u = vi[a] - vj[b];
-                            D[a][b] = fmaf(u, u, D[a][b]);
-                        }
-                }
-            }
+            pt_dist(jb.X, jb.N, d, ti * kTile, tj * kTile, xi, xj, ty, tx, D);
             const int64_t gi0 = ti * kTile + ty, gj0 = tj * kTile + tx;
 #pragma unroll
             for (int a = 0; a < 8; ++a)
@@ -167,7 +133,7 @@ __global__ void calibrate_queue_reduce_kernel(const JobDesc* __restrict__ jobs, 
 }
 
 size_t queue_smem() {
-    return (2 * kTile * (size_t)kFP + kMaxScalesB + 8 * kMaxScalesB) * sizeof(float);
+    return (2 * kPtTile * (size_t)kPtPitch + kMaxScalesB + 8 * kMaxScalesB) * sizeof(float);
 }
 
 }  // namespace
@@ -192,7 +158,7 @@ int run_calibrate_batched(kevd_ctx* ctx, const kevd_calib_job* jobs, int n_jobs,
     // item size: about 16 items per SM over the whole batch unless given
     int64_t per = tiles_per_item > 0 ? tiles_per_item
                                      : std::max<int64_t>(1, total_tiles / ((int64_t)ctx->num_sms * 16));
-    // features are staged kFC at a time, so shared memory does not depend on d
+    // features are staged kPtChunk at a time, so shared memory does not depend on d
     // and one persistent launch serves every dataset of the batch
     std::vector<int> order(n_jobs);
     for (int q = 0; q < n_jobs; ++q) order[q] = q;

@@ -14,6 +14,7 @@
 // per-CTA FP64 partials go to a scratch array and a second kernel reduces them
 // in a fixed order, so the result is deterministic.
 #include "kevd_internal.cuh"
+#include "kevd_pairtile.cuh"
 
 #include <cuda.h>
 
@@ -56,46 +57,14 @@ __device__ __forceinline__ void load_chunk(const float* __restrict__ X, int64_t 
     }
 }
 
-// 8 x 8 squared distances of thread (ty, tx): rows ti*128 + ty + 16a against
-// rows tj*128 + tx + 16b, summed over the feature index in increasing order,
-// the features staged kFC at a time (any d).  Called by all threads of the CTA.
-__device__ __forceinline__ void tile_dist(const float* __restrict__ X, int64_t N, int d, int64_t ti, int64_t tj,
-                                          float* xi, float* xj, int ty, int tx, float (&D)[8][8]) {
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int b = 0; b < 8; ++b) D[a][b] = 0.f;
-    for (int c0 = 0; c0 < d; c0 += kFC) {
-        const int w = min(kFC, d - c0);
-        __syncthreads();
-        load_chunk(X, N, d, ti * kCalTile, c0, w, xi);
-        load_chunk(X, N, d, tj * kCalTile, c0, w, xj);
-        __syncthreads();
-        for (int k = 0; k < w; ++k) {
-            float vi[8], vj[8];
-#pragma unroll
-            for (int a = 0; a < 8; ++a) vi[a] = xi[(ty + 16 * a) * kFP + k];
-#pragma unroll
-            for (int b = 0; b < 8; ++b) vj[b] = xj[(tx + 16 * b) * kFP + k];
-#pragma unroll
-            for (int a = 0; a < 8; ++a)
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    const float t = vi[a] - vj[b];
-                    D[a][b] = fmaf(t, t, D[a][b]);
-                }
-        }
-    }
-}
-
 __global__ void __launch_bounds__(256, 2)
 calibrate_tiles_kernel(const float* __restrict__ X, int64_t N, int d,
                        const float* __restrict__ c2, int n_scales, int64_t n_tiles,
                        double* __restrict__ partial) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     float* xi = sm;
-    float* xj = sm + kCalTile * kFP;
-    float* cs = xj + kCalTile * kFP;                     // n_scales
+    float* xj = sm + kPtTile * kPtPitch;
+    float* cs = xj + kPtTile * kPtPitch;                 // n_scales
     float* red = cs + kCalMaxScales;                     // 8 warps x n_scales
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -105,7 +74,7 @@ calibrate_tiles_kernel(const float* __restrict__ X, int64_t N, int d,
         int64_t ti, tj;
         tri_tile(t, ti, tj);
         float D[8][8];
-        tile_dist(X, N, d, ti, tj, xi, xj, ty, tx, D);
+        pt_dist(X, N, d, ti * kCalTile, tj * kCalTile, xi, xj, ty, tx, D);
         const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
 #pragma unroll
         for (int a = 0; a < 8; ++a)
@@ -256,7 +225,7 @@ int run_calibrate_fp64(kevd_ctx* ctx, const float* X, int64_t N, int d, const do
 
 static size_t calib_smem(int d) {
     (void)d;
-    return (2 * kCalTile * (size_t)kFP + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
+    return (2 * kPtTile * (size_t)kPtPitch + kCalMaxScales + 8 * kCalMaxScales) * sizeof(float);
 }
 
 int run_calibrate(kevd_ctx* ctx, const float* X, int64_t N, int d, const double* scales,
@@ -429,17 +398,17 @@ __device__ __forceinline__ void hist_add(unsigned* h, float D, int shift, unsign
 __global__ void __launch_bounds__(256, 2)
 median_tiles_kernel(const float* __restrict__ X, int64_t N, int d, int64_t n_tiles, int shift,
                     unsigned mask, unsigned prefix, int hi_shift, unsigned* __restrict__ hist) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     float* xi = sm;
-    float* xj = sm + kCalTile * kFP;
-    unsigned* h = reinterpret_cast<unsigned*>(xj + kCalTile * kFP);
+    float* xj = sm + kPtTile * kPtPitch;
+    unsigned* h = reinterpret_cast<unsigned*>(xj + kPtTile * kPtPitch);
     for (int e = threadIdx.x; e < kHistBins; e += blockDim.x) h[e] = 0u;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         int64_t ti, tj;
         tri_tile(t, ti, tj);
         float D[8][8];
-        tile_dist(X, N, d, ti, tj, xi, xj, ty, tx, D);
+        pt_dist(X, N, d, ti * kCalTile, tj * kCalTile, xi, xj, ty, tx, D);
         const int64_t gi0 = ti * kCalTile + ty, gj0 = tj * kCalTile + tx;
 #pragma unroll
         for (int a = 0; a < 8; ++a)
@@ -490,7 +459,7 @@ int run_pair_median(kevd_ctx* ctx, const float* X, int64_t N, int d, const int64
     int st = KEVD_OK;
     unsigned* hist = arena_get<unsigned>(ctx, "med.hist", kHistBins, &st);
     if (st != KEVD_OK) return st;
-    const size_t smem = 2 * kCalTile * (size_t)kFP * sizeof(float) + kHistBins * sizeof(unsigned);
+    const size_t smem = 2 * kPtTile * (size_t)kPtPitch * sizeof(float) + kHistBins * sizeof(unsigned);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&median_tiles_kernel), (int)smem));
     const int shifts[3] = {20, 8, 0};
     const unsigned masks[3] = {0xfffu, 0xfffu, 0xffu};

@@ -234,7 +234,8 @@ __global__ void ev_symmetrize_kernel(double* __restrict__ W, int64_t k) {
 }
 
 // ---- U = Dtil^{-1} F Z (row-major float, N x k_out) -------------------------
-// CTA: 64 rows x k_out (<= 64) columns; Z chunks of 32 rows staged as T.
+// CTA: 64 rows x 64 columns (column chunk blockIdx.y of k_out <= 256); Z
+// chunks of 32 rows staged as T.
 template <typename T>
 __global__ void __launch_bounds__(256)
 ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const double* __restrict__ Z,
@@ -243,6 +244,7 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
     __shared__ T Zs[32][65];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int64_t row0 = (int64_t)blockIdx.x * 64;
+    const int j0 = 64 * blockIdx.y;
     T acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -257,7 +259,7 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
         for (int e = threadIdx.x; e < 32 * 64; e += 256) {
             const int cc = e / 64, j = e - cc * 64;
             const int64_t c = c0 + cc;
-            Zs[cc][j] = (c < k && j < k_out) ? (T)Z[(int64_t)j * k + c] : (T)0;
+            Zs[cc][j] = (c < k && j0 + j < k_out) ? (T)Z[(int64_t)(j0 + j) * k + c] : (T)0;
         }
         __syncthreads();
 #pragma unroll 8
@@ -281,7 +283,7 @@ ev_u_kernel(const T* __restrict__ F, int64_t ldF, int64_t N, int64_t k, const do
         const double di = dinv[i];
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const int j = tx + 16 * b;
+            const int j = j0 + tx + 16 * b;
             if (j < k_out) U[i * k_out + j] = (float)((double)acc[a][b] * di);
         }
     }
@@ -1116,7 +1118,7 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
             if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
             evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U, Yrr);
         } else
-            ev_u_kernel<T><<<ceil_div(N, 64), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
+            ev_u_kernel<T><<<dim3(ceil_div(N, 64), ceil_div(k_out, 64)), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
         KEVD_LAUNCH(ctx);
     }
     if (dump) KEVD_TRY(d2h(ctx, dump->Z, Z, (size_t)k * k_out, s));
@@ -1181,10 +1183,10 @@ int run_weighted_gram2(kevd_ctx* ctx, const void* F, int precision, int64_t N, i
 int run_bistochastic_evd(kevd_ctx* ctx, const void* F, int precision, int64_t N, int64_t k,
                          int64_t ldF, int k_out, double* lam, float* U, kevd_evd_info* info,
                          kevd_evd_dump* dump, cudaStream_t s) {
-    if (!F || !U || N < 1 || k < 1 || ldF < k || k_out < 1 || k_out > 64 || k_out > k || k > 8192)
+    if (!F || !U || N < 1 || k < 1 || ldF < k || k_out < 1 || k_out > 256 || k_out > k || k > 8192)
         return set_error(ctx, KEVD_ERR_ARG,
                          "bistochastic_evd: need F, U, N >= 1, 1 <= k <= 8192, ldF >= k, "
-                         "1 <= k_out <= min(k, 64)");
+                         "1 <= k_out <= min(k, 256)");
     if (precision == KEVD_FP64)
         return evd_impl<double>(ctx, (const double*)F, N, k, ldF, k_out, lam, U, info, dump, s);
     if (precision == KEVD_MIXED)

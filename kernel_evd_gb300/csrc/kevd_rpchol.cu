@@ -706,7 +706,7 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     const double floor_rel = sizeof(T) == 4 ? kMixedFloor : 0.0;
     const int64_t nblk = (N + kRowBlock - 1) / kRowBlock;
     const int n_split = (int)((p->k_max + kColChunk - 1) / kColChunk);
-    const int n_kss = 8;
+    const int n_kss = 32;   // CTAs sharing the FP64 K(S', S') block (one element per thread, same order)
     int st = KEVD_OK;
     double* dvec = arena_get<double>(ctx, "rp.d", N, &st);
     double* dblk = arena_get<double>(ctx, "rp.dblk", nblk, &st);

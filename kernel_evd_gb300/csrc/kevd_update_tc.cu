@@ -10,13 +10,15 @@
 //
 // Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
 // lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
-// stage accumulates hi_a hi_b in one accumulator and the two small terms
-// hi_a lo_b + lo_a hi_b in a second one; every stage uses a fresh TMEM partial
-// (four MMA updates of the large accumulator), and the epilogue sums the
-// partials in FP32 registers with round-to-nearest, so the tensor-core
-// accumulator's one-sided rounding never builds up over r.  (Measured top-32
-// eigenvalue error against FP64 on the same pivots at N = 2M, k = 2000: four
-// stages per partial 2.0e-8, two 1.2e-8, one 8.2e-9 at 5 % more update time.)
+// stage accumulates hi_a hi_b + lo_a hi_b and, in a second accumulator,
+// hi_a lo_b; every stage uses a fresh TMEM partial (eight MMA updates of the
+// first accumulator), and the epilogue sums the partials in FP32 registers
+// with round-to-nearest, so the tensor-core accumulator's one-sided rounding
+// never builds up over r.  (Top-32 eigenvalue error against FP64 on the same
+// pivots at N = 2M, k = 2000, five seeds: one stage per partial median 6.6e-9,
+// max 8.4e-9; two stages per partial median 1.6e-8; lo_a hi_b moved into the
+// second accumulator median 8.0e-9, max 1.0e-8.  One-stage partials cost about
+// 5 % more update time than two.)
 //
 // CTA (448 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
@@ -68,10 +70,10 @@ constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the r
 constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of kPartCols columns
 constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulated per TMEM partial
 // A partial buffer holds two 64-column accumulators side by side: columns
-// [0,64) take hi_a hi_b, columns [64,128) take hi_a lo_b + lo_a hi_b (one
+// [0,64) take hi_a hi_b + lo_a hi_b, columns [64,128) take hi_a lo_b (one
 // N = 128 MMA against the b-hi and b-lo tiles, which lie back to back in
-// shared memory as one 128-row operand, plus one N = 64 MMA into the second
-// half: 8 MMAs per stage instead of 12)
+// shared memory as one 128-row operand, plus one N = 64 MMA: 8 MMAs per stage
+// instead of 12)
 constexpr int kPartCols = 2 * kCols;
 static_assert((kBufs & (kBufs - 1)) == 0 && (kPerPartial & (kPerPartial - 1)) == 0,
               "partial-buffer count and stages per partial are powers of two");
@@ -261,11 +263,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     tc::tc_fence_after();
 #pragma unroll
                     for (int j = 0; j < kKs / 8; ++j) {
-                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the
-                        // second half, so the first half takes one (large) update per
-                        // k-step and the small terms accumulate at their own scale
+                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the first half
                         tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc2, j > 0 ? 1u : acc0);
-                        tc::mma_tf32_tmem_a(dt + (uint32_t)kCols, alo + 8u * j, dbh[sl][j], idesc, 1u);
+                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[sl]);
                     if (last) {
