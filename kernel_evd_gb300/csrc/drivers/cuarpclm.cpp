@@ -1,25 +1,29 @@
 // Stage 2 driver (the reference's ./cuarpclm, ks_arpclm.cu:566-1152): block
 // RPCholesky of the delay-embedded samples; writes L^{-1} and the pivot set
 // and prints the per-round table.  Compile-time configuration as in the
-// reference; override with -D.
+// reference (ks_arpclm.cu:38, :587-602: L = 30 pi, 128 gridpoints, 32,831
+// snapshots, Nq = 64, BLK = 512, bw = 0.8) except the round count: the
+// reference's 64 rounds (rank 32,768) would need a 550 GB stored factor, so 8
+// rounds (rank 4,096, 69 GB in FP32) are the default; the mixed form (FP32
+// factor) stands for the reference's FP32 update; override with -D.
 #include <ctime>
 
 #include "driver_io.h"
 
 #ifndef LFACT
-#define LFACT 22
+#define LFACT 30
 #endif
 #ifndef MGRID
-#define MGRID 8
+#define MGRID 128
 #endif
 #ifndef NDATA
-#define NDATA 2000
+#define NDATA 32831
 #endif
 #ifndef NQ
-#define NQ 32
+#define NQ 64
 #endif
 #ifndef BLK
-#define BLK 32
+#define BLK 512
 #endif
 #ifndef NROUNDS
 #define NROUNDS 8
@@ -28,7 +32,7 @@
 #define BW 0.8
 #endif
 #ifndef PRECISION
-#define PRECISION KEVD_FP64
+#define PRECISION KEVD_MIXED
 #endif
 
 int main() {

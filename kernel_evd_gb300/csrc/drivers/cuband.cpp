@@ -1,22 +1,23 @@
 // Stage 1 driver (the reference's ./cuband, ks_bandwidth.cu:339-667): delay
 // embedding of u, pair sums over the 36-bandwidth sweep, selection, bw0.out.
-// Compile-time configuration as in the reference; override with -D.
+// Compile-time configuration as in the reference (ks_bandwidth.cu:359-365:
+// L = 30 pi, 128 gridpoints, 4,607 snapshots, Nq = 512); override with -D.
 #include <cmath>
 #include <ctime>
 
 #include "driver_io.h"
 
 #ifndef LFACT
-#define LFACT 22
+#define LFACT 30
 #endif
 #ifndef MGRID
-#define MGRID 8
+#define MGRID 128
 #endif
 #ifndef NDATA
-#define NDATA 600
+#define NDATA 4607
 #endif
 #ifndef NQ
-#define NQ 32
+#define NQ 512
 #endif
 
 int main() {

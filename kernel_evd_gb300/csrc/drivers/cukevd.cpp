@@ -2,25 +2,30 @@
 // normalisation and EVD from the stage-2 outputs (L^{-1}, pivots); writes the
 // eigenvalues (ascending) and the top k_out eigenvector block.  A library status
 // other than KEVD_OK ends the program with that code, as the reference's
-// MPI_Abort codes do.  Compile-time configuration; override with -D.
+// MPI_Abort codes do.  Compile-time configuration as in the reference
+// (ks_kevd.cu:439-481: L = 30 pi, 128 gridpoints, 32,831 snapshots, Nq = 64,
+// bw = 0.8, k_out = 256), reading the stage-2 files of the cuarpclm defaults
+// (BLK = 512, 8 rounds); the factor is formed and decomposed in the mixed form
+// (FP32 factor: at rank 4,096 it and its column-major copy take 138 GB);
+// override with -D.
 #include <ctime>
 
 #include "driver_io.h"
 
 #ifndef LFACT
-#define LFACT 22
+#define LFACT 30
 #endif
 #ifndef MGRID
-#define MGRID 8
+#define MGRID 128
 #endif
 #ifndef NDATA
-#define NDATA 2000
+#define NDATA 32831
 #endif
 #ifndef NQ
-#define NQ 32
+#define NQ 64
 #endif
 #ifndef BLK
-#define BLK 32
+#define BLK 512
 #endif
 #ifndef NROUNDS
 #define NROUNDS 8
@@ -29,7 +34,10 @@
 #define BW 0.8
 #endif
 #ifndef KOUT
-#define KOUT 16
+#define KOUT 256
+#endif
+#ifndef PRECISION
+#define PRECISION KEVD_MIXED
 #endif
 
 int main() {
@@ -59,15 +67,15 @@ int main() {
     double* F = nullptr;
     DRV_CUDA(cudaMalloc(&u_dev, u.size() * sizeof(float)));
     DRV_CUDA(cudaMalloc(&X_dev, NM * Nq * sizeof(float)));
-    DRV_CUDA(cudaMalloc(&F, NM * Nr * sizeof(double)));
+    DRV_CUDA(cudaMalloc(&F, NM * Nr * (PRECISION == KEVD_FP64 ? sizeof(double) : sizeof(float))));
     DRV_CUDA(cudaMalloc(&U_dev, NM * k_out * sizeof(float)));
     DRV_CUDA(cudaMemcpy(u_dev, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice));
     DRV_KEVD(ctx, kevd_hankel_rows(ctx, u_dev, (int64_t)Ndata, (int64_t)M, (int64_t)Nq, X_dev, nullptr));
     DRV_KEVD(ctx, kevd_factor_from_linv(ctx, X_dev, (int64_t)NM, (int32_t)Nq, 1.0 / ((double)Nq * BW), spiv.data(),
-                                        (int64_t)Nr, linv.data(), KEVD_FP64, F, (int64_t)Nr, nullptr));
+                                        (int64_t)Nr, linv.data(), PRECISION, F, (int64_t)Nr, nullptr));
     std::vector<double> lam(Nr);
     kevd_evd_info info = {};
-    DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, KEVD_FP64, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
+    DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, PRECISION, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
                                         lam.data(), U_dev, &info, nullptr, nullptr));
     std::vector<float> U(NM * k_out);
     DRV_CUDA(cudaMemcpy(U.data(), U_dev, U.size() * sizeof(float), cudaMemcpyDeviceToHost));

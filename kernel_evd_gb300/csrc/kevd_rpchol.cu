@@ -297,7 +297,6 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
     __shared__ double us[kSmallBlock];    // the round's acceptance uniforms
     __shared__ double kfl[kSmallBlock];   // acceptance floor per proposal (0 in the FP64 form)
     __shared__ int accpos[kSmallBlock];
-    __shared__ int s_dec, s_m;
     const int tid = threadIdx.x;
     const int64_t r = st->rank;
     const int nz = (int)((r + kColChunk - 1) / kColChunk);
@@ -332,31 +331,35 @@ rp_factor_kernel(const double* __restrict__ kss, const double* __restrict__ hpar
         kfl[p] = floor_rel * kss[p * b + p];
         us[p] = uniforms ? uniforms[((int64_t)round * 2 + 1) * b + p] : philox_uniform(seed, (uint32_t)round, 1u, (uint32_t)p);
     }
-    if (tid == 0) s_m = 0;
-    __syncthreads();
     const int64_t cap = k_max - r;
+    // Every thread takes the same decisions (H_ii is final once the previous
+    // accepted step's trailing update has passed its barrier), so a rejected
+    // proposal costs no barrier and an accepted one a single barrier.  The
+    // trailing update forms the scaled column l_j = H_ji f in registers, the
+    // same product that is stored into column i after the barrier (the next
+    // steps never touch column i, so that write overlaps them).
+    int m = 0;
+    __syncthreads();
     for (int i = 0; i < b; ++i) {
-        __syncthreads();  // everyone has consumed the previous decision
-        if (tid == 0) {
-            const double u = us[i];
-            const double hii = H[i * b + i];
-            const int acc = (s_m < cap) && (H0[i] * u < hii) && (hii > tol) && (hii > kfl[i]);
-            s_dec = acc;
-            if (acc) accpos[s_m++] = i;
+        const double hii = H[i * b + i];
+        const bool acc = (m < cap) && (H0[i] * us[i] < hii) && (hii > tol) && (hii > kfl[i]);
+        if (!acc) continue;
+        if (tid == 0) accpos[m] = i;
+        ++m;
+        const double f = 1.0 / sqrt(hii);
+        // trailing update of the lower triangle, 16 x 16 threads over (jj, kk)
+        for (int jj = i + 1 + (tid >> 4); jj < b; jj += 16) {
+            const double lj = H[jj * b + i] * f;
+            for (int kk = i + 1 + (tid & 15); kk <= jj; kk += 16) {
+                const double lk = H[kk * b + i] * f;
+                H[jj * b + kk] -= lj * lk;
+            }
         }
         __syncthreads();
-        if (s_dec) {
-            const double f = 1.0 / sqrt(H[i * b + i]);
-            __syncthreads();
-            for (int j = i + tid; j < b; j += blockDim.x) H[j * b + i] *= f;
-            __syncthreads();
-            // trailing update of the lower triangle, 16 x 16 threads over (jj, kk)
-            for (int jj = i + 1 + (tid >> 4); jj < b; jj += 16)
-                for (int kk = i + 1 + (tid & 15); kk <= jj; kk += 16) H[jj * b + kk] -= H[jj * b + i] * H[kk * b + i];
-            __syncthreads();
-        }
+        for (int j = i + tid; j < b; j += blockDim.x) H[j * b + i] *= f;
     }
-    const int nacc = s_m;
+    __syncthreads();   // the last scaled column is written
+    const int nacc = m;
     // forward substitution, one column per thread, in shared memory (the
     // sequential dot products read what the same thread wrote a step earlier)
     // on the compacted factor LC (no index indirection inside the chains)

@@ -20,7 +20,7 @@
 // second accumulator median 8.0e-9, max 1.0e-8.  One-stage partials cost about
 // 5 % more update time than two.)
 //
-// CTA (448 threads, persistent over row blocks):
+// CTA (576 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
 //              and the pre-split S_i tiles (bulk copy)
 //   warp 1     TMEM allocation and the single MMA-issuing thread (A from
@@ -33,7 +33,11 @@
 //              stages: thread m owns row m of the F tile (its TMEM lane
 //              quarter is warp % 4), zeroes columns >= r and writes the hi and
 //              lo parts into the stage's Tensor Memory a-slot (tcgen05.st)
-//   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows)
+//   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows): sums the
+//              partials of a row block and leaves T = K - P in the K tile
+//   warps 14-17 tail: G = T L_i^{-T}, the d update, the F write and the block
+//              sum of d for one row block while the other roles run ahead on
+//              the next ones
 // Ring of 4 stages (shared-memory tiles + Tensor Memory a-slots of 64 columns)
 // and 2 TMEM partial buffers of 128 columns, handed over with mbarriers; every
 // wait is bounded (error flag on timeout).  The F tile never goes back to
@@ -83,7 +87,7 @@ constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
 constexpr int kAOp = kRows * kKs * 4;     // 16 KB
 constexpr int kBOp = kCols * kKs * 4;     // 8 KB
 constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
-constexpr int kThreads = 448;
+constexpr int kThreads = 576;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = kMaxFeatures;
 constexpr int kFeatChunk = 64;      // features staged at a time by update_kcols_kernel
@@ -96,14 +100,15 @@ struct Bars {
     uint64_t accf[kBufs];
     uint64_t acce[kBufs];
     uint64_t kfull;     // K(R, S_i) tile landed
-    uint64_t kempty;    // epilogue done with the K tile
+    uint64_t tready;    // epilogue left T = K - P in the K tile
+    uint64_t kempty;    // tail warps done with the K tile
     uint64_t done;
     uint32_t tmem_base;
 };
 
 // converter warps: group 0 = {2, 3, 8, 9} takes the even stages, group 1 =
 // {10, 11, 12, 13} the odd ones; warp % 4 is the TMEM lane quarter it writes
-__device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || w >= 8; }
+__device__ __forceinline__ bool is_cvt_warp(int w) { return w == 2 || w == 3 || (w >= 8 && w <= 13); }
 __device__ __forceinline__ int cvt_group(int w) { return w >= 10 ? 1 : 0; }
 
 struct RoundView {   // must match the RoundState layout of kevd_rpchol.cu
@@ -164,6 +169,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             tc::mbar_init(&bar->acce[t], 128);
         }
         tc::mbar_init(&bar->kfull, 1);
+        tc::mbar_init(&bar->tready, 128);
         tc::mbar_init(&bar->kempty, 128);
         tc::mbar_init(&bar->done, 1);
         tc::mbar_fence_init();
@@ -322,21 +328,19 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             }
             if (!ok) break;
         }
-    } else {
+    } else if (warp < 8) {
         // ---------------- epilogue: warps 4..7, TMEM lane quarter q = warp - 4.
-        // After a timed-out wait the warp stops waiting but keeps walking the
-        // row blocks, so all four warps meet the same named barriers.
+        // Sums each row block's partials as they land and leaves T = K - P in
+        // the K tile (this thread's row, in place) for the tail warps.  After a
+        // timed-out wait the warp stops waiting but keeps walking the row
+        // blocks and arriving, so no other role waits for it in vain.
         const int q = warp - 4;
         const int rloc = 32 * q + lane;
         const int n_part = (n_st + kPerPartial - 1) / kPerPartial;
         int64_t g = 0;
         int64_t kit = 0;
         bool ok = true;
-        __shared__ double wsum[2][4];
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
-            const int64_t row0 = rb * kRows;
-            const int64_t i = row0 + rloc;
-            const double d_old = (i < N) ? dvec[i] : 0.0;
             float acc[kCols];
 #pragma unroll
             for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
@@ -350,16 +354,16 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     continue;
                 }
                 tc::tc_fence_after();
-                float v[32];
+                float v[16];
                 const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kPartCols);
-                // 32 columns at a time (register budget of 448 threads): the main
+                // 16 columns at a time (register budget of 576 threads): the main
                 // sums, then the hi_a lo_b sums of the same columns
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    tc::tmem_ld32(ta + (uint32_t)((h & 1) * 32 + (h >> 1) * kCols), v);
+                for (int h = 0; h < 8; ++h) {
+                    tc::tmem_ld16(ta + (uint32_t)((h & 3) * 16 + (h >> 2) * kCols), v);
                     tc::tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) acc[32 * (h & 1) + j] += v[j];
+                    for (int j = 0; j < 16; ++j) acc[16 * (h & 3) + j] += v[j];
                 }
                 tc::tc_fence_before();
                 tc::mbar_arrive(&bar->acce[tb]);
@@ -368,21 +372,60 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 atomicExch(err, 17);
                 ok = false;
             }
-            double nd = d_old;
-            const bool live = ok && i < N;
-            if (live) {
-                // T = K(i, S_i) - P  (K(:, S_i) by update_kcols_kernel, TMA tile in smem)
+            if (ok) {
+                // T = K(i, S_i) - P over the K tile's row (K(:, S_i) by
+                // update_kcols_kernel, TMA tile in smem)
 #pragma unroll
                 for (int c4 = 0; c4 < kCols / 4; ++c4) {
-                    const float4 kv = *reinterpret_cast<const float4*>(
+                    float4* kp = reinterpret_cast<float4*>(
                         ktile + (c4 >> 3) * kAOp + tc::sw128_off((uint32_t)rloc, (uint32_t)(4 * (c4 & 7))));
-                    acc[4 * c4 + 0] = kv.x - acc[4 * c4 + 0];
-                    acc[4 * c4 + 1] = kv.y - acc[4 * c4 + 1];
-                    acc[4 * c4 + 2] = kv.z - acc[4 * c4 + 2];
-                    acc[4 * c4 + 3] = kv.w - acc[4 * c4 + 3];
+                    float4 kv = *kp;
+                    kv.x -= acc[4 * c4 + 0];
+                    kv.y -= acc[4 * c4 + 1];
+                    kv.z -= acc[4 * c4 + 2];
+                    kv.w -= acc[4 * c4 + 3];
+                    *kp = kv;
+                }
+                // the tile is written by TMA again once the tail warps release it
+                tc::fence_async_smem();
+            }
+            tc::mbar_arrive(&bar->tready);
+            ++kit;
+        }
+    } else {
+        // ---------------- tail: warps 14..17, row 32q + lane of each row block.
+        // G = T L_i^{-T}, the d update, the F write and the block sum of d,
+        // overlapped with the MMA and the epilogue working on the next row
+        // blocks.  The K tile (holding T) is released as soon as this thread's
+        // row is in registers.
+        const int q = warp - 14;
+        const int rloc = 32 * q + lane;
+        int64_t it = 0;
+        bool ok = true;
+        __shared__ double wsum[2][4];
+        for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
+            const int64_t row0 = rb * kRows;
+            const int64_t i = row0 + rloc;
+            const double d_old = (i < N) ? dvec[i] : 0.0;
+            if (ok && !tc::mbar_wait(&bar->tready, (uint32_t)(it & 1), kTimeoutNs)) {
+                atomicExch(err, 18);
+                ok = false;
+            }
+            const bool live = ok && i < N;
+            float t[kCols];
+            if (live) {
+#pragma unroll
+                for (int c4 = 0; c4 < kCols / 4; ++c4) {
+                    const float4 tv = *reinterpret_cast<const float4*>(
+                        ktile + (c4 >> 3) * kAOp + tc::sw128_off((uint32_t)rloc, (uint32_t)(4 * (c4 & 7))));
+                    t[4 * c4 + 0] = tv.x;
+                    t[4 * c4 + 1] = tv.y;
+                    t[4 * c4 + 2] = tv.z;
+                    t[4 * c4 + 3] = tv.w;
                 }
             }
             tc::mbar_arrive(&bar->kempty);   // this thread is done with the K tile: the next one may land
+            double nd = d_old;
             if (live) {
                 // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
                 // chains; the two 16-byte broadcast loads of L_i^{-1} for term e+2
@@ -409,14 +452,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                                 p0 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0);
                                 p1 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0 + 4);
                             }
-                            g8[0] = fmaf(acc[e], m0.x, g8[0]);
-                            g8[1] = fmaf(acc[e], m0.y, g8[1]);
-                            g8[2] = fmaf(acc[e], m0.z, g8[2]);
-                            g8[3] = fmaf(acc[e], m0.w, g8[3]);
-                            g8[4] = fmaf(acc[e], m1.x, g8[4]);
-                            g8[5] = fmaf(acc[e], m1.y, g8[5]);
-                            g8[6] = fmaf(acc[e], m1.z, g8[6]);
-                            g8[7] = fmaf(acc[e], m1.w, g8[7]);
+                            g8[0] = fmaf(t[e], m0.x, g8[0]);
+                            g8[1] = fmaf(t[e], m0.y, g8[1]);
+                            g8[2] = fmaf(t[e], m0.z, g8[2]);
+                            g8[3] = fmaf(t[e], m0.w, g8[3]);
+                            g8[4] = fmaf(t[e], m1.x, g8[4]);
+                            g8[5] = fmaf(t[e], m1.y, g8[5]);
+                            g8[6] = fmaf(t[e], m1.z, g8[6]);
+                            g8[7] = fmaf(t[e], m1.w, g8[7]);
                         }
 #pragma unroll
                         for (int u = 0; u < 8; ++u) {
@@ -451,11 +494,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
             }
             __syncwarp();
-            ++kit;
-            // block sum of the new d over the 128 epilogue threads
+            ++it;
+            // block sum of the new d over the 128 tail threads
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
-            double* ws = wsum[kit & 1];   // alternate buffers: one barrier per row block
+            double* ws = wsum[it & 1];   // alternate buffers: one barrier per row block
             if (lane == 0) ws[q] = nd;
             asm volatile("bar.sync 1, 128;" ::: "memory");
             if (rloc == 0) dblk[rb] = (ws[0] + ws[1]) + (ws[2] + ws[3]);

@@ -1,8 +1,12 @@
-"""The three stage drivers (kernel_evd_gb300/bin: cuband, cuarpclm, cukevd) run
-as the reference's programs do: no arguments, compile-time configuration,
-files under ./data (raw arrays in place of HDF5 datasets), bw0.out and the
-round table on stdout.  Their outputs are checked against the FP64 oracle."""
+"""The three stage drivers (cuband, cuarpclm, cukevd) run as the reference's
+programs do: no arguments, compile-time configuration, files under ./data (raw
+arrays in place of HDF5 datasets), bw0.out and the round table on stdout.  The
+built drivers (kernel_evd_gb300/bin) carry the reference's own constants; these
+tests compile test-sized copies of the same sources with -D overrides, as a
+user of the reference edits its constants, and check their outputs against the
+FP64 oracle."""
 import os
+import shutil
 import subprocess
 
 import numpy as np
@@ -13,8 +17,30 @@ from oracle import calibrate, evd, kernel, ks, rpchol
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-BIN = os.path.join(ROOT, "kernel_evd_gb300", "bin")
+SRC = os.path.join(ROOT, "kernel_evd_gb300", "csrc", "drivers")
+LIBDIR = os.path.join(ROOT, "kernel_evd_gb300", "lib")
 M, NQ, LFACT, BLK, NROUNDS, BW = 8, 32, 22, 32, 8, 0.8
+DEFS = {"cuband": dict(LFACT=LFACT, MGRID=M, NDATA=600, NQ=NQ),
+        "cuarpclm": dict(LFACT=LFACT, MGRID=M, NDATA=2000, NQ=NQ, BLK=BLK, NROUNDS=NROUNDS, BW=BW,
+                         PRECISION="KEVD_FP64"),
+        "cukevd": dict(LFACT=LFACT, MGRID=M, NDATA=2000, NQ=NQ, BLK=BLK, NROUNDS=NROUNDS, BW=BW, KOUT=16,
+                       PRECISION="KEVD_FP64")}
+
+
+@pytest.fixture(scope="module")
+def bindir(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(os.path.join(LIBDIR, "libkevd.so")) or not os.path.exists(nvcc):
+        pytest.skip("libkevd.so or nvcc missing")
+    out = tmp_path_factory.mktemp("drivers")
+    for prog, defs in DEFS.items():
+        cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17",
+               "-I", os.path.join(ROOT, "include"), *[f"-D{k}={v}" for k, v in defs.items()],
+               os.path.join(SRC, prog + ".cpp"), "-o", str(out / prog), "-L", LIBDIR, "-lkevd",
+               "-Xlinker", "-rpath", "-Xlinker", LIBDIR]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+    return str(out)
 
 
 def _write_u(d, ndata):
@@ -24,20 +50,18 @@ def _write_u(d, ndata):
     return u.ravel()
 
 
-def _run(d, prog):
-    exe = os.path.join(BIN, prog)
-    if not os.path.exists(exe):
-        pytest.skip(f"{prog} not built")
+def _run(bindir, d, prog):
+    exe = os.path.join(bindir, prog)
     r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     return r.stdout
 
 
-def test_cuband_selects_the_oracle_bandwidth(tmp_path):
+def test_cuband_selects_the_oracle_bandwidth(bindir, tmp_path):
     d = str(tmp_path)
     os.makedirs(os.path.join(d, "data"))
     u = _write_u(d, 600)
-    out = _run(d, "cuband")
+    out = _run(bindir, d, "cuband")
     assert "Total time:" in out
     lines = open(os.path.join(d, "bw0.out")).read().split("\n")
     eopt = float(lines[-3])
@@ -50,12 +74,12 @@ def test_cuband_selects_the_oracle_bandwidth(tmp_path):
     np.testing.assert_allclose(got[:, 1], logS[1:-1], rtol=1e-4, atol=1e-6)
 
 
-def test_cuarpclm_then_cukevd_match_the_oracle(tmp_path):
+def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     d = str(tmp_path)
     os.makedirs(os.path.join(d, "data"))
     ndata = 2000
     u = _write_u(d, ndata)
-    out = _run(d, "cuarpclm")
+    out = _run(bindir, d, "cuarpclm")
     assert "# round accepted cumrank relerr" in out
     N = ndata - NQ + 1
     spiv = np.fromfile(os.path.join(d, "data", f"spiv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.bin"), dtype=np.uint64)
@@ -67,7 +91,7 @@ def test_cuarpclm_then_cukevd_match_the_oracle(tmp_path):
     r = spiv.size
     Li = rpchol.linv_from_F(ref["F"], ref["piv"])
     np.testing.assert_allclose(linv.reshape(r, r, order="F"), Li, rtol=0, atol=1e-8 * np.abs(Li).max())
-    out = _run(d, "cukevd")
+    out = _run(bindir, d, "cukevd")
     lam = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_lam.bin"), dtype=np.float64)
     U = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_U.bin"), dtype=np.float32)
     e = evd.evd_from_factor(ref["F"], 16)
