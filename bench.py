@@ -815,9 +815,10 @@ def main():
         t = t / 1e3
         roof["gram_tc"] = {"bound": "tensor", "achieved": gram_flops / t / 1e12, "peak": tc, "unit": "TFLOP/s",
                            "frac": gram_flops / t / 1e12 / tc, "traffic": None, "flops_per_launch": gram_flops,
-                           "issued_tf32_tflops": 3.0 * gram_flops / t / 1e12,
-                           "note": src + " bf16 dense; useful flops of both Grams (3xTF32 issues 3x this at the "
-                                   "TF32 rate, half the bf16 rate)"}
+                           "issued_f16_tflops": 3.0 * gram_flops / t / 1e12,
+                           "issued_frac": 3.0 * gram_flops / t / 1e12 / tc,
+                           "note": src + " bf16 dense; useful flops of both Grams (the two-term f16 split issues "
+                                   "3x this at the f16 rate, the bf16 rate)"}
     # the kernel with the most time among those with a roofline model (the residual
     # update at N = 2M; at small N the dense k x k solvers lead and have none)
     dom = max(roof, key=lambda k_: prof[k_][0]) if roof else None

@@ -265,8 +265,9 @@ typedef struct {
 /* Weighted Gram G = F^T diag(s)^2 F (k x k, column-major, both triangles) --
  * the Atil / Btil accumulation of ks_kevd.cu:1091-1159, :1627-1685 on a stored
  * factor.  F: device N x ldF (double for KEVD_FP64, float for KEVD_MIXED: the
- * FP32 factor is contracted on the tensor cores in 3xTF32 with FP64
- * accumulation across row chunks).  s: device, N doubles.  G: device. */
+ * FP32 factor is contracted on the tensor cores as a two-term f16 split,
+ * scaled by powers of two to max |F| and max s^2, with FP64 accumulation
+ * across row chunks).  s: device, N doubles.  G: device. */
 int kevd_weighted_gram(kevd_ctx* ctx, const void* F, int32_t precision,
                        int64_t N, int64_t k, int64_t ldF, const double* s,
                        double* G, void* stream);

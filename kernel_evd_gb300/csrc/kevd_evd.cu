@@ -26,21 +26,23 @@
 
 namespace kevd {
 
-int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s, double* G,
-                cudaStream_t st);
-int run_gram2_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s,
-                 const double* s2, double* G, double* G2, cudaStream_t st);
+int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const unsigned* colmax,
+                const double* s, double* G, cudaStream_t st);
+int run_gram2_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const unsigned* colmax,
+                 const double* s, const double* s2, double* G, double* G2, cudaStream_t st);
 int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
-                      cudaStream_t st);
+                      unsigned* amax, cudaStream_t st);
 
-// Column-major copy of an FP32 factor for the tensor-core Grams (K-major TMA tiles).
+// Column-major copy of an FP32 factor for the tensor-core Grams (K-major TMA
+// tiles), and its column maxima (device float bits) for their f16 scaling.
 static int transposed(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float** FT,
-                      int64_t* ldT, cudaStream_t s) {
+                      int64_t* ldT, unsigned** colmax, cudaStream_t s) {
     *ldT = (N + 3) / 4 * 4;
     int st = KEVD_OK;
     *FT = arena_get<float>(ctx, "ev.FT", (size_t)k * (size_t)(*ldT), &st);
+    *colmax = arena_get<unsigned>(ctx, "ev.FTmax", (size_t)k, &st);
     if (st != KEVD_OK) return set_error(ctx, st, "transpose: out of device memory");
-    return run_transpose_f32(ctx, F, ldF, N, k, *FT, *ldT, s);
+    return run_transpose_f32(ctx, F, ldF, N, k, *FT, *ldT, *colmax, s);
 }
 
 // ---- column sums c = F^T w (w == nullptr: ones) ----------------------------
@@ -948,8 +950,9 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     // along rows, K-major tensor-core tiles for the Grams)
     float* FT = nullptr;
     int64_t ldT = 0;
+    unsigned* colmax = nullptr;
     if (sizeof(T) == 4) {
-        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, s));
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, &colmax, s));
         const size_t vsm = (size_t)2 * k * sizeof(float);
         KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&evt_rowdot_kernel), (int)std::max(vsm, (size_t)1024)));
         ProfScope ps(ctx, "ev_passes", s);
@@ -985,10 +988,10 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
 
     // Grams: A = (Dtil^{-1} F)^T (Dtil^{-1} F), B = (Qtil^{-1/2} F)^T (Qtil^{-1/2} F)
     if (sizeof(T) == 4) {
-        // FP32 factor: 3xTF32 tcgen05 Gram with FP64 accumulation across row chunks
+        // FP32 factor: two-term f16 tcgen05 Grams with FP64 accumulation across row chunks
         ev_rsqrt_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(qtil, w2, N);
         KEVD_LAUNCH(ctx);
-        KEVD_TRY(run_gram2_tc(ctx, FT, ldT, N, k, dinv, w2, A, B, s));
+        KEVD_TRY(run_gram2_tc(ctx, FT, ldT, N, k, colmax, dinv, w2, A, B, s));
     } else {
         ev_square_kernel<<<ctx->num_sms * 4, 256, 0, s>>>(dinv, w2, N);
         KEVD_LAUNCH(ctx);
@@ -1047,8 +1050,8 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     const double one = 1.0;
     if (sizeof(T) == 4) {
         // FP32 factor: W only has to deliver the leading subspace, which is
-        // refined against F afterwards, and B carries the 1e-5 error of the
-        // 3xTF32 Gram, so W is formed in FP32 (two strmm) and widened back
+        // refined against F afterwards, and B carries the FP32-level error of
+        // the tensor-core Gram, so W is formed in FP32 (two strmm) and widened back
         ProfScope p2(ctx, "dense_trmm", s);
         float* Lf = arena_get<float>(ctx, "ev.Lf", (size_t)k * k, &st);
         float* Bf = arena_get<float>(ctx, "ev.Bf", (size_t)k * k, &st);
@@ -1152,8 +1155,9 @@ int run_weighted_gram(kevd_ctx* ctx, const void* F, int precision, int64_t N, in
     if (precision == KEVD_MIXED) {
         float* FT = nullptr;
         int64_t ldT = 0;
-        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, st));
-        return run_gram_tc(ctx, FT, ldT, N, k, s_dev, G, st);
+        unsigned* colmax = nullptr;
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, &colmax, st));
+        return run_gram_tc(ctx, FT, ldT, N, k, colmax, s_dev, G, st);
     }
     if (precision != KEVD_FP64) return set_error(ctx, KEVD_ERR_ARG, "weighted_gram: unknown precision");
     int rc = KEVD_OK;
@@ -1173,8 +1177,9 @@ int run_weighted_gram2(kevd_ctx* ctx, const void* F, int precision, int64_t N, i
     if (precision == KEVD_MIXED) {
         float* FT = nullptr;
         int64_t ldT = 0;
-        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, st));
-        return run_gram2_tc(ctx, FT, ldT, N, k, s_dev, s2_dev, G, G2, st);
+        unsigned* colmax = nullptr;
+        KEVD_TRY(transposed(ctx, (const float*)F, ldF, N, k, &FT, &ldT, &colmax, st));
+        return run_gram2_tc(ctx, FT, ldT, N, k, colmax, s_dev, s2_dev, G, G2, st);
     }
     KEVD_TRY(run_weighted_gram(ctx, F, precision, N, k, ldF, s_dev, G, st));
     return run_weighted_gram(ctx, F, precision, N, k, ldF, s2_dev, G2, st);

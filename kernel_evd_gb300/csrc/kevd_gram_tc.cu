@@ -1,47 +1,41 @@
-// Weighted Gram G = Y^T Y, Y = diag(s) F, of an FP32 factor on the tcgen05
-// tensor cores (the A and B Grams of the bistochastic EVD).
+// Weighted Grams G = Y^T Y, Y = diag(s) F, of an FP32 factor on the tcgen05
+// tensor cores (the A and B Grams of the bistochastic EVD, ks_kevd.cu:1152-1158,
+// and the single weighted Gram of the API).
 //
-// Precision: 3xTF32 with the weights on one side, G = (diag(s^2) F)^T F.
-// The tensor core reads an FP32 operand as tf32 by dropping its low 13
-// mantissa bits, so an element v is used as hi = trunc_tf32(v) when passed
-// as it is, and lo = v - hi is exact in FP32 (its own read drops at most
-// 2^-21 |v|).  The a operand is y = s_i^2 F[i][a] (hi: y itself, lo: y -
-// trunc(y), both in Tensor Memory); the b operand is the raw F tile (hi: the
-// TMA tile as loaded, lo: F - trunc(F) in the b-lo tile).  A 128 x 128 output
-// tile accumulates hi_a lo_b^T + lo_a hi_b^T + hi_a hi_b^T in FP32 in Tensor
-// Memory; the dropped parts (lo_a lo_b, the truncation of the lo reads) are
-// below 2^-20 of each product and shrink its magnitude by about 5e-7 on
-// average.  The tensor-core accumulator rounds each update with a one-sided
-// bias, so the FP32 partial is kept short: every 2048 rows it is added into
-// an FP64 tile in global memory and the long sum over N rows is FP64 (the
-// Gram accumulators of the reference are FP64, ks_kevd.cu:1152-1158).  The
-// relative error of a Gram entry is about 4e-5 (1024-row partials halve it
-// and cost 14 % more time at N = 2M, k = 2000); eigenvalues are then refined
-// in FP64 by Rayleigh-Ritz (kevd_evd.cu).
+// Precision: a two-term f16 split with the weights on one side,
+// G = (diag(s^2) F)^T F.  Every factor column is scaled by its own power of
+// two into the f16 range (b side: F(:, c) 2^eb_c with 2^eb_c max|F(:, c)|
+// <= 2^14; a side: s^2 F(:, c) 2^ea_c with 2^ea_c max(s^2) max|F(:, c)| <=
+// 2^14), so late columns, orders of magnitude smaller than the first ones,
+// keep their precision clear of the f16 subnormal range; the values are split
+// as hi = rn_f16(v), lo = rn_f16(v - hi): 22 significant bits, the precision
+// of a two-term tf32 split, at twice the kind::tf32 rate and half the operand
+// bytes.  A 128 x 128 output
+// tile accumulates per 32-row stage the cross terms hi_a lo_b^T and
+// lo_a hi_b^T, then hi_a hi_b^T, in FP32 in Tensor Memory; the dropped lo_a
+// lo_b is below 2^-22 of each product.  The tensor-core accumulator rounds
+// each update with a one-sided bias, so the FP32 partial is kept short: every
+// 2048 rows it is added into an FP64 tile in global memory and the long sum
+// over N rows is FP64 (the Gram accumulators of the reference are FP64).  The
+// scales 2^(ea_a + eb_b) of entry (a, b) are removed exactly when the
+// row-split partials are summed.
+// Eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
 //
 // CTA roles (448 threads):
 //   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
 //               lanes 32q..32q+31 = tile rows)
 //   warps 4-7   a converters: thread m owns row m of the a tile (factor column
 //               a0+m, 32 rows of F): row weights and the hi/lo split, written
-//               to the stage's Tensor Memory a-slot (tcgen05.st, hi and lo
-//               columns)
+//               to the stage's Tensor Memory a-slot (tcgen05.st, packed pairs)
 //   warp 8      TMA producer
 //   warp 9      TMEM allocation and the single MMA-issuing thread (A from
 //               Tensor Memory, B from shared memory)
-//   warps 10-13 b converters: row m of the b tile, its lo part into the b-lo
-//               tile (the raw tile is the hi operand)
-// The conversion and the MMA issue are the per-stage critical paths: two
-// groups of four converter warps (one per SM sub-partition each), and the
-// MMA thread issues a stage's 12 MMAs back to back from precomputed
-// descriptors (measured on GB300: a kind::tf32 MMA of 128 x 128 x 8 takes 64
-// cycles when issued back to back, 128 x 64 x 8 takes 48, and each dependent
-// instruction between two MMAs adds its latency).
-// A 4-stage ring (shared-memory tiles and their Tensor Memory a-slots) and a
-// double-buffered TMEM accumulator (2 x 128 columns) are handed over with
-// mbarriers; every wait is bounded and sets an error flag on timeout.
-// Keeping the a operand out of shared memory removes its split stores and the
-// MMA's a-operand reads (about 80 KB of shared-memory traffic per stage).
+//   warps 10-13 b converters: row m of the b tile split into the f16 b-hi and
+//               b-lo tiles (SWIZZLE_64B); on a diagonal tile (b = a) the a
+//               converters write them
+// A 4-stage ring (shared-memory tiles and Tensor Memory a-slots) and one TMEM
+// accumulator per Gram are handed over with mbarriers; every wait is bounded
+// and sets an error flag on timeout.
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
@@ -57,12 +51,14 @@ namespace {
 constexpr int kTT = 128;               // output tile edge
 constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
 constexpr int kStages = 4;
-constexpr int kPrefetch = 0;          // stages of F prefetched into L2 ahead of the ring (0: off;
-                                      // at N = 2M, k = 2000 a 6-stage prefetch cost 1.8x: it
-                                      // broke the L2 sharing of panels between CTAs)
 constexpr int kFlushStages = 64;       // 2048 rows per FP32 TMEM partial
-constexpr int kOpBytes = kTT * kTK * 4;     // one operand tile, 16 KB
-constexpr int kStageBytes = 3 * kOpBytes;   // a (raw), b hi, b lo
+constexpr int kOpBytes = kTT * kTK * 4;     // one raw FP32 operand tile, 16 KB
+constexpr int kHalfBytes = kTT * kTK * 2;   // one f16 operand tile, 8 KB
+// Per stage: [a raw 16 KB][b raw 16 KB][b hi 8 KB][b lo 8 KB]; a multiple of
+// 1024, so every stage stays 1024-aligned (the TMA's SWIZZLE_128B boxes)
+constexpr int kOffB = kOpBytes, kOffBh = 2 * kOpBytes, kOffBl = 2 * kOpBytes + kHalfBytes;
+constexpr int kStageBytes = 2 * kOpBytes + 2 * kHalfBytes;
+static_assert(kStageBytes % 1024 == 0, "stage alignment");
 constexpr int kEpiWarps = 4;        // warps 0-3
 constexpr int kCvtWarp0 = 4;        // warps 4-7: a operand -> Tensor Memory
 constexpr int kProdWarp = 8;
@@ -70,299 +66,16 @@ constexpr int kMmaWarp = 9;
 constexpr int kCvtBWarp0 = 10;      // warps 10-13: b operand, in shared memory
 constexpr int kCvtWarps = 8;        // arrivals per stage on the "converted" barrier
 constexpr int kThreads = 14 * 32;
-constexpr uint32_t kTmemCols = 512;       // accumulators [0,256), a-operand slots [256,512)
+constexpr uint32_t kTmemCols = 512;       // accumulators [0, 256), a-slots [256, 512)
 constexpr uint32_t kTmemA = 256;
-constexpr uint32_t kTmemASlot = 64;       // hi columns [0,32), lo [32,64)
-static_assert(kTmemA + kStages * kTmemASlot <= kTmemCols, "Tensor Memory holds 512 columns");
+constexpr int kTSlots = 4;                // one a-slot per ring stage
+constexpr uint32_t kTSlotCols = 64;       // per Gram: 16 columns of hi pairs, 16 of lo
+static_assert(kTmemA + kTSlots * kTSlotCols <= kTmemCols, "Tensor Memory holds 512 columns");
+static_assert(kFlushStages % kStages == 0 && kStages % kTSlots == 0, "slot indices are compile-time per stage");
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
-    alignas(16) float w2[kStages][32];   // squared row weights of each stage (bulk copy with the tiles)
-    uint64_t tma[kStages];
-    uint64_t full[kStages];
-    uint64_t empty[kStages];
-    uint64_t accf[2];
-    uint64_t acce[2];
-    uint64_t done;
-    uint32_t tmem_base;
-};
-
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
-static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
-
-__device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
-    int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (i * (i + 1) / 2 > t) --i;
-    while ((i + 1) * (i + 2) / 2 <= t) ++i;
-    ta = i;
-    tb = t - i * (i + 1) / 2;
-}
-
-// Per stage (32 rows of F = 32 columns of FT):
-//   [a 16 KB][b 16 KB][b lo 16 KB]
-// The TMA writes the raw FT boxes (128 factor columns x 32 rows, K-major,
-// SWIZZLE_128B) into the a and b tiles.  With y = s_i^2 F[i][c], the a
-// converters write y and y - trunc(y) into the stage's Tensor Memory a-slot;
-// the b converters write F - trunc(F) of the b tile into the b-lo tile and
-// leave the b tile as it is (on a diagonal tile b = a: the a converters also
-// write the b-lo tile).  Element (m, k) of a tile sits at sw128_off(m, k), so a
-// 16-byte chunk holds 4 consecutive rows k of one column m.
-constexpr int kStageAlloc = kStageBytes;   // a multiple of 1024: every stage stays 1024-aligned
-
-// Row m of a K-major SW128 tile: its 8 16-byte chunks (K = 4c .. 4c+3).
-__device__ __forceinline__ void load_row(const uint8_t* tile, int m, float (&x)[32]) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const float4 v = *reinterpret_cast<const float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c));
-        x[4 * c] = v.x;
-        x[4 * c + 1] = v.y;
-        x[4 * c + 2] = v.z;
-        x[4 * c + 3] = v.w;
-    }
-}
-
-__device__ __forceinline__ void store_row(uint8_t* tile, int m, const float (&x)[32]) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-        *reinterpret_cast<float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c)) =
-            make_float4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
-}
-
-__global__ void __launch_bounds__(kThreads, 1)
-gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict__ w2, int64_t N, int64_t k,
-               int n_tiles, int64_t rows_per, double* __restrict__ partial, int* __restrict__ err) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageAlloc);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    const int64_t tix = blockIdx.x % n_tiles;
-    const int64_t split = blockIdx.x / n_tiles;
-    int64_t ta, tb;
-    tile_of(tix, ta, tb);
-    const bool diag = (ta == tb);
-    const int64_t a0 = ta * kTT, b0 = tb * kTT;
-    const int64_t r0 = split * rows_per;
-    const int64_t r1 = min(N, r0 + rows_per);
-    const int64_t n_stages = (r1 > r0) ? (r1 - r0 + kTK - 1) / kTK : 0;
-    const int64_t n_chunks = (n_stages + kFlushStages - 1) / kFlushStages;
-    double* out = partial + (int64_t)blockIdx.x * kTT * kTT;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
-            tc::mbar_init(&bar->tma[s], 1);
-            tc::mbar_init(&bar->full[s], kCvtWarps);
-            tc::mbar_init(&bar->empty[s], 1);
-        }
-        for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&bar->accf[b], 1);
-            tc::mbar_init(&bar->acce[b], kEpiWarps * 32);
-        }
-        tc::mbar_init(&bar->done, 1);
-        tc::mbar_fence_init();
-    }
-    if (warp == kMmaWarp) {
-        tc::tmem_alloc(&bar->tmem_base, kTmemCols);
-        tc::tmem_relinquish();
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    tc::tc_fence_after();
-    const uint32_t tbase = bar->tmem_base;
-
-    if (warp == kProdWarp) {
-        // ---------------- TMA producer
-        if (lane == 0) {
-            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes);
-            for (int64_t s = 0; s < n_stages; ++s) {
-                const int slot = (int)(s % kStages);
-                const uint32_t use = (uint32_t)(s / kStages);
-                if (!tc::mbar_wait(&bar->empty[slot], (use & 1u) ^ 1u, kTimeoutNs)) {
-                    atomicExch(err, 1);
-                    break;
-                }
-                uint8_t* st = base + (size_t)slot * kStageAlloc;
-                const int x = (int)(r0 + s * kTK);
-                if (kPrefetch > 0 && s + kPrefetch < n_stages) {
-                    const int xp = (int)(r0 + (s + kPrefetch) * kTK);
-                    tc::tma_prefetch_2d(&tmF, xp, (int)a0);
-                    if (!diag) tc::tma_prefetch_2d(&tmF, xp, (int)b0);
-                }
-                tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes + kTK * 4);
-                tc::bulk_load(bar->w2[slot], w2 + x, kTK * 4, &bar->tma[slot]);
-                tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
-                if (!diag) tc::tma_load_2d(st + kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
-            }
-        }
-        __syncwarp();
-    } else if ((warp >= kCvtWarp0 && warp < kCvtWarp0 + 4) || warp >= kCvtBWarp0) {
-        // ---------------- converters: thread m owns row m of the a tile (warps
-        // 4-7, to Tensor Memory) or of the b tile (warps 10-13, lo part only)
-        const bool grp_a = warp < kProdWarp;
-        const int m = 32 * (warp & 3) + lane;
-        const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);   // this warp's TMEM lanes
-        for (int64_t s = 0; s < n_stages; ++s) {
-            const int slot = (int)(s % kStages);
-            const uint32_t use = (uint32_t)(s / kStages);
-            float x[32], l[32];
-            if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
-                atomicExch(err, 5);
-                break;
-            }
-            uint8_t* st = base + (size_t)slot * kStageAlloc;
-            if (grp_a) {
-                // a operand -> Tensor Memory: y = s^2 x as the hi operand (the
-                // tensor core reads its top 19 bits) and y - trunc(y) as lo; on a
-                // diagonal tile the raw a tile is also b, whose lo part goes to
-                // the b-lo tile
-                const uint32_t ta = tlane + kTmemA + (uint32_t)slot * kTmemASlot;
-                load_row(st, m, x);
-                float y[32];
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot])[c];
-                    y[4 * c + 0] = x[4 * c + 0] * wv.x;
-                    y[4 * c + 1] = x[4 * c + 1] * wv.y;
-                    y[4 * c + 2] = x[4 * c + 2] * wv.z;
-                    y[4 * c + 3] = x[4 * c + 3] * wv.w;
-                }
-#pragma unroll
-                for (int u = 0; u < 32; ++u) l[u] = y[u] - tc::tf32_trunc(y[u]);
-                tc::tmem_st32(ta, y);
-                tc::tmem_st32(ta + 32, l);
-                if (diag) {
-#pragma unroll
-                    for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                    store_row(st + 2 * kOpBytes, m, l);
-                }
-                tc::tmem_wait_st();
-                tc::tc_fence_before();
-            } else if (!diag) {
-                load_row(st + kOpBytes, m, x);
-#pragma unroll
-                for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                store_row(st + 2 * kOpBytes, m, l);
-            }
-            tc::fence_async_smem();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
-        }
-    } else if (warp == kMmaWarp) {
-        // ---------------- MMA issuer.  The tensor core takes an MMA only when
-        // the previous one is nearly done, so every address of a stage is in a
-        // register before its 12 MMAs are issued back to back.
-        if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_tf32(kTT, kTT);
-            // low descriptor words of each slot's b-hi (raw b, or raw a on a
-            // diagonal tile) and b-lo tiles; the high word is a constant
-            uint32_t bh0[kStages], bl0[kStages];
-#pragma unroll
-            for (int sl = 0; sl < kStages; ++sl) {
-                uint8_t* stg = base + (size_t)sl * kStageAlloc;
-                bh0[sl] = tc::desc_lo_sw128(tc::smem_u32(diag ? stg : stg + kOpBytes));
-                bl0[sl] = tc::desc_lo_sw128(tc::smem_u32(stg + 2 * kOpBytes));
-            }
-            bool ok = true;
-            for (int64_t c = 0; c < n_chunks && ok; ++c) {
-                const int tb_ = (int)(c & 1);
-                const uint32_t tuse = (uint32_t)(c >> 1);
-                if (!tc::mbar_wait(&bar->acce[tb_], (tuse & 1u) ^ 1u, kTimeoutNs)) {
-                    ok = false;
-                    break;
-                }
-                tc::tc_fence_after();
-                const uint32_t d = tbase + (uint32_t)(tb_ * kTT);
-                const int64_t s0 = c * kFlushStages;   // a multiple of kStages: slot = s - s0 (mod kStages)
-                const int64_t s1 = min(n_stages, s0 + kFlushStages);
-                for (int64_t sb = s0; sb < s1 && ok; sb += kStages) {
-                    const uint32_t use = (uint32_t)(sb / kStages);
-#pragma unroll
-                    for (int sl = 0; sl < kStages; ++sl) {
-                        if (sb + sl >= s1) break;
-                        if (!tc::mbar_wait(&bar->full[sl], use & 1u, kTimeoutNs)) {
-                            ok = false;
-                            break;
-                        }
-                        tc::tc_fence_after();
-                        const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * kTmemASlot, alo = ahi + 32;
-                        uint64_t dbh[kTK / 8], dbl[kTK / 8];
-#pragma unroll
-                        for (int j = 0; j < kTK / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
-                            dbh[j] = tc::desc_sw128_from_lo(bh0[sl] + 2u * j);
-                            dbl[j] = tc::desc_sw128_from_lo(bl0[sl] + 2u * j);
-                            tc::reg_pin(dbh[j]);
-                            tc::reg_pin(dbl[j]);
-                        }
-                        const uint32_t acc0 = (sb + sl > s0) ? 1u : 0u;
-#pragma unroll
-                        for (int j = 0; j < kTK / 8; ++j) {
-                            tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbl[j], idesc, j > 0 ? 1u : acc0);
-                            tc::mma_tf32_tmem_a(d, alo + 8 * j, dbh[j], idesc, 1u);
-                            tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbh[j], idesc, 1u);
-                        }
-                        tc::mma_commit(&bar->empty[sl]);
-                    }
-                }
-                if (ok) tc::mma_commit(&bar->accf[tb_]);
-            }
-            if (!ok) atomicExch(err, 2);
-            // retire every issued MMA before the TMEM is released
-            tc::mma_commit(&bar->done);
-            if (!tc::mbar_wait(&bar->done, 0u, kTimeoutNs)) atomicExch(err, 3);
-        }
-        __syncwarp();
-    } else {
-        // ---------------- epilogue: warp q owns tile rows 32q..32q+31; the FP64
-        // tile is stored column-major ([n][m]) so a warp's accesses coalesce
-        const int m = warp * 32 + lane;
-        double* orow = out + m;
-        for (int n = 0; n < kTT; ++n) orow[n * kTT] = 0.0;
-        for (int64_t c = 0; c < n_chunks; ++c) {
-            const int tb_ = (int)(c & 1);
-            const uint32_t use = (uint32_t)(c >> 1);
-            if (!tc::mbar_wait(&bar->accf[tb_], use & 1u, kTimeoutNs)) {
-                atomicExch(err, 4);
-                break;
-            }
-            tc::tc_fence_after();
-#pragma unroll 1
-            for (int cb = 0; cb < kTT / 32; ++cb) {
-                float v[32];
-                tc::tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tb_ * kTT + 32 * cb), v);
-                tc::tmem_wait_ld();
-#pragma unroll
-                for (int n = 0; n < 32; ++n) tc::red_add(orow + (32 * cb + n) * kTT, (double)v[n]);
-            }
-            tc::tc_fence_before();
-            tc::mbar_arrive(&bar->acce[tb_]);
-        }
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    tc::tc_fence_after();
-    if (warp == kMmaWarp) tc::tmem_dealloc(tbase, kTmemCols);
-}
-
-// ---------------------------------------------------------------------------
-// Two weighted Grams of the same factor in one pass: G_A = F^T diag(sA)^2 F and
-// G_B = F^T diag(sB)^2 F (the A and B Grams of the bistochastic EVD share F and
-// differ only in the row weights).  Every F tile is loaded and its b side
-// converted once for both: the stage's a tile is scaled twice into Tensor
-// Memory (hi/lo of sA^2 F and of sB^2 F), the raw b tile and its lo part serve
-// both, and 24 MMAs per stage accumulate the two output tiles.  Same precision
-// scheme and FP64 flush as gram_tc_kernel.
-//
-// Tensor Memory: accumulators A [0,128) and B [128,256) (single-buffered: at a
-// flush the MMA waits until the epilogue has read the accumulator it is about
-// to overwrite); two a-slots of 128 columns at [256,512) (hi A, lo A, hi B, lo
-// B, 32 each), handed back by the MMA through tfree barriers.
-namespace dual {
-
-constexpr int kTSlots = 2;
-constexpr uint32_t kTSlotCols = 128;
-
-struct Barriers {
-    alignas(16) float w2[kStages][2][32];   // squared row weights of each stage, A then B
+    alignas(16) float w2[kStages][2][32];   // scaled squared row weights of each stage, A then B
     uint64_t tma[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -375,20 +88,62 @@ struct Barriers {
 
 constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
-static_assert(2 * kTT + kTSlots * kTSlotCols <= kTmemCols, "Tensor Memory holds 512 columns");
-static_assert(kFlushStages % kStages == 0 && kStages % kTSlots == 0, "slot indices are compile-time per stage");
 
-}  // namespace dual
+// Power-of-two scale exponents of one Gram call (device, per factor column c):
+// eb[c] for the b side, ea[g][c] for the a side of Gram g.
+struct GramExp {
+    const int* eb;
+    const int* ea0;
+    const int* ea1;
+};
 
+__device__ __forceinline__ void tile_of(int64_t t, int64_t& ta, int64_t& tb) {
+    int64_t i = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    ta = i;
+    tb = t - i * (i + 1) / 2;
+}
+
+// Row m of a K-major SW128 tile of FP32: its 8 16-byte chunks (K = 4c .. 4c+3).
+// The TMA writes the raw FT boxes (128 factor columns x 32 rows) this way, so
+// a 16-byte chunk holds 4 consecutive rows k of one column m.
+__device__ __forceinline__ void load_row(const uint8_t* tile, int m, float (&x)[32]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const float4 v = *reinterpret_cast<const float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c));
+        x[4 * c] = v.x;
+        x[4 * c + 1] = v.y;
+        x[4 * c + 2] = v.z;
+        x[4 * c + 3] = v.w;
+    }
+}
+
+// Row m of the b-hi and b-lo tiles from the 32 raw values of b row m.
+__device__ __forceinline__ void store_b_split(uint8_t* st, int m, const float (&x)[32], float bscale) {
+    uint32_t h[16], l[16];
+#pragma unroll
+    for (int p = 0; p < 16; ++p) tc::split_f16x2(x[2 * p] * bscale, x[2 * p + 1] * bscale, h[p], l[p]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const uint32_t off = tc::sw64_off16((uint32_t)m, 8u * c);
+        *reinterpret_cast<uint4*>(st + kOffBh + off) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+        *reinterpret_cast<uint4*>(st + kOffBl + off) = make_uint4(l[4 * c], l[4 * c + 1], l[4 * c + 2], l[4 * c + 3]);
+    }
+}
+
+// NG weighted Grams of the same factor in one pass: G_g = F^T diag(s_g)^2 F.
+// Every F tile is loaded and its b side split once for all of them: the
+// stage's a tile is weighted NG times into Tensor Memory and 6 MMAs per stage
+// and Gram accumulate the output tiles.
+template <int NG>
 __global__ void __launch_bounds__(kThreads, 1)
-gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict__ w2a, const float* __restrict__ w2b,
-                int64_t N, int64_t k, int n_tiles, int64_t rows_per, double* __restrict__ partial,
-                float* __restrict__ scratch, int n_scratch, int* __restrict__ err) {
-    using dual::kTSlots;
-    using dual::kTSlotCols;
+gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict__ w2a, const float* __restrict__ w2b,
+               GramExp ex, int64_t N, int64_t k, int n_tiles, int64_t rows_per,
+               double* __restrict__ partial, float* __restrict__ scratch, int n_scratch, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    dual::Barriers* bar = reinterpret_cast<dual::Barriers*>(base + (size_t)kStages * kStageAlloc);
+    Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     const int64_t tix = blockIdx.x % n_tiles;
@@ -401,8 +156,8 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
     const int64_t r1 = min(N, r0 + rows_per);
     const int64_t n_stages = (r1 > r0) ? (r1 - r0 + kTK - 1) / kTK : 0;
     const int64_t n_chunks = (n_stages + kFlushStages - 1) / kFlushStages;
-    double* out = partial + (int64_t)blockIdx.x * 2 * kTT * kTT;   // [G][n][m]
-    // FP32 staging of the two accumulators at a flush, one per SM (one CTA per
+    double* out = partial + (int64_t)blockIdx.x * NG * kTT * kTT;   // [G][n][m]
+    // FP32 staging of the accumulators at a flush, one per SM (one CTA per
     // SM: shared memory and Tensor Memory both admit only one)
     uint32_t smid, nsmid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
@@ -411,7 +166,7 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
         if (threadIdx.x == 0) atomicExch(err, 7);
         return;
     }
-    float* scr = scratch + (size_t)smid * 2 * kTT * kTT;   // [G][n][m]
+    float* scr = scratch + (size_t)smid * NG * kTT * kTT;   // [G][n][m]
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -436,9 +191,9 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
     const uint32_t tbase = bar->tmem_base;
 
     if (warp == kProdWarp) {
-        // ---------------- TMA producer: raw a and b tiles and both weight rows
+        // ---------------- TMA producer: raw a and b tiles and the weight rows
         if (lane == 0) {
-            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes) + 2 * kTK * 4;
+            const uint32_t bytes = (uint32_t)(diag ? kOpBytes : 2 * kOpBytes) + NG * kTK * 4;
             for (int64_t s = 0; s < n_stages; ++s) {
                 const int slot = (int)(s % kStages);
                 const uint32_t use = (uint32_t)(s / kStages);
@@ -446,31 +201,38 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                     atomicExch(err, 1);
                     break;
                 }
-                uint8_t* st = base + (size_t)slot * kStageAlloc;
+                uint8_t* st = base + (size_t)slot * kStageBytes;
                 const int x = (int)(r0 + s * kTK);
                 tc::mbar_arrive_expect_tx(&bar->tma[slot], bytes);
                 tc::bulk_load(bar->w2[slot][0], w2a + x, kTK * 4, &bar->tma[slot]);
-                tc::bulk_load(bar->w2[slot][1], w2b + x, kTK * 4, &bar->tma[slot]);
+                if (NG == 2) tc::bulk_load(bar->w2[slot][1], w2b + x, kTK * 4, &bar->tma[slot]);
                 tc::tma_load_2d(st, &tmF, x, (int)a0, &bar->tma[slot]);
-                if (!diag) tc::tma_load_2d(st + kOpBytes, &tmF, x, (int)b0, &bar->tma[slot]);
+                if (!diag) tc::tma_load_2d(st + kOffB, &tmF, x, (int)b0, &bar->tma[slot]);
             }
         }
         __syncwarp();
     } else if ((warp >= kCvtWarp0 && warp < kCvtWarp0 + 4) || warp >= kCvtBWarp0) {
-        // ---------------- converters (a: both scaled copies into the stage's
-        // Tensor Memory a-slot; b: lo part into the b-lo tile)
+        // ---------------- converters (a: the weighted copies into the stage's
+        // Tensor Memory a-slot; b: the split into the b-hi and b-lo tiles)
         const bool grp_a = warp < kProdWarp;
         const int m = 32 * (warp & 3) + lane;
         const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
+        // this thread's column scales (a converters: column a0 + m, which is
+        // also the b column of a diagonal tile; b converters: column b0 + m)
+        const int64_t cm = (grp_a ? a0 : b0) + m;
+        const bool cin = cm < k;
+        const float bscale = cin ? ldexpf(1.f, ex.eb[cm]) : 1.f;
+        const float as0 = (grp_a && cin) ? ldexpf(1.f, ex.ea0[cm]) : 1.f;
+        const float as1 = (grp_a && cin && NG == 2) ? ldexpf(1.f, ex.ea1[cm]) : 1.f;
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
-            float x[32], l[32];
+            float x[32];
             if (!tc::mbar_wait(&bar->tma[slot], use & 1u, kTimeoutNs)) {
                 atomicExch(err, 5);
                 break;
             }
-            uint8_t* st = base + (size_t)slot * kStageAlloc;
+            uint8_t* st = base + (size_t)slot * kStageBytes;
             if (grp_a) {
                 const int ts = (int)(s % kTSlots);
                 const uint32_t tuse = (uint32_t)(s / kTSlots);
@@ -482,50 +244,38 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                 tc::tc_fence_after();
                 const uint32_t ta_ = tlane + kTmemA + (uint32_t)ts * kTSlotCols;
 #pragma unroll
-                for (int gsel = 0; gsel < 2; ++gsel) {
-                    float y[32];
+                for (int gsel = 0; gsel < NG; ++gsel) {
+                    // y = (s^2 F) 2^ea: the power of two scales the rounded
+                    // product exactly.  Words 0..15: hi pairs (rows 2p, 2p+1),
+                    // words 16..31: lo pairs
+                    const float as = gsel ? as1 : as0;
+                    uint32_t w[32];
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
                         const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot][gsel])[c];
-                        y[4 * c + 0] = x[4 * c + 0] * wv.x;
-                        y[4 * c + 1] = x[4 * c + 1] * wv.y;
-                        y[4 * c + 2] = x[4 * c + 2] * wv.z;
-                        y[4 * c + 3] = x[4 * c + 3] * wv.w;
+                        tc::split_f16x2((x[4 * c + 0] * wv.x) * as, (x[4 * c + 1] * wv.y) * as, w[2 * c],
+                                        w[16 + 2 * c]);
+                        tc::split_f16x2((x[4 * c + 2] * wv.z) * as, (x[4 * c + 3] * wv.w) * as, w[2 * c + 1],
+                                        w[17 + 2 * c]);
                     }
-#pragma unroll
-                    for (int u = 0; u < 32; ++u) l[u] = y[u] - tc::tf32_trunc(y[u]);
-                    tc::tmem_st32(ta_ + 64u * gsel, y);
-                    tc::tmem_st32(ta_ + 64u * gsel + 32u, l);
+                    tc::tmem_st32u(ta_ + 32u * gsel, w);
                 }
-                if (diag) {
-#pragma unroll
-                    for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                    store_row(st + 2 * kOpBytes, m, l);
-                }
+                if (diag) store_b_split(st, m, x, bscale);
                 tc::tmem_wait_st();
                 tc::tc_fence_before();
             } else if (!diag) {
-                load_row(st + kOpBytes, m, x);
-#pragma unroll
-                for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                store_row(st + 2 * kOpBytes, m, l);
+                load_row(st + kOffB, m, x);
+                store_b_split(st, m, x, bscale);
             }
             tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }
     } else if (warp == kMmaWarp) {
-        // ---------------- MMA issuer: per stage 12 MMAs into accumulator A,
-        // then 12 into B, from descriptors held in registers
+        // ---------------- MMA issuer: per stage 6 MMAs into each accumulator
+        // from descriptors held in registers
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_tf32(kTT, kTT);
-            uint32_t bh0[kStages], bl0[kStages];
-#pragma unroll
-            for (int sl = 0; sl < kStages; ++sl) {
-                uint8_t* stg = base + (size_t)sl * kStageAlloc;
-                bh0[sl] = tc::desc_lo_sw128(tc::smem_u32(diag ? stg : stg + kOpBytes));
-                bl0[sl] = tc::desc_lo_sw128(tc::smem_u32(stg + 2 * kOpBytes));
-            }
+            constexpr uint32_t idesc = tc::idesc_f16(kTT, kTT);
             bool ok = true;
             for (int64_t c = 0; c < n_chunks && ok; ++c) {
                 const int64_t s0 = c * kFlushStages;
@@ -536,11 +286,12 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                     for (int sl = 0; sl < kStages; ++sl) {
                         if (sb + sl >= s1) break;
                         const int ts = sl % kTSlots;   // sb is a multiple of kStages, hence of kTSlots
-                        uint64_t dbh[kTK / 8], dbl[kTK / 8];
+                        uint64_t dbh[kTK / 16], dbl[kTK / 16];
+                        const uint32_t bh = tc::smem_u32(base + (size_t)sl * kStageBytes + kOffBh);
 #pragma unroll
-                        for (int j = 0; j < kTK / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
-                            dbh[j] = tc::desc_sw128_from_lo(bh0[sl] + 2u * j);
-                            dbl[j] = tc::desc_sw128_from_lo(bl0[sl] + 2u * j);
+                        for (int j = 0; j < kTK / 16; ++j) {   // +32 bytes of K per MMA
+                            dbh[j] = tc::desc_sw64(bh + 32u * j);
+                            dbl[j] = tc::desc_sw64(bh + kHalfBytes + 32u * j);
                             tc::reg_pin(dbh[j]);
                             tc::reg_pin(dbl[j]);
                         }
@@ -551,7 +302,7 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                         tc::tc_fence_after();
                         const bool first = (sb + sl == s0);
 #pragma unroll
-                        for (int gsel = 0; gsel < 2; ++gsel) {
+                        for (int gsel = 0; gsel < NG; ++gsel) {
                             if (first && c > 0) {
                                 // the epilogue has read this accumulator's previous chunk
                                 if (!tc::mbar_wait(&bar->acce[gsel], (uint32_t)((c - 1) & 1), kTimeoutNs)) {
@@ -561,15 +312,16 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                                 tc::tc_fence_after();
                             }
                             const uint32_t d = tbase + (uint32_t)(gsel * kTT);
-                            const uint32_t ahi = tbase + kTmemA + (uint32_t)ts * kTSlotCols + 64u * gsel;
-                            const uint32_t alo = ahi + 32u;
+                            const uint32_t ahi = tbase + kTmemA + (uint32_t)ts * kTSlotCols + 32u * gsel;
+                            const uint32_t alo = ahi + 16u;
                             const uint32_t acc0 = first ? 0u : 1u;
 #pragma unroll
-                            for (int j = 0; j < kTK / 8; ++j) {
-                                tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbl[j], idesc, j > 0 ? 1u : acc0);
-                                tc::mma_tf32_tmem_a(d, alo + 8 * j, dbh[j], idesc, 1u);
-                                tc::mma_tf32_tmem_a(d, ahi + 8 * j, dbh[j], idesc, 1u);
+                            for (int j = 0; j < kTK / 16; ++j) {
+                                tc::mma_f16_tmem_a(d, ahi + 8u * j, dbl[j], idesc, j > 0 ? 1u : acc0);
+                                tc::mma_f16_tmem_a(d, alo + 8u * j, dbh[j], idesc, 1u);
                             }
+#pragma unroll
+                            for (int j = 0; j < kTK / 16; ++j) tc::mma_f16_tmem_a(d, ahi + 8u * j, dbh[j], idesc, 1u);
                         }
                         if (!ok) break;
                         tc::mma_commit(&bar->empty[sl]);
@@ -585,13 +337,10 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue: warp q owns tile rows 32q..32q+31 of both
-        // accumulators; FP64 tiles column-major ([n][m]), A then B
+        // ---------------- epilogue: warp q owns tile rows 32q..32q+31 of the
+        // accumulators; FP64 tiles column-major ([n][m]), Gram after Gram
         const int m = warp * 32 + lane;
-        for (int n = 0; n < kTT; ++n) {
-            out[n * kTT + m] = 0.0;
-            out[kTT * kTT + n * kTT + m] = 0.0;
-        }
+        for (int n = 0; n < NG * kTT; ++n) out[n * kTT + m] = 0.0;
         bool ok = true;
         for (int64_t c = 0; c < n_chunks && ok; ++c) {
             if (!tc::mbar_wait(&bar->accf, (uint32_t)(c & 1), kTimeoutNs)) {
@@ -600,11 +349,11 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
                 break;
             }
             tc::tc_fence_after();
-            // 1. both FP32 accumulators -> this SM's scratch (plain stores, no
+            // 1. the FP32 accumulators -> this SM's scratch (plain stores, no
             //    waiting on memory), each handed back to the MMA as soon as it
             //    is read
 #pragma unroll 1
-            for (int gsel = 0; gsel < 2; ++gsel) {
+            for (int gsel = 0; gsel < NG; ++gsel) {
                 const uint32_t tacc = tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(gsel * kTT);
                 float* srow = scr + (size_t)gsel * kTT * kTT + m;
 #pragma unroll 1
@@ -623,7 +372,7 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
             // 2. fold into the FP64 tiles while the MMA runs the next chunk (the
             //    thread reads back only what it wrote)
 #pragma unroll 1
-            for (int e0 = 0; e0 < 2 * kTT; e0 += 16) {
+            for (int e0 = 0; e0 < NG * kTT; e0 += 16) {
                 double o[16];
                 float v[16];
 #pragma unroll
@@ -642,6 +391,33 @@ gram2_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict
     if (warp == kMmaWarp) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
+// max(s_i^2) over i < N of each weight vector into mx[g] (float bits, atomicMax).
+__global__ void gram_wmax_kernel(const double* __restrict__ s, const double* __restrict__ s2, int64_t N,
+                                 unsigned* __restrict__ mx) {
+    float m0 = 0.f, m1 = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        m0 = fmaxf(m0, (float)(s[i] * s[i]));
+        if (s2) m1 = fmaxf(m1, (float)(s2[i] * s2[i]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(mx, __float_as_uint(m0));
+        if (s2) atomicMax(mx + 1, __float_as_uint(m1));
+    }
+}
+
+// e with 2^e v <= 2^14 < 2^(e+1) v for v > 0 (v = 0 or not finite: 0).
+__device__ __forceinline__ int f16_range_exp(double v) {
+    if (!(v > 0.0) || !isfinite(v)) return 0;
+    int e;
+    frexp(v, &e);   // v = f 2^e, 0.5 <= f < 1
+    return 14 - e;
+}
+
 // w2[i] = s_i^2 rounded to FP32 for i < N, zero up to len (the last stage of
 // the last row split may run past N).
 __global__ void gram_w2_kernel(const double* __restrict__ s, const double* __restrict__ s2, int64_t N, int64_t len,
@@ -652,11 +428,24 @@ __global__ void gram_w2_kernel(const double* __restrict__ s, const double* __res
     }
 }
 
-// Sum the row-split partial tiles and write the full symmetric k x k matrix
-// (column-major).
+// Per-column scale exponents from max |F(:, c)| (colmax, float bits) and
+// max s^2 of each Gram (wmax, float bits).
+__global__ void gram_exp_kernel(const unsigned* __restrict__ colmax, const unsigned* __restrict__ wmax, int nG,
+                                int64_t k, int* __restrict__ eb, int* __restrict__ ea0, int* __restrict__ ea1) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    const double cm = (double)__uint_as_float(colmax[c]);
+    eb[c] = f16_range_exp(cm);
+    ea0[c] = f16_range_exp(cm * (double)__uint_as_float(wmax[0]));
+    if (nG == 2) ea1[c] = f16_range_exp(cm * (double)__uint_as_float(wmax[1]));
+}
+
+// Sum the row-split partial tiles, remove the scale, and write the full
+// symmetric k x k matrix (column-major).
 // Partial tile of (split p, tile t, Gram g) at ((p * n_tiles + t) * nG + g) * kTT^2.
 __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_tiles, int n_split, int nG, int g,
-                                      int64_t k, double* __restrict__ G) {
+                                      int64_t k, const int* __restrict__ ea, const int* __restrict__ eb,
+                                      double* __restrict__ G) {
     const int64_t t = blockIdx.x;
     int64_t ta, tb;
     tile_of(t, ta, tb);
@@ -669,6 +458,7 @@ __global__ void gram_tc_reduce_kernel(const double* __restrict__ partial, int n_
         if (ta == tb && ia < ib) continue;
         double s = 0.0;
         for (int p = 0; p < n_split; ++p) s += partial[(((int64_t)p * n_tiles + t) * nG + g) * kTT * kTT + e];
+        s = ldexp(s, -(ea[ga] + eb[gb]));   // the a side scales column ga, the b side column gb
         G[gb * k + ga] = s;
         G[ga * k + gb] = s;
     }
@@ -692,16 +482,41 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // FT[c * ldT + i] = F[i * ldF + c]: 64 x 64 tiles through shared memory, read
 // and written in 16-byte pieces where a piece lies inside the matrix and its
 // row stride allows (F rows: ldF % 4 == 0; FT rows: ldT % 4 == 0 always), else
-// element by element.
+// element by element.  Also max |F(:, c)| of every column into colmax[c]
+// (bits of a non-negative float, so unsigned order is float order; colmax
+// starts at 0): thread tid writes rows 4 (tid & 15) .. +3 of tile columns
+// (tid >> 4) + 16 j, the same columns in every tile, so it keeps their maxima
+// while its tiles stay in one column panel and flushes them (16-lane
+// reduction, one atomic per column) when the panel changes.
+__device__ __forceinline__ void flush_colmax(float (&mx)[4], int64_t c0, int64_t k, int tid,
+                                             unsigned* __restrict__ colmax) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float m = mx[j];
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const int64_t c = c0 + (tid >> 4) + 16 * j;
+        if ((tid & 15) == 0 && c < k) atomicMax(colmax + c, __float_as_uint(m));
+        mx[j] = 0.f;
+    }
+}
+
 __global__ void __launch_bounds__(256) transpose_kernel(const float* __restrict__ F, int64_t ldF, int64_t N,
-                                                        int64_t k, float* __restrict__ FT, int64_t ldT) {
+                                                        int64_t k, float* __restrict__ FT, int64_t ldT,
+                                                        unsigned* __restrict__ colmax) {
     __shared__ float t[64][65];
+    float mx[4] = {0.f, 0.f, 0.f, 0.f};
+    int64_t cur_c0 = -1;
     const int64_t n_ti = (N + 63) / 64, n_tc = (k + 63) / 64;
     const bool vec_in = (ldF % 4) == 0 && ((uintptr_t)F % 16) == 0;
     const bool vec_out = (ldT % 4) == 0 && ((uintptr_t)FT % 16) == 0;
     const int tid = threadIdx.x;
     for (int64_t tile = blockIdx.x; tile < n_ti * n_tc; tile += gridDim.x) {
         const int64_t i0 = (tile % n_ti) * 64, c0 = (tile / n_ti) * 64;
+        if (c0 != cur_c0) {   // uniform over the CTA
+            if (cur_c0 >= 0) flush_colmax(mx, cur_c0, k, tid, colmax);
+            cur_c0 = c0;
+        }
         __syncthreads();
         for (int e = tid; e < 64 * 16; e += 256) {
             const int r = e >> 4, c4 = (e & 15) * 4;   // row r, columns c4..c4+3 of the tile
@@ -717,6 +532,8 @@ __global__ void __launch_bounds__(256) transpose_kernel(const float* __restrict_
         __syncthreads();
         for (int e = tid; e < 64 * 16; e += 256) {
             const int cc = e >> 4, r4 = (e & 15) * 4;   // FT row c0 + cc, rows i0 + r4..+3
+            mx[e >> 8] = fmaxf(mx[e >> 8], fmaxf(fmaxf(fabsf(t[r4][cc]), fabsf(t[r4 + 1][cc])),
+                                                 fmaxf(fabsf(t[r4 + 2][cc]), fabsf(t[r4 + 3][cc]))));
             const int64_t c = c0 + cc, i = i0 + r4;
             if (c >= k) continue;
             if (vec_out && i + 3 < ldT) {
@@ -729,24 +546,26 @@ __global__ void __launch_bounds__(256) transpose_kernel(const float* __restrict_
             }
         }
     }
+    if (cur_c0 >= 0) flush_colmax(mx, cur_c0, k, tid, colmax);
 }
-
 }  // namespace
 
-// Column-major copy FT (k x ldT, ldT = N rounded up to 4) of a row-major FP32 factor.
+// Column-major copy FT (k x ldT, ldT = N rounded up to 4) of a row-major FP32
+// factor, and max |F(:, c)| into colmax[c] (k float bits; the call resets them).
 int run_transpose_f32(kevd_ctx* ctx, const float* F, int64_t ldF, int64_t N, int64_t k, float* FT, int64_t ldT,
-                      cudaStream_t st) {
+                      unsigned* colmax, cudaStream_t st) {
     ProfScope ps(ctx, "ev_transpose", st);
+    KEVD_CUDA(ctx, cudaMemsetAsync(colmax, 0, (size_t)k * sizeof(unsigned), st));
     const int64_t tiles = ((N + 63) / 64) * ((k + 63) / 64);
     const int grid = (int)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 8);
-    transpose_kernel<<<grid, 256, 0, st>>>(F, ldF, N, k, FT, ldT);
+    transpose_kernel<<<grid, 256, 0, st>>>(F, ldF, N, k, FT, ldT, colmax);
     KEVD_LAUNCH(ctx);
     return KEVD_OK;
 }
 
 // Shared host path of the one- and two-Gram kernels (s2 == nullptr: one).
-static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s,
-                        const double* s2, double* G, double* G2, cudaStream_t st) {
+static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const unsigned* colmax,
+                        const double* s, const double* s2, double* G, double* G2, cudaStream_t st) {
     const int nG = s2 ? 2 : 1;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     if (!enc) return set_error(ctx, KEVD_ERR_CUDA, "gram_tc: cuTensorMapEncodeTiled unavailable");
@@ -777,37 +596,44 @@ static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, 
     int rc = KEVD_OK;
     double* partial = arena_get<double>(ctx, "tc.gpart", (size_t)n_split * n_tiles * nG * kTT * kTT, &rc);
     int* err = arena_get<int>(ctx, "tc.err", 1, &rc);
+    unsigned* wmax = arena_get<unsigned>(ctx, "tc.wmax", 2, &rc);
+    int* exps = arena_get<int>(ctx, "tc.exps", (size_t)3 * k, &rc);   // eb, ea0, ea1
     // squared weights, one 128-byte bulk copy per stage (row offsets are
     // multiples of 32, so every copy is 128-byte aligned)
     const int64_t w2_len = (N + kTK - 1) / kTK * kTK + kTK;
     float* w2 = arena_get<float>(ctx, "tc.w2", (size_t)w2_len, &rc);
     float* w22 = s2 ? arena_get<float>(ctx, "tc.w2b", (size_t)w2_len, &rc) : nullptr;
+    // FP32 flush staging indexed by SM id (ids below %nsmid; the kernel checks
+    // the bound and reports code 7 if it is exceeded)
+    const int n_scratch = std::max(256, 2 * ctx->num_sms);
+    float* scratch = arena_get<float>(ctx, "tc.gscr", (size_t)n_scratch * nG * kTT * kTT, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
     KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
-    gram_w2_kernel<<<(int)std::min<int64_t>((w2_len + 255) / 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(
-        s, s2, N, w2_len, w2, w22);
+    KEVD_CUDA(ctx, cudaMemsetAsync(wmax, 0, 2 * sizeof(unsigned), st));
+    const int wgrid = (int)std::min<int64_t>((w2_len + 255) / 256, (int64_t)ctx->num_sms * 8);
+    gram_wmax_kernel<<<wgrid, 256, 0, st>>>(s, s2, N, wmax);
     KEVD_LAUNCH(ctx);
-    if (nG == 1) {
-        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel), (int)kSmemBytes));
+    gram_w2_kernel<<<wgrid, 256, 0, st>>>(s, s2, N, w2_len, w2, w22);
+    KEVD_LAUNCH(ctx);
+    const GramExp ex{exps, exps + k, exps + 2 * k};
+    gram_exp_kernel<<<ceil_div(k, 256), 256, 0, st>>>(colmax, wmax, nG, k, exps, exps + k, exps + 2 * k);
+    KEVD_LAUNCH(ctx);
+    {
         ProfScope ps(ctx, "gram_tc", st);
-        gram_tc_kernel<<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(tmF, w2, N, k, n_tiles, rows_per, partial,
-                                                                       err);
-        KEVD_LAUNCH(ctx);
-    } else {
-        KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram2_tc_kernel), (int)dual::kSmemBytes));
-        ProfScope ps(ctx, "gram_tc", st);
-        // FP32 flush staging indexed by SM id (ids below %nsmid; the kernel
-        // checks the bound and reports code 7 if it is exceeded)
-        const int n_scratch = std::max(256, 2 * ctx->num_sms);
-        float* scratch = arena_get<float>(ctx, "tc.gscr", (size_t)n_scratch * 2 * kTT * kTT, &rc);
-        if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
-        gram2_tc_kernel<<<n_tiles * n_split, kThreads, dual::kSmemBytes, st>>>(tmF, w2, w22, N, k, n_tiles,
-                                                                              rows_per, partial, scratch,
-                                                                              n_scratch, err);
+        if (nG == 1) {
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel<1>), (int)kSmemBytes));
+            gram_tc_kernel<1><<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(
+                tmF, w2, w2, ex, N, k, n_tiles, rows_per, partial, scratch, n_scratch, err);
+        } else {
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel<2>), (int)kSmemBytes));
+            gram_tc_kernel<2><<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(
+                tmF, w2, w22, ex, N, k, n_tiles, rows_per, partial, scratch, n_scratch, err);
+        }
         KEVD_LAUNCH(ctx);
     }
     for (int g = 0; g < nG; ++g) {
-        gram_tc_reduce_kernel<<<n_tiles, 256, 0, st>>>(partial, n_tiles, n_split, nG, g, k, g ? G2 : G);
+        gram_tc_reduce_kernel<<<n_tiles, 256, 0, st>>>(partial, n_tiles, n_split, nG, g, k, g ? ex.ea1 : ex.ea0,
+                                                        ex.eb, g ? G2 : G);
         KEVD_LAUNCH(ctx);
     }
     int herr = 0;
@@ -818,16 +644,17 @@ static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, 
 }
 
 // G (k x k, column-major, full) = F^T diag(s)^2 F from the column-major FP32
-// factor FT (k x ldT).  s: device, N doubles.
-int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s, double* G,
-                cudaStream_t st) {
-    return gram_tc_impl(ctx, FT, ldT, N, k, s, nullptr, G, nullptr, st);
+// factor FT (k x ldT) and its column maxima (colmax, device float bits, as
+// written by run_transpose_f32).  s: device, N doubles.
+int run_gram_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const unsigned* colmax,
+                const double* s, double* G, cudaStream_t st) {
+    return gram_tc_impl(ctx, FT, ldT, N, k, colmax, s, nullptr, G, nullptr, st);
 }
 
 // G = F^T diag(s)^2 F and G2 = F^T diag(s2)^2 F in one pass over F.
-int run_gram2_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const double* s,
-                 const double* s2, double* G, double* G2, cudaStream_t st) {
-    return gram_tc_impl(ctx, FT, ldT, N, k, s, s2, G, G2, st);
+int run_gram2_tc(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, int64_t k, const unsigned* colmax,
+                 const double* s, const double* s2, double* G, double* G2, cudaStream_t st) {
+    return gram_tc_impl(ctx, FT, ldT, N, k, colmax, s, s2, G, G2, st);
 }
 
 }  // namespace kevd

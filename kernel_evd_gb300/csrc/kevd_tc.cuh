@@ -254,6 +254,24 @@ __device__ __forceinline__ void mma_tf32_tmem_a(uint32_t d_tmem, uint32_t a_tmem
         : "memory");
 }
 
+// Instruction descriptor, kind::f16: D f32, A and B f16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A * B^T, kind::f16, A read from Tensor Memory (row m in lane m,
+// 16 elements of K in 8 consecutive 32-bit columns, two per column with the
+// lower K index in the low half) and B from shared memory.
+__device__ __forceinline__ void mma_f16_tmem_a(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                               uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrive on bar once every previously issued tcgen05.mma of this thread is done.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -265,6 +283,51 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 // (32 elements of K per 128-byte row).
 __host__ __device__ constexpr uint32_t sw128_off(uint32_t row, uint32_t k) {
     return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + (k & 3u) * 4u;
+}
+
+// Shared-memory matrix descriptor split into its two 32-bit words for a
+// K-major SWIZZLE_64B tile (64-byte rows = 32 16-bit elements of K, 8-row
+// atoms of 512 B = the stride byte offset, descriptor version 1, base aligned
+// to 512 B).  Adding 2 to the low word moves the start by 32 bytes (one
+// kind::f16 MMA's K) within a row.
+__host__ __device__ constexpr uint32_t desc_hi_sw64() {
+    return (512u >> 4) | (1u << (46 - 32)) | (4u << (61 - 32));
+}
+__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+    return ((uint64_t)desc_hi_sw64() << 32) | (((saddr & 0x3FFFFu) >> 4) | (1u << 16));
+}
+
+// Byte offset of 16-bit element (row, k) in a K-major SW64 tile: 64-byte rows,
+// 16-byte chunk index (address bits 4-5) XORed with address bits 7-8.
+__host__ __device__ constexpr uint32_t sw64_off16(uint32_t row, uint32_t k) {
+    return (row >> 3) * 512u + (row & 7u) * 64u + ((((k >> 3) ^ ((row >> 1) & 3u)) & 3u) << 4) + (k & 7u) * 2u;
+}
+
+// Two-term f16 split of a pair of FP32 values already scaled into f16 range:
+// hi = rn_f16(s), lo = rn_f16(s - hi) (s - hi is exact in FP32), both
+// saturating at the largest finite f16; packed two per word, s0 in the low
+// half.  hi + lo carries 22 significant bits of s (the lo rounding error is
+// at most 2^-12 |s - hi|, or half an f16 subnormal step, 2^-25).
+__device__ __forceinline__ void split_f16x2(float s0, float s1, uint32_t& hi, uint32_t& lo) {
+    asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(s1), "f"(s0));
+    const unsigned short h0 = (unsigned short)(hi & 0xFFFFu), h1 = (unsigned short)(hi >> 16);
+    float f0, f1;
+    asm("cvt.f32.f16 %0, %1;" : "=f"(f0) : "h"(h0));
+    asm("cvt.f32.f16 %0, %1;" : "=f"(f1) : "h"(h1));
+    asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(s1 - f1), "f"(s0 - f0));
+}
+
+// 32 lanes x 32 consecutive 32-bit columns from raw words.
+__device__ __forceinline__ void tmem_st32u(uint32_t taddr, const uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+        : "memory");
 }
 
 // *p += v in global memory without waiting for the old value (red.global.add,

@@ -3,46 +3,51 @@
 // factor stored):
 //
 //   for every 128-row block R:
-//     P = F(R, 0:r) F(S_i, 0:r)^T                    tcgen05, 3xTF32
+//     P = F(R, 0:r) F(S_i, 0:r)^T                    tcgen05, two-term f16 split
 //     T = K(R, S_i) - P      (K(:, S_i) by update_kcols_kernel, FP32 direct distances)
 //     G = T L_i^{-T};  F(R, r:r+nacc) = G
 //     d(R) <- max(d(R) - rowsq(G), 0)  (FP64);  block sum of d for the sampler
 //
-// Precision.  F elements are split a = hi + lo with hi = rn_tf32(a),
-// lo = rn_tf32(a - hi) (exact tf32 values, unbiased split); each 32-column
-// stage accumulates hi_a hi_b + lo_a hi_b and, in a second accumulator,
-// hi_a lo_b; every stage uses a fresh TMEM partial (eight MMA updates of the
-// first accumulator), and the epilogue sums the partials in FP32 registers
-// with round-to-nearest, so the tensor-core accumulator's one-sided rounding
-// never builds up over r.  (Top-32 eigenvalue error against FP64 on the same
-// pivots at N = 2M, k = 2000, five seeds: one stage per partial median 6.6e-9,
-// max 8.4e-9; two stages per partial median 1.6e-8; lo_a hi_b moved into the
-// second accumulator median 8.0e-9, max 1.0e-8.  One-stage partials cost about
-// 5 % more update time than two.)
+// Precision.  F elements are scaled by 2^14 and split in two f16 parts,
+// hi = rn_f16(a), lo = rn_f16(a - hi): 22 significant bits, the precision of
+// a two-term tf32 split, at twice the kind::tf32 rate and half its operand
+// bytes (|F| <= 1 keeps every scaled value inside the f16 range).  Each
+// 32-column stage accumulates, into a fresh TMEM partial, hi_a hi_b in one
+// 64-column accumulator and the cross terms hi_a lo_b + lo_a hi_b (2^-11
+// smaller) in a second; the epilogue sums the partials in FP32 registers with
+// round-to-nearest, so the tensor core's one-sided accumulator rounding never
+// builds up over r, and removes the 2^28 scale exactly.  That bias is
+// systematic, so it does not average out in the eigenvalues: top-32 error
+// against FP64 on the same pivots at N = 2M, k = 2000 over five seeds, max
+// (median): cross terms in the hi_a hi_b accumulator 1.13e-8 (9.7e-9), in one
+// accumulator per 128-row block 1.09e-8 (1.0e-8), a fresh one per stage
+// 9.2e-9 (8.4e-9).
 //
 // CTA (576 threads, persistent over row blocks):
 //   warp 0     TMA producer: F(R, c:c+32) tiles (128 x 32 fp32, SWIZZLE_128B)
-//              and the pre-split S_i tiles (bulk copy)
+//              and the pre-split S_i tiles (bulk copy, f16 SWIZZLE_64B)
 //   warp 1     TMEM allocation and the single MMA-issuing thread (A from
-//              Tensor Memory, B from shared memory); a stage's 8 MMAs are
-//              issued back to back from descriptors computed before its wait
-//              (a 128 x 64 x 8 kind::tf32 MMA takes 48 cycles that way on
-//              GB300, and each dependent instruction between two MMAs adds
-//              its latency)
+//              Tensor Memory, B from shared memory); a stage's 4 kind::f16
+//              MMAs (K = 16) are issued back to back from descriptors
+//              computed before its wait
 //   warps 2,3,8,9 and 10-13  converters, two groups of four taking alternate
 //              stages: thread m owns row m of the F tile (its TMEM lane
-//              quarter is warp % 4), zeroes columns >= r and writes the hi and
-//              lo parts into the stage's Tensor Memory a-slot (tcgen05.st)
+//              quarter is warp % 4), zeroes columns >= r and writes the packed
+//              hi and lo pairs into the stage's Tensor Memory a-slot
+//              (tcgen05.st)
 //   warps 4-7  epilogue (TMEM lane quarter = warp % 4 = tile rows): sums the
 //              partials of a row block and leaves T = K - P in the K tile
 //   warps 14-17 tail: G = T L_i^{-T}, the d update, the F write and the block
 //              sum of d for one row block while the other roles run ahead on
-//              the next ones
-// Ring of 4 stages (shared-memory tiles + Tensor Memory a-slots of 64 columns)
+//              the next ones; also the TMA loads of the K(R, S_i) tiles (a
+//              second producer lane in warp 0 would share that warp's issue
+//              slots with the F-ring producer's waits)
+// Ring of 6 stages (shared-memory tiles + Tensor Memory a-slots of 32 columns)
 // and 2 TMEM partial buffers of 128 columns, handed over with mbarriers; every
 // wait is bounded (error flag on timeout).  The F tile never goes back to
-// shared memory split, so per stage the shared-memory traffic is the TMA write,
-// one read by the converters and the MMA's B reads.
+// shared memory split, so per stage the shared-memory traffic is the TMA
+// writes (16 KB of F, 8 KB of S_i), one read of F by the converters and the
+// MMA's B reads.
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
@@ -59,34 +64,36 @@ constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
 // Pipeline shape (tuning parameters; Tensor Memory holds kBufs partial buffers
-// of 128 columns and kStages a-slots of 64 columns, 512 columns in all)
+// of 64 columns and kStages a-slots of 32 columns)
 #ifndef KEVD_UPD_STAGES
-#define KEVD_UPD_STAGES 4
+#define KEVD_UPD_STAGES 6
 #endif
 #ifndef KEVD_UPD_BUFS
 #define KEVD_UPD_BUFS 2
 #endif
-#ifndef KEVD_UPD_PER_PARTIAL
-#define KEVD_UPD_PER_PARTIAL 1
-#endif
 constexpr int kStages = KEVD_UPD_STAGES;
 constexpr int kPrefetch = 8;        // F tiles prefetched into L2 ahead of the ring
-constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers of kPartCols columns
-constexpr int kPerPartial = KEVD_UPD_PER_PARTIAL; // 32-column stages accumulated per TMEM partial
-// A partial buffer holds two 64-column accumulators side by side: columns
-// [0,64) take hi_a hi_b + lo_a hi_b, columns [64,128) take hi_a lo_b (one
-// N = 128 MMA against the b-hi and b-lo tiles, which lie back to back in
-// shared memory as one 128-row operand, plus one N = 64 MMA: 8 MMAs per stage
-// instead of 12)
+constexpr int kBufs = KEVD_UPD_BUFS;              // TMEM partial buffers (one per stage in flight)
+// A partial buffer holds two 64-column FP32 accumulators side by side:
+// [0, 64) hi_a hi_b, [64, 128) the cross terms hi_a lo_b + lo_a hi_b (one
+// N = 128 MMA of hi_a against the b-hi and b-lo tiles, which lie back to back
+// in shared memory as one 128-row operand, and one N = 64 MMA of lo_a hi_b)
 constexpr int kPartCols = 2 * kCols;
-static_assert((kBufs & (kBufs - 1)) == 0 && (kPerPartial & (kPerPartial - 1)) == 0,
-              "partial-buffer count and stages per partial are powers of two");
-constexpr uint32_t kTmemA = kBufs * kPartCols;   // a-slots after the partials, 64 per stage (hi 32, lo 32)
-static_assert(kBufs * kPartCols + kStages * 64 <= 512, "Tensor Memory holds 512 columns");
+static_assert((kBufs & (kBufs - 1)) == 0, "partial-buffer count is a power of two");
+constexpr uint32_t kASlotCols = 32;               // a-slot: 16 columns of packed hi pairs, then 16 of lo
+constexpr uint32_t kTmemA = kBufs * kPartCols;    // a-slots after the partials
+static_assert(kTmemA + kStages * kASlotCols <= 512, "Tensor Memory holds 512 columns");
 constexpr uint32_t kTmemCols = 512;       // allocated and freed as one block
-constexpr int kAOp = kRows * kKs * 4;     // 16 KB
-constexpr int kBOp = kCols * kKs * 4;     // 8 KB
-constexpr int kStageBytes = kAOp + 2 * kBOp;   // raw F tile, b_hi, b_lo
+constexpr int kAOp = kRows * kKs * 4;     // raw F tile, 16 KB
+constexpr int kBTile = kCols * kKs * 2;   // one f16 operand tile of the S_i rows (64 rows x 64 B), 4 KB
+constexpr int kStageBytes = kAOp + 2 * kBTile;   // raw F tile, b_hi, b_lo
+static_assert(kStageBytes % 1024 == 0, "stage tiles keep the 1024-byte alignment of SWIZZLE_128B");
+// The split works on F 2^14 (every |F(i, a)| <= 1 for a unit-diagonal kernel,
+// so the scaled values stay far below the f16 maximum, 65504, and above its
+// normal range down to |F| = 2^-28); each product carries 2^28, removed
+// exactly in the epilogue.
+constexpr float kSplitScale = 16384.f;
+constexpr float kSplitUnscale = 1.0f / (16384.f * 16384.f);
 constexpr int kThreads = 576;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr int kMaxD = kMaxFeatures;
@@ -101,7 +108,6 @@ struct Bars {
     uint64_t acce[kBufs];
     uint64_t kfull;     // K(R, S_i) tile landed
     uint64_t tready;    // epilogue left T = K - P in the K tile
-    uint64_t kempty;    // tail warps done with the K tile
     uint64_t done;
     uint32_t tmem_base;
 };
@@ -130,6 +136,13 @@ __device__ __forceinline__ bool pass_view(const RoundView* st, int group, int64_
     r = st->r_old + (int64_t)kCols * group;
     nacc = min(kCols, st->nacc - kCols * group);
     return nacc > 0;
+}
+
+// K(R, S_i) for row block rb: two 128 x 32 SWIZZLE_128B boxes into the K tile
+__device__ __forceinline__ void load_ktile(const CUtensorMap* tmk, uint8_t* ktile, uint64_t* kfull, int64_t rb) {
+    tc::mbar_arrive_expect_tx(kfull, 2 * kAOp);
+    tc::tma_load_2d(ktile, tmk, 0, (int)(rb * kRows), kfull);
+    tc::tma_load_2d(ktile + kAOp, tmk, 32, (int)(rb * kRows), kfull);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -168,9 +181,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             tc::mbar_init(&bar->accf[t], 1);
             tc::mbar_init(&bar->acce[t], 128);
         }
+
         tc::mbar_init(&bar->kfull, 1);
         tc::mbar_init(&bar->tready, 128);
-        tc::mbar_init(&bar->kempty, 128);
         tc::mbar_init(&bar->done, 1);
         tc::mbar_fence_init();
     }
@@ -202,24 +215,12 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                         const int64_t rbp = rb + (int64_t)(sp / n_st) * gridDim.x;
                         if (rbp < nblk) tc::tma_prefetch_2d(&tmap, (sp % n_st) * kKs, (int)(rbp * kRows));
                     }
-                    tc::mbar_arrive_expect_tx(&bar->tma_full[slot], kAOp + 2 * kBOp);
+                    tc::mbar_arrive_expect_tx(&bar->tma_full[slot], kAOp + 2 * kBTile);
                     tc::tma_load_2d(stg, &tmap, s * kKs, (int)(rb * kRows), &bar->tma_full[slot]);
-                    tc::bulk_load(stg + kAOp, bprep + (size_t)s * 2 * kBOp, 2 * kBOp, &bar->tma_full[slot]);
+                    tc::bulk_load(stg + kAOp, bprep + (size_t)s * 2 * kBTile, 2 * kBTile, &bar->tma_full[slot]);
                 }
             }
             if (!ok) atomicExch(err, 11);
-        } else if (lane == 1) {
-            // K(R, S_i) tiles, one per row block, single-buffered
-            int64_t it = 0;
-            for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x, ++it) {
-                if (!tc::mbar_wait(&bar->kempty, ((uint32_t)it & 1u) ^ 1u, kTimeoutNs)) {
-                    atomicExch(err, 16);
-                    break;
-                }
-                tc::mbar_arrive_expect_tx(&bar->kfull, 2 * kAOp);
-                tc::tma_load_2d(ktile, &tmk, 0, (int)(rb * kRows), &bar->kfull);
-                tc::tma_load_2d(ktile + kAOp, &tmk, 32, (int)(rb * kRows), &bar->kfull);
-            }
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -228,16 +229,16 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // time, so the ring slot of each stage, and with it every operand
         // descriptor, is a compile-time index into registers filled once.
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_tf32(kRows, kCols);
-            constexpr uint32_t idesc2 = tc::idesc_tf32(kRows, kPartCols);
-            const uint32_t bh_base = tc::desc_lo_sw128(tc::smem_u32(base + kAOp));   // slot 0's b-hi tile
-            uint64_t dbh[kStages][kKs / 8];   // b-hi and b-lo tiles as one 128-row operand
+            constexpr uint32_t idesc = tc::idesc_f16(kRows, kCols);
+            constexpr uint32_t idesc2 = tc::idesc_f16(kRows, kPartCols);
+            constexpr int kSteps = kKs / 16;   // K = 16 per kind::f16 MMA
+            uint64_t dbh[kStages][kSteps];   // b-hi and b-lo tiles as one 128-row operand
 #pragma unroll
             for (int sl = 0; sl < kStages; ++sl)
 #pragma unroll
-                for (int j = 0; j < kKs / 8; ++j) {   // +32 bytes of K per MMA: +2 in the address field
-                    const uint32_t bh = bh_base + (uint32_t)sl * (uint32_t)(kStageBytes >> 4);
-                    dbh[sl][j] = tc::desc_sw128_from_lo(bh + 2u * j);
+                for (int j = 0; j < kSteps; ++j) {   // +32 bytes of K per MMA
+                    const uint32_t bh = tc::smem_u32(base + (size_t)sl * kStageBytes + kAOp) + 32u * j;
+                    dbh[sl][j] = tc::desc_sw64(bh);
                     tc::reg_pin(dbh[sl][j]);
                 }
             const int64_t my_blocks = (nblk - blockIdx.x + gridDim.x - 1) / gridDim.x;
@@ -253,31 +254,26 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 #pragma unroll
                 for (int sl = 0; sl < kStages; ++sl) {
                     if (g0 + sl >= total) break;
+                    // both sums into a fresh partial buffer every stage
                     const uint32_t tb = pg & (uint32_t)(kBufs - 1);
                     const uint32_t tpar = ((pg / (uint32_t)kBufs) & 1u) ^ 1u;
-                    const uint32_t sp = s & (uint32_t)(kPerPartial - 1);
-                    const bool first = sp == 0u;
-                    const bool last = sp == (uint32_t)(kPerPartial - 1) || s == last_s;
-                    const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * 64u, alo = ahi + 32u;
+                    const uint32_t ahi = tbase + kTmemA + (uint32_t)sl * kASlotCols, alo = ahi + 16u;
                     const uint32_t dt = tbase + tb * (uint32_t)kPartCols;
-                    const uint32_t acc0 = first ? 0u : 1u;
-                    if ((first && !tc::mbar_wait(&bar->acce[tb], tpar, kTimeoutNs)) ||
+                    if (!tc::mbar_wait(&bar->acce[tb], tpar, kTimeoutNs) ||
                         !tc::mbar_wait(&bar->cvt_full[sl], use & 1u, kTimeoutNs)) {
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
 #pragma unroll
-                    for (int j = 0; j < kKs / 8; ++j) {
-                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the first half
-                        tc::mma_tf32_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc2, j > 0 ? 1u : acc0);
-                        tc::mma_tf32_tmem_a(dt, alo + 8u * j, dbh[sl][j], idesc, 1u);
+                    for (int j = 0; j < kSteps; ++j) {
+                        // [hi_a hi_b | hi_a lo_b] (N = 128), then lo_a hi_b into the second half
+                        tc::mma_f16_tmem_a(dt, ahi + 8u * j, dbh[sl][j], idesc2, j > 0 ? 1u : 0u);
+                        tc::mma_f16_tmem_a(dt + (uint32_t)kCols, alo + 8u * j, dbh[sl][j], idesc, 1u);
                     }
                     tc::mma_commit(&bar->empty[sl]);
-                    if (last) {
-                        tc::mma_commit(&bar->accf[tb]);
-                        ++pg;
-                    }
+                    tc::mma_commit(&bar->accf[tb]);
+                    ++pg;
                     s = (s == last_s) ? 0u : s + 1u;
                 }
             }
@@ -305,22 +301,27 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 }
                 const uint8_t* stg = base + (size_t)slot * kStageBytes;
                 const int64_t cbase = (int64_t)s * kKs;
-                float h[32], l[32];
+                float x[32];
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                     const float4 a =
                         *reinterpret_cast<const float4*>(stg + tc::sw128_off((uint32_t)m, (uint32_t)(4 * c)));
-                    const float v[4] = {a.x, a.y, a.z, a.w};
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float x = (cbase + 4 * c + u < r) ? v[u] : 0.f;
-                        h[4 * c + u] = tc::tf32_rn(x);
-                        l[4 * c + u] = tc::tf32_rn(x - h[4 * c + u]);
-                    }
+                    x[4 * c + 0] = a.x;
+                    x[4 * c + 1] = a.y;
+                    x[4 * c + 2] = a.z;
+                    x[4 * c + 3] = a.w;
                 }
-                const uint32_t ta = tlane + kTmemA + (uint32_t)slot * 64u;
-                tc::tmem_st32(ta, h);
-                tc::tmem_st32(ta + 32u, l);
+                if (cbase + kKs > r) {   // the last stage of a row block: columns >= r are zero
+#pragma unroll
+                    for (int u = 0; u < 32; ++u)
+                        if (cbase + u >= r) x[u] = 0.f;
+                }
+                // words 0..15: hi pairs (K = 2p, 2p+1), words 16..31: lo pairs
+                uint32_t w[32];
+#pragma unroll
+                for (int p2 = 0; p2 < 16; ++p2)
+                    tc::split_f16x2(x[2 * p2] * kSplitScale, x[2 * p2 + 1] * kSplitScale, w[p2], w[16 + p2]);
+                tc::tmem_st32u(tlane + kTmemA + (uint32_t)slot * kASlotCols, w);
                 tc::tmem_wait_st();
                 tc::tc_fence_before();
                 __syncwarp();
@@ -336,7 +337,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // blocks and arriving, so no other role waits for it in vain.
         const int q = warp - 4;
         const int rloc = 32 * q + lane;
-        const int n_part = (n_st + kPerPartial - 1) / kPerPartial;
+        const int n_part = n_st;   // one partial per stage
         int64_t g = 0;
         int64_t kit = 0;
         bool ok = true;
@@ -356,11 +357,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 tc::tc_fence_after();
                 float v[16];
                 const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(tb * kPartCols);
-                // 16 columns at a time (register budget of 576 threads): the main
-                // sums, then the hi_a lo_b sums of the same columns
+                // 16 columns at a time (register budget of 576 threads): the
+                // hi_a hi_b sums, then the cross-term sums of the same columns
 #pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    tc::tmem_ld16(ta + (uint32_t)((h & 3) * 16 + (h >> 2) * kCols), v);
+                for (int h = 0; h < kPartCols / 16; ++h) {
+                    tc::tmem_ld16(ta + (uint32_t)(16 * h), v);
                     tc::tmem_wait_ld();
 #pragma unroll
                     for (int j = 0; j < 16; ++j) acc[16 * (h & 3) + j] += v[j];
@@ -374,16 +375,16 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             }
             if (ok) {
                 // T = K(i, S_i) - P over the K tile's row (K(:, S_i) by
-                // update_kcols_kernel, TMA tile in smem)
+                // update_kcols_kernel, TMA tile in smem); P = acc 2^-28 exactly
 #pragma unroll
                 for (int c4 = 0; c4 < kCols / 4; ++c4) {
                     float4* kp = reinterpret_cast<float4*>(
                         ktile + (c4 >> 3) * kAOp + tc::sw128_off((uint32_t)rloc, (uint32_t)(4 * (c4 & 7))));
                     float4 kv = *kp;
-                    kv.x -= acc[4 * c4 + 0];
-                    kv.y -= acc[4 * c4 + 1];
-                    kv.z -= acc[4 * c4 + 2];
-                    kv.w -= acc[4 * c4 + 3];
+                    kv.x = fmaf(-acc[4 * c4 + 0], kSplitUnscale, kv.x);
+                    kv.y = fmaf(-acc[4 * c4 + 1], kSplitUnscale, kv.y);
+                    kv.z = fmaf(-acc[4 * c4 + 2], kSplitUnscale, kv.z);
+                    kv.w = fmaf(-acc[4 * c4 + 3], kSplitUnscale, kv.w);
                     *kp = kv;
                 }
                 // the tile is written by TMA again once the tail warps release it
@@ -396,13 +397,15 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
         // ---------------- tail: warps 14..17, row 32q + lane of each row block.
         // G = T L_i^{-T}, the d update, the F write and the block sum of d,
         // overlapped with the MMA and the epilogue working on the next row
-        // blocks.  The K tile (holding T) is released as soon as this thread's
-        // row is in registers.
+        // blocks.  The tail also loads the K tiles (single-buffered): the next
+        // row block's tile is issued as soon as the four warps hold their T
+        // rows in registers.
         const int q = warp - 14;
         const int rloc = 32 * q + lane;
         int64_t it = 0;
         bool ok = true;
         __shared__ double wsum[2][4];
+        if (rloc == 0) load_ktile(&tmk, ktile, &bar->kfull, blockIdx.x);
         for (int64_t rb = blockIdx.x; rb < nblk; rb += gridDim.x) {
             const int64_t row0 = rb * kRows;
             const int64_t i = row0 + rloc;
@@ -424,7 +427,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                     t[4 * c4 + 3] = tv.w;
                 }
             }
-            tc::mbar_arrive(&bar->kempty);   // this thread is done with the K tile: the next one may land
+            // every tail thread holds its T row: the next K tile may land (the
+            // epilogue's writes of T were fenced for the async proxy before
+            // tready; these reads are ordered before the TMA by the barrier)
+            asm volatile("bar.sync 2, 128;" ::: "memory");
+            if (rloc == 0 && rb + gridDim.x < nblk) {
+                tc::fence_async_smem();
+                load_ktile(&tmk, ktile, &bar->kfull, rb + gridDim.x);
+            }
             double nd = d_old;
             if (live) {
                 // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
@@ -622,11 +632,12 @@ __global__ void update_prep_kernel(const float* __restrict__ F, int64_t ldF, con
         const int qrow = rem / kKs, kk = rem - qrow * kKs;
         const int64_t c = (int64_t)s * kKs + kk;
         const float v = (qrow < nacc && c < r) ? F[sacc[qrow] * ldF + c] : 0.f;
-        const float h = tc::tf32_rn(v), l = tc::tf32_rn(v - h);
-        uint8_t* t = bprep + (size_t)s * 2 * kBOp;
-        const uint32_t off = tc::sw128_off((uint32_t)qrow, (uint32_t)kk);
-        *reinterpret_cast<float*>(t + off) = h;
-        *reinterpret_cast<float*>(t + kBOp + off) = l;
+        uint32_t h, l;   // the converters' split of the same value (low halves)
+        tc::split_f16x2(v * kSplitScale, 0.f, h, l);
+        uint8_t* t = bprep + (size_t)s * 2 * kBTile;
+        const uint32_t off = tc::sw64_off16((uint32_t)qrow, (uint32_t)kk);
+        *reinterpret_cast<uint16_t*>(t + off) = (uint16_t)(h & 0xFFFFu);
+        *reinterpret_cast<uint16_t*>(t + kBTile + off) = (uint16_t)(l & 0xFFFFu);
     }
     (void)n_stages_max;
 }
@@ -685,7 +696,7 @@ int launch_update_tc(kevd_ctx* ctx, float* F, int64_t ldF, int64_t N, int64_t k_
     const int n_stages_max = (int)((k_max + kKs - 1) / kKs);
     const int n_groups = (b + kCols - 1) / kCols;
     int rc = KEVD_OK;
-    uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBOp, &rc);
+    uint8_t* bprep = arena_get<uint8_t>(ctx, "utc.bprep", (size_t)std::max(1, n_stages_max) * 2 * kBTile, &rc);
     if (rc != KEVD_OK) return set_error(ctx, rc, "update_tc: out of device memory");
     const RoundView* rv = static_cast<const RoundView*>(round_state);
     // K(R, S_i): update_kcols_kernel writes an N x 64 buffer that the update

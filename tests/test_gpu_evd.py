@@ -73,7 +73,7 @@ def test_mixed_evd_close_to_fp64(ctx, fac):
     np.testing.assert_allclose(g.lam[-16:], e["lam"][-16:], rtol=0, atol=1e-8)
     ang = evd.eigvec_angles(g.U.cpu().numpy()[:, -4:], e["U"][:, -4:])
     assert np.all(ang < 1e-4)
-    # the rest of the spectrum comes from the 3xTF32 Grams and the FP32 eigensolve of W
+    # the rest of the spectrum comes from the tensor-core Grams and the FP32 eigensolve of W
     np.testing.assert_allclose(g.lam[:-16], e["lam"][:-16], rtol=0, atol=1e-4)
 
 

@@ -1,6 +1,6 @@
 """Weighted Gram G = F^T diag(s)^2 F: the FP32 factor on the tcgen05 tensor cores
-(3xTF32, FP64 across row chunks) and the FP64 factor on the FP64 path, against
-NumPy FP64 on the same inputs."""
+(two-term f16 split scaled to max |F| and max s^2, FP64 across row chunks) and
+the FP64 factor on the FP64 path, against NumPy FP64 on the same inputs."""
 import numpy as np
 import pytest
 import torch
@@ -9,9 +9,8 @@ pytestmark = pytest.mark.gpu
 
 
 # Relative error bound of a Gram entry against sqrt(G_ii G_jj): the tensor-core
-# FP32 accumulator rounds each MMA update with a one-sided bias of about 0.4 ulp,
-# and a TMEM partial takes 2048 rows (256 k-steps x 3 products) before its FP64
-# flush, about 4.6e-5 expected on all-positive columns.
+# FP32 accumulator rounds each MMA update with a one-sided bias, and a TMEM
+# partial takes 2048 rows (128 k-steps x 3 products) before its FP64 flush.
 GRAM_RTOL = 6e-5
 
 
@@ -33,8 +32,9 @@ def test_gram_tc_fp32_factor(ctx, N, k, ld):
     R = _ref(Fb[:, :k], s)
     scale = np.sqrt(np.outer(np.diag(R), np.diag(R)))
     err = np.abs(G - R) / scale
-    # 3xTF32 products (exact hi/lo pieces); the tensor-core FP32 accumulator over
-    # 2048-row partials limits the relative error (FP64 across partials)
+    # two-term f16 products (22-bit hi/lo pieces); the tensor-core FP32
+    # accumulator over 2048-row partials limits the relative error (FP64 across
+    # partials)
     assert err.max() < GRAM_RTOL, err.max()
     np.testing.assert_allclose(G, G.T, rtol=0, atol=0)
 
