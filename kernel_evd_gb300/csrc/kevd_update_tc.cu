@@ -415,21 +415,24 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
                 ok = false;
             }
             const bool live = ok && i < N;
-            float t[kCols];
+            // T row -> this thread's staging row (pitch kGPitch: the 32 rows of
+            // a warp fall in distinct banks for every column)
+            float* grow = gbuf + rloc * kGPitch;
             if (live) {
 #pragma unroll
                 for (int c4 = 0; c4 < kCols / 4; ++c4) {
                     const float4 tv = *reinterpret_cast<const float4*>(
                         ktile + (c4 >> 3) * kAOp + tc::sw128_off((uint32_t)rloc, (uint32_t)(4 * (c4 & 7))));
-                    t[4 * c4 + 0] = tv.x;
-                    t[4 * c4 + 1] = tv.y;
-                    t[4 * c4 + 2] = tv.z;
-                    t[4 * c4 + 3] = tv.w;
+                    grow[4 * c4 + 0] = tv.x;
+                    grow[4 * c4 + 1] = tv.y;
+                    grow[4 * c4 + 2] = tv.z;
+                    grow[4 * c4 + 3] = tv.w;
                 }
             }
-            // every tail thread holds its T row: the next K tile may land (the
-            // epilogue's writes of T were fenced for the async proxy before
-            // tready; these reads are ordered before the TMA by the barrier)
+            // every tail thread has copied its T row: the next K tile may land
+            // (the epilogue's writes of T were fenced for the async proxy
+            // before tready; these reads are ordered before the TMA by the
+            // barrier)
             asm volatile("bar.sync 2, 128;" ::: "memory");
             if (rloc == 0 && rb + gridDim.x < nblk) {
                 tc::fence_async_smem();
@@ -437,49 +440,43 @@ update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
             }
             double nd = d_old;
             if (live) {
-                // G = T L_i^{-T}, eight outputs at a time (eight independent FMA
-                // chains; the two 16-byte broadcast loads of L_i^{-1} for term e+2
-                // are issued before the FMAs of term e); each G[a] sums e = 0..a in
-                // increasing order (the zero terms above the diagonal leave it
-                // unchanged); G -> own row of the staging buffer
+                // G = T L_i^{-T} in place in the staging row, blocks of eight
+                // outputs from the last to the first: block a0 reads T[0 ..
+                // a0+7] and overwrites T[a0 .. a0+7], which no earlier block
+                // needs.  Eight independent FMA chains per block, each G[a]
+                // summing e = 0..a in increasing order (the zero terms above
+                // the diagonal leave it unchanged); runtime loops keep the code
+                // small (fully unrolled, the 2,080 FMAs of a row took 11k cycles
+                // per row block against 2k of FP32 pipe time).
+                const int nb = (nacc + 7) >> 3;
                 float sq = 0.f;
+                for (int blk = nb - 1; blk >= 0; --blk) {
+                    const int a0 = 8 * blk;
+                    float g8[8];
 #pragma unroll
-                for (int a0 = 0; a0 < kCols; a0 += 8) {
-                    if (a0 < nacc) {
-                        float g8[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) g8[u] = 0.f;
-                        float4 n0 = *reinterpret_cast<const float4*>(mv + a0);
-                        float4 n1 = *reinterpret_cast<const float4*>(mv + a0 + 4);
-                        float4 p0 = *reinterpret_cast<const float4*>(mv + kCols + a0);
-                        float4 p1 = *reinterpret_cast<const float4*>(mv + kCols + a0 + 4);
-#pragma unroll
-                        for (int e = 0; e < a0 + 8; ++e) {
-                            const float4 m0 = n0, m1 = n1;
-                            n0 = p0;
-                            n1 = p1;
-                            if (e + 2 < a0 + 8) {
-                                p0 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0);
-                                p1 = *reinterpret_cast<const float4*>(mv + (e + 2) * kCols + a0 + 4);
-                            }
-                            g8[0] = fmaf(t[e], m0.x, g8[0]);
-                            g8[1] = fmaf(t[e], m0.y, g8[1]);
-                            g8[2] = fmaf(t[e], m0.z, g8[2]);
-                            g8[3] = fmaf(t[e], m0.w, g8[3]);
-                            g8[4] = fmaf(t[e], m1.x, g8[4]);
-                            g8[5] = fmaf(t[e], m1.y, g8[5]);
-                            g8[6] = fmaf(t[e], m1.z, g8[6]);
-                            g8[7] = fmaf(t[e], m1.w, g8[7]);
-                        }
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const int a = a0 + u;
-                            if (a < nacc) {
-                                gbuf[rloc * kGPitch + a] = g8[u];
-                                sq = fmaf(g8[u], g8[u], sq);
-                            }
-                        }
+                    for (int u = 0; u < 8; ++u) g8[u] = 0.f;
+                    const float* mcol = mv + a0;
+#pragma unroll 4
+                    for (int e = 0; e < a0 + 8; ++e) {
+                        const float te = grow[e];
+                        const float4 m0 = *reinterpret_cast<const float4*>(mcol + e * kCols);
+                        const float4 m1 = *reinterpret_cast<const float4*>(mcol + e * kCols + 4);
+                        g8[0] = fmaf(te, m0.x, g8[0]);
+                        g8[1] = fmaf(te, m0.y, g8[1]);
+                        g8[2] = fmaf(te, m0.z, g8[2]);
+                        g8[3] = fmaf(te, m0.w, g8[3]);
+                        g8[4] = fmaf(te, m1.x, g8[4]);
+                        g8[5] = fmaf(te, m1.y, g8[5]);
+                        g8[6] = fmaf(te, m1.z, g8[6]);
+                        g8[7] = fmaf(te, m1.w, g8[7]);
                     }
+                    float sb = 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        grow[a0 + u] = g8[u];
+                        if (a0 + u < nacc) sb = fmaf(g8[u], g8[u], sb);
+                    }
+                    sq += sb;
                 }
                 nd = fmax(d_old - (double)sq, 0.0);
                 dvec[i] = nd;
