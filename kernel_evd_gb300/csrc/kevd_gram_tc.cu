@@ -43,6 +43,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 
 namespace kevd {
 
@@ -68,18 +70,28 @@ constexpr int kCvtWarps = 8;        // arrivals per stage on the "converted" bar
 constexpr int kThreads = 14 * 32;
 constexpr uint32_t kTmemCols = 512;       // accumulators [0, 256), a-slots [256, 512)
 constexpr uint32_t kTmemA = 256;
-constexpr int kTSlots = 4;                // one a-slot per ring stage
-constexpr uint32_t kTSlotCols = 64;       // per Gram: 16 columns of hi pairs, 16 of lo
-static_assert(kTmemA + kTSlots * kTSlotCols <= kTmemCols, "Tensor Memory holds 512 columns");
-static_assert(kFlushStages % kStages == 0 && kStages % kTSlots == 0, "slot indices are compile-time per stage");
+// a-slots: f16 split, one per ring stage, per Gram 16 columns of packed hi
+// pairs and 16 of lo; tf32 split, one per two stages, per Gram 32 hi and 32 lo
+template <bool F16> struct Slots {
+    static constexpr int n = F16 ? 4 : 2;
+    static constexpr uint32_t cols = F16 ? 64 : 128;
+    static constexpr uint32_t gram_cols = F16 ? 32 : 64;   // one Gram's hi + lo
+    static constexpr uint32_t lo_off = F16 ? 16 : 32;
+    static_assert(kTmemA + n * cols <= kTmemCols, "Tensor Memory holds 512 columns");
+    static_assert(kFlushStages % kStages == 0 && kStages % n == 0, "slot indices are compile-time per stage");
+};
+// Weight ranges (max s^2 / min s^2) above this take the tf32 split: the f16
+// split keeps a factor column's values within 2^-28 .. 2^14 of its own scale at
+// full precision, and the row weights multiply into that range.
+constexpr float kF16WeightRange = 65536.f;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
-    alignas(16) float w2[kStages][2][32];   // scaled squared row weights of each stage, A then B
+    alignas(16) float w2[kStages][2][32];   // squared row weights of each stage, A then B
     uint64_t tma[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
-    uint64_t tfree[kTSlots];
+    uint64_t tfree[4];
     uint64_t accf;
     uint64_t acce[2];
     uint64_t done;
@@ -119,6 +131,13 @@ __device__ __forceinline__ void load_row(const uint8_t* tile, int m, float (&x)[
     }
 }
 
+__device__ __forceinline__ void store_row(uint8_t* tile, int m, const float (&x)[32]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        *reinterpret_cast<float4*>(tile + tc::sw128_off((uint32_t)m, 4u * c)) =
+            make_float4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
+}
+
 // Row m of the b-hi and b-lo tiles from the 32 raw values of b row m.
 __device__ __forceinline__ void store_b_split(uint8_t* st, int m, const float (&x)[32], float bscale) {
     uint32_t h[16], l[16];
@@ -134,9 +153,16 @@ __device__ __forceinline__ void store_b_split(uint8_t* st, int m, const float (&
 
 // NG weighted Grams of the same factor in one pass: G_g = F^T diag(s_g)^2 F.
 // Every F tile is loaded and its b side split once for all of them: the
-// stage's a tile is weighted NG times into Tensor Memory and 6 MMAs per stage
-// and Gram accumulate the output tiles.
-template <int NG>
+// stage's a tile is weighted NG times into Tensor Memory and each Gram's
+// output tile accumulates the stage's products.
+//   F16 (weights within kF16WeightRange): two-term f16 split of per-column
+//     scaled values, 6 kind::f16 MMAs (K = 16) per stage and Gram; b-hi and
+//     b-lo f16 tiles (SWIZZLE_64B) in shared memory.
+//   tf32 (any weights): the tensor core reads an FP32 operand as tf32 by
+//     dropping its 13 low mantissa bits, so an element v enters as hi = v as it
+//     is and lo = v - trunc_tf32(v) (exact in FP32); 12 kind::tf32 MMAs (K = 8)
+//     per stage and Gram; the raw b tile is b-hi, b-lo an FP32 tile.
+template <int NG, bool F16>
 __global__ void __launch_bounds__(kThreads, 1)
 gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict__ w2a, const float* __restrict__ w2b,
                GramExp ex, int64_t N, int64_t k, int n_tiles, int64_t rows_per,
@@ -174,7 +200,7 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
             tc::mbar_init(&bar->full[s], kCvtWarps);
             tc::mbar_init(&bar->empty[s], 1);
         }
-        for (int t = 0; t < kTSlots; ++t) tc::mbar_init(&bar->tfree[t], 1);
+        for (int t = 0; t < Slots<F16>::n; ++t) tc::mbar_init(&bar->tfree[t], 1);
         tc::mbar_init(&bar->accf, 1);
         tc::mbar_init(&bar->acce[0], kEpiWarps * 32);
         tc::mbar_init(&bar->acce[1], kEpiWarps * 32);
@@ -221,9 +247,10 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
         // also the b column of a diagonal tile; b converters: column b0 + m)
         const int64_t cm = (grp_a ? a0 : b0) + m;
         const bool cin = cm < k;
-        const float bscale = cin ? ldexpf(1.f, ex.eb[cm]) : 1.f;
-        const float as0 = (grp_a && cin) ? ldexpf(1.f, ex.ea0[cm]) : 1.f;
-        const float as1 = (grp_a && cin && NG == 2) ? ldexpf(1.f, ex.ea1[cm]) : 1.f;
+        const float bscale = (F16 && cin) ? ldexpf(1.f, ex.eb[cm]) : 1.f;
+        const float as0 = (F16 && grp_a && cin) ? ldexpf(1.f, ex.ea0[cm]) : 1.f;
+        const float as1 = (F16 && grp_a && cin && NG == 2) ? ldexpf(1.f, ex.ea1[cm]) : 1.f;
+        using SL = Slots<F16>;
         for (int64_t s = 0; s < n_stages; ++s) {
             const int slot = (int)(s % kStages);
             const uint32_t use = (uint32_t)(s / kStages);
@@ -234,48 +261,82 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
             }
             uint8_t* st = base + (size_t)slot * kStageBytes;
             if (grp_a) {
-                const int ts = (int)(s % kTSlots);
-                const uint32_t tuse = (uint32_t)(s / kTSlots);
+                const int ts = (int)(s % SL::n);
+                const uint32_t tuse = (uint32_t)(s / SL::n);
                 load_row(st, m, x);
                 if (!tc::mbar_wait(&bar->tfree[ts], (tuse & 1u) ^ 1u, kTimeoutNs)) {
                     atomicExch(err, 6);
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t ta_ = tlane + kTmemA + (uint32_t)ts * kTSlotCols;
+                const uint32_t ta_ = tlane + kTmemA + (uint32_t)ts * SL::cols;
 #pragma unroll
                 for (int gsel = 0; gsel < NG; ++gsel) {
-                    // y = (s^2 F) 2^ea: the power of two scales the rounded
-                    // product exactly.  Words 0..15: hi pairs (rows 2p, 2p+1),
-                    // words 16..31: lo pairs
-                    const float as = gsel ? as1 : as0;
-                    uint32_t w[32];
+                    if constexpr (F16) {
+                        // y = (s^2 F) 2^ea: the power of two scales the rounded
+                        // product exactly.  Words 0..15: hi pairs (rows 2p,
+                        // 2p+1), words 16..31: lo pairs
+                        const float as = gsel ? as1 : as0;
+                        uint32_t w[32];
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) {
-                        const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot][gsel])[c];
-                        tc::split_f16x2((x[4 * c + 0] * wv.x) * as, (x[4 * c + 1] * wv.y) * as, w[2 * c],
-                                        w[16 + 2 * c]);
-                        tc::split_f16x2((x[4 * c + 2] * wv.z) * as, (x[4 * c + 3] * wv.w) * as, w[2 * c + 1],
-                                        w[17 + 2 * c]);
+                        for (int c = 0; c < 8; ++c) {
+                            const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot][gsel])[c];
+                            tc::split_f16x2((x[4 * c + 0] * wv.x) * as, (x[4 * c + 1] * wv.y) * as, w[2 * c],
+                                            w[16 + 2 * c]);
+                            tc::split_f16x2((x[4 * c + 2] * wv.z) * as, (x[4 * c + 3] * wv.w) * as, w[2 * c + 1],
+                                            w[17 + 2 * c]);
+                        }
+                        tc::tmem_st32u(ta_ + SL::gram_cols * gsel, w);
+                    } else {
+                        float y[32], l[32];
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            const float4 wv = reinterpret_cast<const float4*>(bar->w2[slot][gsel])[c];
+                            y[4 * c + 0] = x[4 * c + 0] * wv.x;
+                            y[4 * c + 1] = x[4 * c + 1] * wv.y;
+                            y[4 * c + 2] = x[4 * c + 2] * wv.z;
+                            y[4 * c + 3] = x[4 * c + 3] * wv.w;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 32; ++u) l[u] = y[u] - tc::tf32_trunc(y[u]);
+                        tc::tmem_st32(ta_ + SL::gram_cols * gsel, y);
+                        tc::tmem_st32(ta_ + SL::gram_cols * gsel + 32u, l);
                     }
-                    tc::tmem_st32u(ta_ + 32u * gsel, w);
                 }
-                if (diag) store_b_split(st, m, x, bscale);
+                if (diag) {
+                    if constexpr (F16) {
+                        store_b_split(st, m, x, bscale);
+                    } else {
+                        float l[32];
+#pragma unroll
+                        for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
+                        store_row(st + kOffBh, m, l);
+                    }
+                }
                 tc::tmem_wait_st();
                 tc::tc_fence_before();
             } else if (!diag) {
                 load_row(st + kOffB, m, x);
-                store_b_split(st, m, x, bscale);
+                if constexpr (F16) {
+                    store_b_split(st, m, x, bscale);
+                } else {
+                    float l[32];
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
+                    store_row(st + kOffBh, m, l);
+                }
             }
             tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar->full[slot]);
         }
     } else if (warp == kMmaWarp) {
-        // ---------------- MMA issuer: per stage 6 MMAs into each accumulator
-        // from descriptors held in registers
+        // ---------------- MMA issuer: per stage 6 (f16) or 12 (tf32) MMAs into
+        // each accumulator from descriptors held in registers
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_f16(kTT, kTT);
+            using SL = Slots<F16>;
+            constexpr uint32_t idesc = F16 ? tc::idesc_f16(kTT, kTT) : tc::idesc_tf32(kTT, kTT);
+            constexpr int kSteps = F16 ? kTK / 16 : kTK / 8;   // 32 bytes of K per MMA either way
             bool ok = true;
             for (int64_t c = 0; c < n_chunks && ok; ++c) {
                 const int64_t s0 = c * kFlushStages;
@@ -285,13 +346,23 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
 #pragma unroll
                     for (int sl = 0; sl < kStages; ++sl) {
                         if (sb + sl >= s1) break;
-                        const int ts = sl % kTSlots;   // sb is a multiple of kStages, hence of kTSlots
-                        uint64_t dbh[kTK / 16], dbl[kTK / 16];
-                        const uint32_t bh = tc::smem_u32(base + (size_t)sl * kStageBytes + kOffBh);
+                        const int ts = sl % SL::n;   // sb is a multiple of kStages, hence of the slot count
+                        uint64_t dbh[kSteps], dbl[kSteps];
+                        uint8_t* stg = base + (size_t)sl * kStageBytes;
 #pragma unroll
-                        for (int j = 0; j < kTK / 16; ++j) {   // +32 bytes of K per MMA
-                            dbh[j] = tc::desc_sw64(bh + 32u * j);
-                            dbl[j] = tc::desc_sw64(bh + kHalfBytes + 32u * j);
+                        for (int j = 0; j < kSteps; ++j) {   // +32 bytes of K per MMA
+                            if constexpr (F16) {
+                                const uint32_t bh = tc::smem_u32(stg + kOffBh);
+                                dbh[j] = tc::desc_sw64(bh + 32u * j);
+                                dbl[j] = tc::desc_sw64(bh + kHalfBytes + 32u * j);
+                            } else {
+                                // b-hi: the raw b tile (the raw a tile on a diagonal
+                                // tile); b-lo: the FP32 tile at kOffBh
+                                const uint32_t bh = tc::desc_lo_sw128(tc::smem_u32(diag ? stg : stg + kOffB));
+                                const uint32_t bl = tc::desc_lo_sw128(tc::smem_u32(stg + kOffBh));
+                                dbh[j] = tc::desc_sw128_from_lo(bh + 2u * j);
+                                dbl[j] = tc::desc_sw128_from_lo(bl + 2u * j);
+                            }
                             tc::reg_pin(dbh[j]);
                             tc::reg_pin(dbl[j]);
                         }
@@ -312,16 +383,26 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
                                 tc::tc_fence_after();
                             }
                             const uint32_t d = tbase + (uint32_t)(gsel * kTT);
-                            const uint32_t ahi = tbase + kTmemA + (uint32_t)ts * kTSlotCols + 32u * gsel;
-                            const uint32_t alo = ahi + 16u;
+                            const uint32_t ahi = tbase + kTmemA + (uint32_t)ts * SL::cols + SL::gram_cols * gsel;
+                            const uint32_t alo = ahi + SL::lo_off;
                             const uint32_t acc0 = first ? 0u : 1u;
+                            if constexpr (F16) {
 #pragma unroll
-                            for (int j = 0; j < kTK / 16; ++j) {
-                                tc::mma_f16_tmem_a(d, ahi + 8u * j, dbl[j], idesc, j > 0 ? 1u : acc0);
-                                tc::mma_f16_tmem_a(d, alo + 8u * j, dbh[j], idesc, 1u);
+                                for (int j = 0; j < kSteps; ++j) {
+                                    tc::mma_f16_tmem_a(d, ahi + 8u * j, dbl[j], idesc, j > 0 ? 1u : acc0);
+                                    tc::mma_f16_tmem_a(d, alo + 8u * j, dbh[j], idesc, 1u);
+                                }
+#pragma unroll
+                                for (int j = 0; j < kSteps; ++j)
+                                    tc::mma_f16_tmem_a(d, ahi + 8u * j, dbh[j], idesc, 1u);
+                            } else {
+#pragma unroll
+                                for (int j = 0; j < kSteps; ++j) {
+                                    tc::mma_tf32_tmem_a(d, ahi + 8u * j, dbl[j], idesc, j > 0 ? 1u : acc0);
+                                    tc::mma_tf32_tmem_a(d, alo + 8u * j, dbh[j], idesc, 1u);
+                                    tc::mma_tf32_tmem_a(d, ahi + 8u * j, dbh[j], idesc, 1u);
+                                }
                             }
-#pragma unroll
-                            for (int j = 0; j < kTK / 16; ++j) tc::mma_f16_tmem_a(d, ahi + 8u * j, dbh[j], idesc, 1u);
                         }
                         if (!ok) break;
                         tc::mma_commit(&bar->empty[sl]);
@@ -391,22 +472,36 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
     if (warp == kMmaWarp) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
-// max(s_i^2) over i < N of each weight vector into mx[g] (float bits, atomicMax).
+// max and min of s_i^2 over i < N of each weight vector: mx[g] (atomicMax,
+// starts at 0) and mx[2 + g] (atomicMin, starts at all ones), float bits of
+// non-negative values, so unsigned order is float order.
 __global__ void gram_wmax_kernel(const double* __restrict__ s, const double* __restrict__ s2, int64_t N,
                                  unsigned* __restrict__ mx) {
-    float m0 = 0.f, m1 = 0.f;
+    float m0 = 0.f, m1 = 0.f, n0 = INFINITY, n1 = INFINITY;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        m0 = fmaxf(m0, (float)(s[i] * s[i]));
-        if (s2) m1 = fmaxf(m1, (float)(s2[i] * s2[i]));
+        const float a = (float)(s[i] * s[i]);
+        m0 = fmaxf(m0, a);
+        n0 = fminf(n0, a);
+        if (s2) {
+            const float b = (float)(s2[i] * s2[i]);
+            m1 = fmaxf(m1, b);
+            n1 = fminf(n1, b);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
         m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+        n0 = fminf(n0, __shfl_xor_sync(0xffffffffu, n0, o));
+        n1 = fminf(n1, __shfl_xor_sync(0xffffffffu, n1, o));
     }
     if ((threadIdx.x & 31) == 0) {
         atomicMax(mx, __float_as_uint(m0));
-        if (s2) atomicMax(mx + 1, __float_as_uint(m1));
+        atomicMin(mx + 2, __float_as_uint(n0));
+        if (s2) {
+            atomicMax(mx + 1, __float_as_uint(m1));
+            atomicMin(mx + 3, __float_as_uint(n1));
+        }
     }
 }
 
@@ -596,7 +691,7 @@ static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, 
     int rc = KEVD_OK;
     double* partial = arena_get<double>(ctx, "tc.gpart", (size_t)n_split * n_tiles * nG * kTT * kTT, &rc);
     int* err = arena_get<int>(ctx, "tc.err", 1, &rc);
-    unsigned* wmax = arena_get<unsigned>(ctx, "tc.wmax", 2, &rc);
+    unsigned* wmax = arena_get<unsigned>(ctx, "tc.wmax", 4, &rc);   // max, max, min, min
     int* exps = arena_get<int>(ctx, "tc.exps", (size_t)3 * k, &rc);   // eb, ea0, ea1
     // squared weights, one 128-byte bulk copy per stage (row offsets are
     // multiples of 32, so every copy is 128-byte aligned)
@@ -610,26 +705,46 @@ static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, 
     if (rc != KEVD_OK) return set_error(ctx, rc, "gram_tc: out of device memory");
     KEVD_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
     KEVD_CUDA(ctx, cudaMemsetAsync(wmax, 0, 2 * sizeof(unsigned), st));
+    KEVD_CUDA(ctx, cudaMemsetAsync(wmax + 2, 0xFF, 2 * sizeof(unsigned), st));
     const int wgrid = (int)std::min<int64_t>((w2_len + 255) / 256, (int64_t)ctx->num_sms * 8);
     gram_wmax_kernel<<<wgrid, 256, 0, st>>>(s, s2, N, wmax);
     KEVD_LAUNCH(ctx);
     gram_w2_kernel<<<wgrid, 256, 0, st>>>(s, s2, N, w2_len, w2, w22);
     KEVD_LAUNCH(ctx);
+    // the split: f16 when every Gram's weights span at most kF16WeightRange
+    // (the host reads the four extremes), else tf32
+    unsigned hw[4];
+    KEVD_CUDA(ctx, cudaMemcpyAsync(hw, wmax, sizeof(hw), cudaMemcpyDeviceToHost, st));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(st));
+    bool f16 = true;
+    for (int g = 0; g < nG; ++g) {
+        float mx, mn;
+        std::memcpy(&mx, &hw[g], sizeof(float));
+        std::memcpy(&mn, &hw[2 + g], sizeof(float));
+        f16 = f16 && mn > 0.f && std::isfinite(mx) && mx <= kF16WeightRange * mn;
+    }
     const GramExp ex{exps, exps + k, exps + 2 * k};
-    gram_exp_kernel<<<ceil_div(k, 256), 256, 0, st>>>(colmax, wmax, nG, k, exps, exps + k, exps + 2 * k);
-    KEVD_LAUNCH(ctx);
-    {
-        ProfScope ps(ctx, "gram_tc", st);
-        if (nG == 1) {
-            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel<1>), (int)kSmemBytes));
-            gram_tc_kernel<1><<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(
-                tmF, w2, w2, ex, N, k, n_tiles, rows_per, partial, scratch, n_scratch, err);
-        } else {
-            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&gram_tc_kernel<2>), (int)kSmemBytes));
-            gram_tc_kernel<2><<<n_tiles * n_split, kThreads, kSmemBytes, st>>>(
-                tmF, w2, w22, ex, N, k, n_tiles, rows_per, partial, scratch, n_scratch, err);
-        }
+    if (f16) {
+        gram_exp_kernel<<<ceil_div(k, 256), 256, 0, st>>>(colmax, wmax, nG, k, exps, exps + k, exps + 2 * k);
         KEVD_LAUNCH(ctx);
+    } else {
+        KEVD_CUDA(ctx, cudaMemsetAsync(exps, 0, (size_t)3 * k * sizeof(int), st));
+    }
+    {
+        ProfScope ps(ctx, f16 ? "gram_tc" : "gram_tc_tf32", st);
+        const int grid = n_tiles * n_split;
+        auto launch = [&](auto kern) -> int {
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(kern), (int)kSmemBytes));
+            kern<<<grid, kThreads, kSmemBytes, st>>>(tmF, w2, nG == 2 ? w22 : w2, ex, N, k, n_tiles, rows_per,
+                                                      partial, scratch, n_scratch, err);
+            KEVD_LAUNCH(ctx);
+            return KEVD_OK;
+        };
+        if (nG == 1) {
+            KEVD_TRY(f16 ? launch(&gram_tc_kernel<1, true>) : launch(&gram_tc_kernel<1, false>));
+        } else {
+            KEVD_TRY(f16 ? launch(&gram_tc_kernel<2, true>) : launch(&gram_tc_kernel<2, false>));
+        }
     }
     for (int g = 0; g < nG; ++g) {
         gram_tc_reduce_kernel<<<n_tiles, 256, 0, st>>>(partial, n_tiles, n_split, nG, g, k, g ? ex.ea1 : ex.ea0,

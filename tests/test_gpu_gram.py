@@ -87,3 +87,25 @@ def test_gram_fp64_factor(ctx):
     s = rng.uniform(0.5, 2.0, 3000)
     G = api.weighted_gram(ctx, torch.from_numpy(F).cuda(), torch.from_numpy(s).cuda()).cpu().numpy()
     np.testing.assert_allclose(G, _ref(F, s), rtol=1e-12, atol=1e-10)
+
+
+@pytest.mark.parametrize("spread", [1e2, 1e9])
+def test_gram2_tc_weight_range(ctx, spread):
+    """Row weights spanning a factor `spread` (s^2 spans its square): up to
+    2^16 in s^2 the Grams take the f16 split, beyond it the tf32 split (the
+    bistochastic weights of a nearly diagonal kernel span 1e17); both stay
+    within the tolerance of FP64 sums."""
+    from kernel_evd_gb300 import api
+    N, k = 40000, 200
+    rng = np.random.default_rng(5)
+    Fb = rng.standard_normal((N, k)).astype(np.float32)
+    Fb[:, : k // 3] = np.abs(Fb[:, : k // 3]) + 0.5
+    s = np.exp(rng.uniform(-0.5, 0.5, N) * np.log(spread))
+    s2 = np.exp(rng.uniform(-0.5, 0.5, N) * np.log(spread))
+    G, G2 = api.weighted_gram2(ctx, torch.from_numpy(Fb).cuda(), torch.from_numpy(s).cuda(),
+                               torch.from_numpy(s2).cuda())
+    for Gt, w in ((G, s), (G2, s2)):
+        R = _ref(Fb, w)
+        scale = np.sqrt(np.outer(np.diag(R), np.diag(R)))
+        err = (np.abs(Gt.cpu().numpy() - R) / scale).max()
+        assert err < GRAM_RTOL, err
