@@ -364,6 +364,7 @@ def batched_phase(ctx, args):
     # FP64 on the same pivots, per dataset
     t0 = time.time()
     errs = []
+    err_of = {}
     singular = []   # datasets whose pivot set is numerically singular in FP64 (rank reached before k)
     for q, (f, ev) in enumerate(zip(facs, evs)):
         if ev is None:
@@ -375,6 +376,7 @@ def batched_phase(ctx, args):
             singular.append(q)
             continue
         errs.append(float(np.abs(ev.lam[-16:] - ev64.lam[-16:]).max()))
+        err_of[q] = errs[-1]
         del F64
     check_s = time.time() - t0
     return {"datasets": n_sets, "seconds": total, "stages": timings, "datagen_s": gen_s,
@@ -382,7 +384,7 @@ def batched_phase(ctx, args):
             "autotune": {"calibration_tiles_per_item": tune_c["tiles_per_item"], "calibration_ms": tune_c["ms"]},
             "per_dataset": [{"L": sp[0], "d": sp[1], "N": sp[2], "k": ks_[q], "eps": float(eopt[q]),
                              "rank": int(facs[q].rank), "trace_error": float(facs[q].trace_error),
-                             "evd": status[q]} for q, sp in enumerate(specs)],
+                             "evd": status[q], "top16_err_vs_fp64": err_of.get(q)} for q, sp in enumerate(specs)],
             "trace_error_max": float(max(f.trace_error for f in facs)),
             "evd_failed": failed, "top16_eig_err_vs_fp64_same_pivots_max": float(max(errs)) if errs else None,
             "top16_eig_err_median": float(np.median(errs)) if errs else None, "fp64_check_s": check_s,
