@@ -798,10 +798,10 @@ def main():
     upd_bytes = float(np.sum(N * (4.0 * r_old + 4.0 * acc + 4.0 * d + 16.0)))
     # one launch forms both EVD Grams: two lower triangles incl. the diagonal, 2 flops per MAC
     gram_flops = 2.0 * float(N) * k * (k + 1)
-    # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000
-    # read + wrote 540.6 MB against 542.4 MB of algorithmic bytes; traffic grows with N r, so the
-    # full-size figure is the algorithmic bytes scaled by that ratio
-    upd_traffic_ratio = 540.6 / 542.4
+    # DRAM traffic per update launch: the ncu capture of update_tc_kernel at N = 300,000 (round
+    # 10, r of about 640) read + wrote 935.4 MB against about 927 MB of algorithmic bytes; traffic
+    # grows with N r, so the full-size figure is the algorithmic bytes scaled by that ratio
+    upd_traffic_ratio = 935.4 / 927.0
     roof = {}
     if "rp_update" in prof:
         t = prof["rp_update"][0] / args.steps / 1e3
@@ -811,7 +811,7 @@ def main():
                              "traffic": upd_bytes / nl * upd_traffic_ratio,
                              "bytes_per_launch": upd_bytes / nl,
                              "note": src + "; traffic scaled from the ncu capture at N = 300,000 (DRAM / algorithmic "
-                                     "bytes = 0.997)"}
+                                     "bytes = 1.01)"}
     if "gram_tc" in prof:
         t = prof["gram_tc"][0] / max(1, prof["gram_tc"][1])   # ms per launch
         t = t / 1e3
