@@ -2,24 +2,28 @@
 // tensor cores (the A and B Grams of the bistochastic EVD, ks_kevd.cu:1152-1158,
 // and the single weighted Gram of the API).
 //
-// Precision: a two-term f16 split with the weights on one side,
-// G = (diag(s^2) F)^T F.  Every factor column is scaled by its own power of
-// two into the f16 range (b side: F(:, c) 2^eb_c with 2^eb_c max|F(:, c)|
-// <= 2^14; a side: s^2 F(:, c) 2^ea_c with 2^ea_c max(s^2) max|F(:, c)| <=
-// 2^14), so late columns, orders of magnitude smaller than the first ones,
-// keep their precision clear of the f16 subnormal range; the values are split
-// as hi = rn_f16(v), lo = rn_f16(v - hi): 22 significant bits, the precision
-// of a two-term tf32 split, at twice the kind::tf32 rate and half the operand
-// bytes.  A 128 x 128 output
-// tile accumulates per 32-row stage the cross terms hi_a lo_b^T and
-// lo_a hi_b^T, then hi_a hi_b^T, in FP32 in Tensor Memory; the dropped lo_a
-// lo_b is below 2^-22 of each product.  The tensor-core accumulator rounds
-// each update with a one-sided bias, so the FP32 partial is kept short: every
-// 2048 rows it is added into an FP64 tile in global memory and the long sum
-// over N rows is FP64 (the Gram accumulators of the reference are FP64).  The
-// scales 2^(ea_a + eb_b) of entry (a, b) are removed exactly when the
-// row-split partials are summed.
-// Eigenvalues are then refined in FP64 by Rayleigh-Ritz (kevd_evd.cu).
+// Precision, with the weights on one side, G = (diag(s^2) F)^T F:
+//   f16 split (when every Gram's s^2 spans at most 2^16): every factor column
+//   is scaled by its own power of two into the f16 range (b side: F(:, c)
+//   2^eb_c with 2^eb_c max|F(:, c)| <= 2^14; a side: s^2 F(:, c) 2^ea_c with
+//   2^ea_c max(s^2) max|F(:, c)| <= 2^14), so late columns, orders of
+//   magnitude smaller than the first ones, stay clear of the f16 subnormal
+//   range; hi = rn_f16(v), lo = rn_f16(v - hi) carry 22 significant bits, the
+//   precision of a two-term tf32 split, at twice the kind::tf32 rate and half
+//   the operand bytes.  The scales 2^(ea_a + eb_b) of entry (a, b) are removed
+//   exactly when the row-split partials are summed.
+//   tf32 split (any weights: the bistochastic weights of a nearly diagonal
+//   kernel span 1e17, beyond any f16 scale): v as the tensor core reads it
+//   (hi, its 13 low mantissa bits dropped) and lo = v - trunc_tf32(v), exact in
+//   FP32.
+// A 128 x 128 output tile accumulates per 32-row stage the cross terms
+// hi_a lo_b^T and lo_a hi_b^T and hi_a hi_b^T in FP32 in Tensor Memory; the
+// dropped lo_a lo_b is below 2^-20 of each product.  The tensor-core
+// accumulator rounds each update with a one-sided bias, so the FP32 partial is
+// kept short: every 2048 rows it is added into an FP64 tile in global memory
+// and the long sum over N rows is FP64 (the Gram accumulators of the reference
+// are FP64).  Eigenvalues are then refined in FP64 by Rayleigh-Ritz
+// (kevd_evd.cu).
 //
 // CTA roles (448 threads):
 //   warps 0-3   epilogue: TMEM -> registers -> FP64 tile (warp q owns TMEM
@@ -31,8 +35,9 @@
 //   warp 9      TMEM allocation and the single MMA-issuing thread (A from
 //               Tensor Memory, B from shared memory)
 //   warps 10-13 b converters: row m of the b tile split into the f16 b-hi and
-//               b-lo tiles (SWIZZLE_64B); on a diagonal tile (b = a) the a
-//               converters write them
+//               b-lo tiles (SWIZZLE_64B), or its tf32 lo part into an FP32
+//               b-lo tile (the raw tile is then b-hi); on a diagonal tile
+//               (b = a) the a converters write them
 // A 4-stage ring (shared-memory tiles and Tensor Memory a-slots) and one TMEM
 // accumulator per Gram are handed over with mbarriers; every wait is bounded
 // and sets an error flag on timeout.
