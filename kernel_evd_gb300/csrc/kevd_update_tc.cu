@@ -64,7 +64,7 @@ constexpr int kRows = 128;          // rows per block (MMA M)
 constexpr int kCols = 64;           // accepted columns per round (MMA N), nacc <= 64
 constexpr int kKs = 32;             // F columns per stage
 // Pipeline shape (tuning parameters; Tensor Memory holds kBufs partial buffers
-// of 64 columns and kStages a-slots of 32 columns)
+// of 128 columns and kStages a-slots of 32 columns)
 #ifndef KEVD_UPD_STAGES
 #define KEVD_UPD_STAGES 6
 #endif
