@@ -74,6 +74,62 @@ struct RpcholDeferred {
     int64_t* piv_h;
 };
 
+// Kernel values of a fixed pseudo-random sample of kDensityPairs pairs (i, j),
+// i != j, counted when K(i, j) >= 2^-24.  A factorisation whose kernel is
+// nearly diagonal (fewer than half the sampled values reach 2^-24) keeps the
+// FP32 SIMT residual update: the tensor-core update splits F into f16 parts
+// scaled to |F| <= 1, which hold F's tiny entries only to about 2^-39
+// absolutely, and the bistochastic weights 1/dtil^2 of such kernels amplify
+// exactly those rows (top-16 eigenvalue errors of 1e-6 .. 1e-5 against FP64
+// on the same pivots, against at most 7e-7 with the SIMT update).
+constexpr int kDensityPairs = 4096;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {   // splitmix64 finaliser
+    z ^= z >> 30;
+    z *= 0xBF58476D1CE4E5B9ull;
+    z ^= z >> 27;
+    z *= 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) kernel_density_kernel(const float* __restrict__ X, int64_t N, int d,
+                                                              double scale, int* __restrict__ count) {
+    int c = 0;
+    for (int t = threadIdx.x; t < kDensityPairs; t += blockDim.x) {
+        const int64_t i = (int64_t)(mix64(2 * (uint64_t)t + 1) % (uint64_t)N);
+        int64_t j = (int64_t)(mix64(2 * (uint64_t)t + 2) % (uint64_t)N);
+        if (j == i) j = (i + 1) % N;
+        float d2 = 0.f;
+        for (int f = 0; f < d; ++f) {
+            const float u = X[i * d + f] - X[j * d + f];
+            d2 = fmaf(u, u, d2);
+        }
+        c += (exp(-scale * (double)d2) >= 5.9604644775390625e-8) ? 1 : 0;   // 2^-24
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(count, c);
+}
+
+// Whether the kernel is nearly diagonal (see kernel_density_kernel); one
+// small launch and a 4-byte copy.  Must not run inside a stream capture.
+static int kernel_nearly_diagonal(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale, cudaStream_t s,
+                                  bool* out) {
+    *out = false;
+    if (N < 2) return KEVD_OK;
+    int st = KEVD_OK;
+    int* cnt = arena_get<int>(ctx, "rp.density", 1, &st);
+    if (st != KEVD_OK) return set_error(ctx, st, "rpchol: out of device memory");
+    KEVD_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int), s));
+    kernel_density_kernel<<<1, 256, 0, s>>>(X, N, d, scale, cnt);
+    KEVD_LAUNCH(ctx);
+    int* h = static_cast<int*>(ctx->pinned);
+    KEVD_CUDA(ctx, cudaMemcpyAsync(h, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    KEVD_CUDA(ctx, cudaStreamSynchronize(s));
+    *out = 2 * *h < kDensityPairs;
+    return KEVD_OK;
+}
+
 __global__ void rp_init_kernel(double* __restrict__ d, double* __restrict__ dblk, int64_t N,
                                int64_t nblk, RoundState* st) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
@@ -704,7 +760,7 @@ template <typename T>
 static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
                        const kevd_rpchol_params* p, T* F, int64_t ldF, int64_t* piv_h,
                        double* err_h, int32_t* hm_h, kevd_rpchol_result* res, cudaStream_t s,
-                       RpcholDeferred* defer = nullptr) {
+                       RpcholDeferred* defer = nullptr, bool tc_allowed = true) {
     const int b = p->block;
     const double floor_rel = sizeof(T) == 4 ? kMixedFloor : 0.0;
     const int64_t nblk = (N + kRowBlock - 1) / kRowBlock;
@@ -749,8 +805,10 @@ static int rpchol_impl(kevd_ctx* ctx, const float* X, int64_t N, int d, double s
     const size_t usm = update_smem<T>(d);
     KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(&rp_update_kernel<T>), (int)usm));
     int* done_h = static_cast<int*>(ctx->pinned);
-    // FP32 factors take the tensor-core residual update when the layout allows TMA
-    const bool use_tc = sizeof(T) == 4 && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d);
+    // FP32 factors take the tensor-core residual update when the layout allows
+    // TMA and the kernel is not nearly diagonal (kernel_density_kernel)
+    const bool use_tc =
+        sizeof(T) == 4 && tc_allowed && update_tc_supported(reinterpret_cast<const float*>(F), ldF, d);
     int* tc_err = arena_get<int>(ctx, "rp.tcerr", 1, &st);
     if (st != KEVD_OK) return st;
     KEVD_CUDA(ctx, cudaMemsetAsync(tc_err, 0, sizeof(int), s));
@@ -841,8 +899,11 @@ int run_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int d, double scale,
         return set_error(ctx, KEVD_ERR_ARG, "rpchol: need k_max >= 1, ldF >= k_max, max_rounds >= 1");
     if (p->precision == KEVD_FP64)
         return rpchol_impl<double>(ctx, X, N, d, scale, p, (double*)F, ldF, piv, err, accepted, res, s);
-    if (p->precision == KEVD_MIXED)
-        return rpchol_impl<float>(ctx, X, N, d, scale, p, (float*)F, ldF, piv, err, accepted, res, s);
+    if (p->precision == KEVD_MIXED) {
+        bool diag = false;
+        if (update_tc_supported((const float*)F, ldF, d)) KEVD_TRY(kernel_nearly_diagonal(ctx, X, N, d, scale, s, &diag));
+        return rpchol_impl<float>(ctx, X, N, d, scale, p, (float*)F, ldF, piv, err, accepted, res, s, nullptr, !diag);
+    }
     return set_error(ctx, KEVD_ERR_ARG, "rpchol: unknown precision %d", p->precision);
 }
 
@@ -903,6 +964,14 @@ int run_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int n_jobs, int use
     }
     if (rc == KEVD_OK && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
         rc = set_error(ctx, KEVD_ERR_CUDA, "rpchol_batched: event setup failed");
+    // the residual-update form of every job, decided before any capture
+    std::vector<char> tc_ok(n_jobs, 1);
+    for (int q = 0; q < n_jobs && rc == KEVD_OK; ++q) {
+        const kevd_rpchol_job& j = jobs[q];
+        bool diag = false;
+        if (update_tc_supported((const float*)j.F, j.ldF, j.d)) rc = kernel_nearly_diagonal(ctx, j.X, j.N, j.d, j.scale, s, &diag);
+        tc_ok[q] = diag ? 0 : 1;
+    }
     // the capture runs on a stream of its own (the caller's stream may be the
     // legacy default stream, which cannot be captured); it is ordered after the
     // caller's work and the graph is launched on the caller's stream
@@ -926,7 +995,7 @@ int run_rpchol_batched(kevd_ctx* ctx, kevd_rpchol_job* jobs, int n_jobs, int use
             p.precision = KEVD_MIXED;
             RpcholDeferred df{x.state_h, x.tcerr_h, x.piv_h};
             const int r = rpchol_impl<float>(x.c, j.X, j.N, j.d, j.scale, &p, (float*)j.F, j.ldF, nullptr, nullptr,
-                                             nullptr, nullptr, x.st, &df);
+                                             nullptr, nullptr, x.st, &df, tc_ok[q] != 0);
             ctx->launches += x.c->launches;
             x.c->launches = 0;
             if (r != KEVD_OK) return set_error(ctx, r, "rpchol_batched: job %d: %s", q, x.c->last_error.c_str());

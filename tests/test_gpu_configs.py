@@ -108,21 +108,24 @@ def test_mixed_low_rank_dataset_stops_at_the_fp32_floor(ctx):
     assert np.abs(em.lam[-16:] - e64.lam[-16:]).max() < 1e-6
 
 
-def test_mixed_evd_of_a_nearly_diagonal_kernel(ctx):
+@pytest.mark.parametrize("k", [115, 116])
+def test_mixed_evd_of_a_nearly_diagonal_kernel(ctx, k):
     """A batched-workload dataset whose calibrated eps is tiny against its
-    pair distances (L = 22, d = 32, N = 51,194, k = 115, eps = 2.806): the
-    kernel is nearly the identity, rows far from every pivot keep a tiny factor
-    row, and the EVD's row weights 1/dtil^2 span about 1e17.  The Grams must
-    take the split that keeps such weights (tf32) and the mixed EVD must match
-    the FP64 EVD of the same pivots."""
+    pair distances (L = 22, d = 32, N = 51,194, eps = 2.806; its own k is 115):
+    the kernel is nearly the identity, rows far from every pivot keep a tiny
+    factor row, and the EVD's row weights 1/dtil^2 span about 1e17.  The Grams
+    must take the split that keeps such weights (tf32), the factorisation the
+    FP32 residual update also when the factor layout would allow the
+    tensor-core one (k = 116), and the mixed EVD must match the FP64 EVD of the
+    same pivots."""
     from kernel_evd_gb300 import api, datagen
     i, eps = 16, 2.805720090866089
     rng = np.random.default_rng(1000 + i)
     L = float(rng.choice([16.0, 22.0, 36.0]))
     m = int(rng.choice([32, 64, 128]))
     n = int(np.exp(rng.uniform(np.log(1e4), np.log(4e5))))
-    k = min(int(rng.integers(100, 1001)), n // 2)
-    assert (L, m, n, k) == (22.0, 32, 51194, 115)
+    k_own = min(int(rng.integers(100, 1001)), n // 2)
+    assert (L, m, n, k_own) == (22.0, 32, 51194, 115)
     X = datagen.seeded_states(n, L=L, M=m, seed=i, warm_time=1000.0, dt=0.25).astype(np.float32)
     Xd = torch.from_numpy(X).cuda()
     fac = api.rpcholesky(ctx, Xd, 1.0 / eps, k_max=k, block=32, seed=i, precision="mixed")
@@ -131,3 +134,9 @@ def test_mixed_evd_of_a_nearly_diagonal_kernel(ctx):
     ev64 = api.bistochastic_evd(ctx, F64, k_out=16)
     assert abs(ev.lam[-1] - 1.0) < 1e-8
     np.testing.assert_allclose(ev.lam[-16:], ev64.lam[-16:], rtol=0, atol=1e-6)
+    if k == 116:   # the update form in use: the SIMT update writes no tensor-core profile entry
+        api.profile_enable(ctx, True)
+        api.rpcholesky(ctx, Xd, 1.0 / eps, k_max=k, block=32, seed=i, precision="mixed")
+        prof = api.profile_read(ctx)
+        api.profile_enable(ctx, False)
+        assert "rp_update" in prof and "rp_update_kcols" not in prof
