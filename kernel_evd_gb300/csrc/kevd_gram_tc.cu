@@ -20,7 +20,7 @@
 // hi_a lo_b^T and lo_a hi_b^T and hi_a hi_b^T in FP32 in Tensor Memory; the
 // dropped lo_a lo_b is below 2^-20 of each product.  The tensor-core
 // accumulator rounds each update with a one-sided bias, so the FP32 partial is
-// kept short: every 2048 rows it is added into an FP64 tile in global memory
+// kept short: every 1920 rows it is added into an FP64 tile in global memory
 // and the long sum over N rows is FP64 (the Gram accumulators of the reference
 // are FP64).  Eigenvalues are then refined in FP64 by Rayleigh-Ritz
 // (kevd_evd.cu).
@@ -38,9 +38,9 @@
 //               b-lo tiles (SWIZZLE_64B), or its tf32 lo part into an FP32
 //               b-lo tile (the raw tile is then b-hi); on a diagonal tile
 //               (b = a) the a converters write them
-// A 4-stage ring (shared-memory tiles and Tensor Memory a-slots) and one TMEM
-// accumulator per Gram are handed over with mbarriers; every wait is bounded
-// and sets an error flag on timeout.
+// A ring of 6 (f16) or 4 (tf32) stages of shared-memory tiles, 4 (f16) or 2
+// (tf32) Tensor Memory a-slots and one TMEM accumulator per Gram are handed
+// over with mbarriers; every wait is bounded and sets an error flag on timeout.
 #include "kevd_internal.cuh"
 #include "kevd_tc.cuh"
 
@@ -57,15 +57,25 @@ namespace {
 
 constexpr int kTT = 128;               // output tile edge
 constexpr int kTK = 32;                // rows of F per stage (MMA K per stage)
-constexpr int kStages = 4;
-constexpr int kFlushStages = 64;       // 2048 rows per FP32 TMEM partial
+constexpr int kMaxStages = 6;
+constexpr int kFlushStages = 60;       // 1920 rows per FP32 TMEM partial (a multiple of both ring depths)
 constexpr int kOpBytes = kTT * kTK * 4;     // one raw FP32 operand tile, 16 KB
 constexpr int kHalfBytes = kTT * kTK * 2;   // one f16 operand tile, 8 KB
-// Per stage: [a raw 16 KB][b raw 16 KB][b hi 8 KB][b lo 8 KB]; a multiple of
-// 1024, so every stage stays 1024-aligned (the TMA's SWIZZLE_128B boxes)
-constexpr int kOffB = kOpBytes, kOffBh = 2 * kOpBytes, kOffBl = 2 * kOpBytes + kHalfBytes;
-constexpr int kStageBytes = 2 * kOpBytes + 2 * kHalfBytes;
-static_assert(kStageBytes % 1024 == 0, "stage alignment");
+constexpr int kOffB = kOpBytes;             // the b region of a stage
+// Stage layout (every stage 1024-aligned for the TMA's SWIZZLE_128B boxes):
+//   f16:  [a raw 16 KB][b raw 16 KB, split in place]: rows 8i..8i+7 of the raw
+//         b tile occupy bytes [1024 i, 1024 i + 1024) of the b region, and the
+//         b converters replace them by the SW64 atoms of the same rows, b-hi at
+//         1024 i, b-lo at 1024 i + 512 (each warp's 32 rows stay inside its own
+//         4 KB, so a warp-level sync orders the reads before the writes);
+//         6 stages
+//   tf32: [a raw 16 KB][b raw 16 KB = b-hi][b-lo FP32 16 KB]; 4 stages
+template <bool F16> struct Layout {
+    static constexpr int stages = F16 ? 6 : 4;
+    static constexpr int stage_bytes = F16 ? 2 * kOpBytes : 3 * kOpBytes;
+    static constexpr int off_blo32 = 2 * kOpBytes;   // tf32 b-lo tile
+    static_assert(stage_bytes % 1024 == 0 && stages <= kMaxStages && kFlushStages % stages == 0, "ring shape");
+};
 constexpr int kEpiWarps = 4;        // warps 0-3
 constexpr int kCvtWarp0 = 4;        // warps 4-7: a operand -> Tensor Memory
 constexpr int kProdWarp = 8;
@@ -83,7 +93,7 @@ template <bool F16> struct Slots {
     static constexpr uint32_t gram_cols = F16 ? 32 : 64;   // one Gram's hi + lo
     static constexpr uint32_t lo_off = F16 ? 16 : 32;
     static_assert(kTmemA + n * cols <= kTmemCols, "Tensor Memory holds 512 columns");
-    static_assert(kFlushStages % kStages == 0 && kStages % n == 0, "slot indices are compile-time per stage");
+
 };
 // Weight ranges (max s^2 / min s^2) above this take the tf32 split: the f16
 // split keeps a factor column's values within 2^-28 .. 2^14 of its own scale at
@@ -92,10 +102,10 @@ constexpr float kF16WeightRange = 65536.f;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 
 struct Barriers {
-    alignas(16) float w2[kStages][2][32];   // squared row weights of each stage, A then B
-    uint64_t tma[kStages];
-    uint64_t full[kStages];
-    uint64_t empty[kStages];
+    alignas(16) float w2[kMaxStages][2][32];   // squared row weights of each stage, A then B
+    uint64_t tma[kMaxStages];
+    uint64_t full[kMaxStages];
+    uint64_t empty[kMaxStages];
     uint64_t tfree[4];
     uint64_t accf;
     uint64_t acce[2];
@@ -103,8 +113,11 @@ struct Barriers {
     uint32_t tmem_base;
 };
 
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + sizeof(Barriers) + 1024;
-static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
+template <bool F16>
+constexpr size_t smem_bytes() {
+    return (size_t)Layout<F16>::stages * Layout<F16>::stage_bytes + sizeof(Barriers) + 1024;
+}
+static_assert(smem_bytes<true>() <= 227 * 1024 && smem_bytes<false>() <= 227 * 1024, "shared memory per CTA");
 
 // Power-of-two scale exponents of one Gram call (device, per factor column c):
 // eb[c] for the b side, ea[g][c] for the a side of Gram g.
@@ -143,16 +156,19 @@ __device__ __forceinline__ void store_row(uint8_t* tile, int m, const float (&x)
             make_float4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
 }
 
-// Row m of the b-hi and b-lo tiles from the 32 raw values of b row m.
-__device__ __forceinline__ void store_b_split(uint8_t* st, int m, const float (&x)[32], float bscale) {
+// Row m of the interleaved b-hi / b-lo atoms of a b region (f16 layout) from
+// the 32 raw values of b row m.
+__device__ __forceinline__ void store_b_split(uint8_t* breg, int m, const float (&x)[32], float bscale) {
     uint32_t h[16], l[16];
 #pragma unroll
     for (int p = 0; p < 16; ++p) tc::split_f16x2(x[2 * p] * bscale, x[2 * p + 1] * bscale, h[p], l[p]);
+    // sw64_off16 places row m at (m >> 3) * 512 + ...; the atoms here are 1024 apart
+    const uint32_t atom = (uint32_t)(m >> 3) * 1024u;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const uint32_t off = tc::sw64_off16((uint32_t)m, 8u * c);
-        *reinterpret_cast<uint4*>(st + kOffBh + off) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
-        *reinterpret_cast<uint4*>(st + kOffBl + off) = make_uint4(l[4 * c], l[4 * c + 1], l[4 * c + 2], l[4 * c + 3]);
+        const uint32_t off = atom + (tc::sw64_off16((uint32_t)(m & 7), 8u * c));
+        *reinterpret_cast<uint4*>(breg + off) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+        *reinterpret_cast<uint4*>(breg + off + 512) = make_uint4(l[4 * c], l[4 * c + 1], l[4 * c + 2], l[4 * c + 3]);
     }
 }
 
@@ -174,6 +190,9 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
                double* __restrict__ partial, float* __restrict__ scratch, int n_scratch, int* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    using LY = Layout<F16>;
+    constexpr int kStages = LY::stages;
+    constexpr int kStageBytes = LY::stage_bytes;
     Barriers* bar = reinterpret_cast<Barriers*>(base + (size_t)kStages * kStageBytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -310,12 +329,12 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
                 }
                 if (diag) {
                     if constexpr (F16) {
-                        store_b_split(st, m, x, bscale);
+                        store_b_split(st + kOffB, m, x, bscale);
                     } else {
                         float l[32];
 #pragma unroll
                         for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                        store_row(st + kOffBh, m, l);
+                        store_row(st + LY::off_blo32, m, l);
                     }
                 }
                 tc::tmem_wait_st();
@@ -323,12 +342,13 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
             } else if (!diag) {
                 load_row(st + kOffB, m, x);
                 if constexpr (F16) {
-                    store_b_split(st, m, x, bscale);
+                    __syncwarp();   // the warp's raw rows are read before its atoms are rewritten
+                    store_b_split(st + kOffB, m, x, bscale);
                 } else {
                     float l[32];
 #pragma unroll
                     for (int u = 0; u < 32; ++u) l[u] = x[u] - tc::tf32_trunc(x[u]);
-                    store_row(st + kOffBh, m, l);
+                    store_row(st + LY::off_blo32, m, l);
                 }
             }
             tc::fence_async_smem();
@@ -351,20 +371,21 @@ gram_tc_kernel(const __grid_constant__ CUtensorMap tmF, const float* __restrict_
 #pragma unroll
                     for (int sl = 0; sl < kStages; ++sl) {
                         if (sb + sl >= s1) break;
-                        const int ts = sl % SL::n;   // sb is a multiple of kStages, hence of the slot count
+                        const int ts = (int)((sb + sl) % SL::n);
                         uint64_t dbh[kSteps], dbl[kSteps];
                         uint8_t* stg = base + (size_t)sl * kStageBytes;
 #pragma unroll
                         for (int j = 0; j < kSteps; ++j) {   // +32 bytes of K per MMA
                             if constexpr (F16) {
-                                const uint32_t bh = tc::smem_u32(stg + kOffBh);
-                                dbh[j] = tc::desc_sw64(bh + 32u * j);
-                                dbl[j] = tc::desc_sw64(bh + kHalfBytes + 32u * j);
+                                // interleaved atoms: b-hi at +0, b-lo at +512, 1024 apart
+                                const uint32_t bh = tc::smem_u32(stg + kOffB);
+                                dbh[j] = tc::desc_sw64_sbo1024(bh + 32u * j);
+                                dbl[j] = tc::desc_sw64_sbo1024(bh + 512u + 32u * j);
                             } else {
                                 // b-hi: the raw b tile (the raw a tile on a diagonal
-                                // tile); b-lo: the FP32 tile at kOffBh
+                                // tile); b-lo: the FP32 tile
                                 const uint32_t bh = tc::desc_lo_sw128(tc::smem_u32(diag ? stg : stg + kOffB));
-                                const uint32_t bl = tc::desc_lo_sw128(tc::smem_u32(stg + kOffBh));
+                                const uint32_t bl = tc::desc_lo_sw128(tc::smem_u32(stg + LY::off_blo32));
                                 dbh[j] = tc::desc_sw128_from_lo(bh + 2u * j);
                                 dbl[j] = tc::desc_sw128_from_lo(bl + 2u * j);
                             }
@@ -739,8 +760,9 @@ static int gram_tc_impl(kevd_ctx* ctx, const float* FT, int64_t ldT, int64_t N, 
         ProfScope ps(ctx, f16 ? "gram_tc" : "gram_tc_tf32", st);
         const int grid = n_tiles * n_split;
         auto launch = [&](auto kern) -> int {
-            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(kern), (int)kSmemBytes));
-            kern<<<grid, kThreads, kSmemBytes, st>>>(tmF, w2, nG == 2 ? w22 : w2, ex, N, k, n_tiles, rows_per,
+            const size_t smem = f16 ? smem_bytes<true>() : smem_bytes<false>();
+            KEVD_CUDA(ctx, raise_smem_limit(reinterpret_cast<const void*>(kern), (int)smem));
+            kern<<<grid, kThreads, smem, st>>>(tmF, w2, nG == 2 ? w22 : w2, ex, N, k, n_tiles, rows_per,
                                                       partial, scratch, n_scratch, err);
             KEVD_LAUNCH(ctx);
             return KEVD_OK;

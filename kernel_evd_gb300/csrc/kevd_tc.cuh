@@ -297,6 +297,13 @@ __device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
     return ((uint64_t)desc_hi_sw64() << 32) | (((saddr & 0x3FFFFu) >> 4) | (1u << 16));
 }
 
+// The same with 8-row atoms 1024 B apart (two SW64 tiles interleaved atom by
+// atom: one at +0, the other at +512).
+__device__ __forceinline__ uint64_t desc_sw64_sbo1024(uint32_t saddr) {
+    return ((uint64_t)((1024u >> 4) | (1u << (46 - 32)) | (4u << (61 - 32))) << 32) |
+           (((saddr & 0x3FFFFu) >> 4) | (1u << 16));
+}
+
 // Byte offset of 16-bit element (row, k) in a K-major SW64 tile: 64-byte rows,
 // 16-byte chunk index (address bits 4-5) XORed with address bits 7-8.
 __host__ __device__ constexpr uint32_t sw64_off16(uint32_t row, uint32_t k) {

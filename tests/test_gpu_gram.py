@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 # Relative error bound of a Gram entry against sqrt(G_ii G_jj): the tensor-core
 # FP32 accumulator rounds each MMA update with a one-sided bias, and a TMEM
-# partial takes 2048 rows (128 k-steps x 3 products) before its FP64 flush.
+# partial takes 1920 rows before its FP64 flush.
 GRAM_RTOL = 6e-5
 
 
@@ -33,7 +33,7 @@ def test_gram_tc_fp32_factor(ctx, N, k, ld):
     scale = np.sqrt(np.outer(np.diag(R), np.diag(R)))
     err = np.abs(G - R) / scale
     # two-term f16 products (22-bit hi/lo pieces); the tensor-core FP32
-    # accumulator over 2048-row partials limits the relative error (FP64 across
+    # accumulator over 1920-row partials limits the relative error (FP64 across
     # partials)
     assert err.max() < GRAM_RTOL, err.max()
     np.testing.assert_allclose(G, G.T, rtol=0, atol=0)
@@ -62,7 +62,7 @@ def test_gram2_tc_one_pass(ctx, N, k, ld):
 
 
 def test_gram2_tc_full_flush_length(ctx):
-    """Row splits long enough for full 2048-row TMEM partials before each FP64
+    """Row splits long enough for full 1920-row TMEM partials before each FP64
     flush (N = 300,000, k = 512: about 2,500 rows per split)."""
     from kernel_evd_gb300 import api
     N, k = 300_000, 512
