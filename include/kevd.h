@@ -203,7 +203,12 @@ typedef struct {
  * written.  piv: host, k_max int64 (pivots in acceptance order, the
  * reference's /spiv).  err, accepted: host, max_rounds entries (per-round
  * trace error and accepted count, the reference's round table
- * ks_arpclm.cu:1129-1136).  Replaces the round loop ks_arpclm.cu:793-1046. */
+ * ks_arpclm.cu:1129-1136).  Replaces the round loop ks_arpclm.cu:793-1046.
+ * KEVD_MIXED runs the residual update on the tensor cores when ldF % 4 == 0
+ * and F is 16-byte aligned, unless the kernel is nearly diagonal (fewer than
+ * half of 4,096 sampled kernel values reach 2^-24: the call then makes one
+ * 4-byte device-to-host copy before the round loop and keeps the FP32 SIMT
+ * update); otherwise the FP32 SIMT update. */
 int kevd_rpchol(kevd_ctx* ctx, const float* X, int64_t N, int32_t d,
                 double scale, const kevd_rpchol_params* params, void* F,
                 int64_t ldF, int64_t* piv, double* err, int32_t* accepted,
