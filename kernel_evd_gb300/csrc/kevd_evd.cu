@@ -392,15 +392,21 @@ evt_rowdot_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t 
     if (!(acc > 0.0)) atomicOr(bad, 1);
 }
 
-// U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32)
+// U[i][:] = dinv_i * sum_j FT[j][i] Z[j][:]  (Z: k x m column-major FP64, m <= 32).
+// CTA = 256 rows; thread t forms columns 16 h .. 16 h + 15 (h = t & 1) of rows
+// p and p + 128 (p = t >> 1), so every broadcast load of a Z row feeds twice as
+// many FMAs as with one full row per thread (there the shared-memory loads
+// and the FMAs each filled their pipe) at the same 32 accumulators.
 __global__ void __launch_bounds__(256)
 evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, const double* __restrict__ Z, int m,
              const double* __restrict__ dinv, float* __restrict__ U, float* __restrict__ Y) {
     __shared__ __align__(16) float Zs[128][32];
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    float acc[32];
+    const int h = threadIdx.x & 1, p = threadIdx.x >> 1;
+    const int64_t i0 = (int64_t)blockIdx.x * 256 + p, i1 = i0 + 128;
+    const bool v0 = i0 < N, v1 = i1 < N;
+    float acc0[16], acc1[16];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) acc[q] = 0.f;
+    for (int q = 0; q < 16; ++q) acc0[q] = acc1[q] = 0.f;
     for (int64_t j0 = 0; j0 < k; j0 += 128) {
         __syncthreads();
         for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
@@ -409,43 +415,62 @@ evt_u_kernel(const float* __restrict__ FT, int64_t ldT, int64_t N, int64_t k, co
             Zs[jj][q] = (j < k && q < m) ? (float)Z[(int64_t)q * k + j] : 0.f;
         }
         __syncthreads();
-        if (i < N) {
+        if (v0) {
             const int jn = (int)min((int64_t)128, k - j0);
-            // the four F values of the next step are loaded before this step's
-            // FMAs (columns past jn read as zero; Zs is zero there too)
-            float fn[4];
+            // the F values of the next four columns are loaded before this
+            // step's FMAs (columns past jn read as zero; Zs is zero there too)
+            float g0[4], g1[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) fn[u] = (u < jn) ? FT[(j0 + u) * ldT + i] : 0.f;
+            for (int u = 0; u < 4; ++u) {
+                g0[u] = (u < jn) ? FT[(j0 + u) * ldT + i0] : 0.f;
+                g1[u] = (u < jn && v1) ? FT[(j0 + u) * ldT + i1] : 0.f;
+            }
             for (int jj = 0; jj < jn; jj += 4) {
-                float f[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) f[u] = fn[u];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) fn[u] = (jj + 4 + u < jn) ? FT[(j0 + jj + 4 + u) * ldT + i] : 0.f;
+                float f0[4], f1[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const float4* zr = reinterpret_cast<const float4*>(Zs[jj + u]);
+                    f0[u] = g0[u];
+                    f1[u] = g1[u];
+                }
 #pragma unroll
-                    for (int q4 = 0; q4 < 8; ++q4) {
+                for (int u = 0; u < 4; ++u) {
+                    const bool in = jj + 4 + u < jn;
+                    g0[u] = in ? FT[(j0 + jj + 4 + u) * ldT + i0] : 0.f;
+                    g1[u] = (in && v1) ? FT[(j0 + jj + 4 + u) * ldT + i1] : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4* zr = reinterpret_cast<const float4*>(Zs[jj + u] + 16 * h);
+#pragma unroll
+                    for (int q4 = 0; q4 < 4; ++q4) {
                         const float4 z = zr[q4];
-                        acc[4 * q4 + 0] = fmaf(f[u], z.x, acc[4 * q4 + 0]);
-                        acc[4 * q4 + 1] = fmaf(f[u], z.y, acc[4 * q4 + 1]);
-                        acc[4 * q4 + 2] = fmaf(f[u], z.z, acc[4 * q4 + 2]);
-                        acc[4 * q4 + 3] = fmaf(f[u], z.w, acc[4 * q4 + 3]);
+                        acc0[4 * q4 + 0] = fmaf(f0[u], z.x, acc0[4 * q4 + 0]);
+                        acc0[4 * q4 + 1] = fmaf(f0[u], z.y, acc0[4 * q4 + 1]);
+                        acc0[4 * q4 + 2] = fmaf(f0[u], z.z, acc0[4 * q4 + 2]);
+                        acc0[4 * q4 + 3] = fmaf(f0[u], z.w, acc0[4 * q4 + 3]);
+                        acc1[4 * q4 + 0] = fmaf(f1[u], z.x, acc1[4 * q4 + 0]);
+                        acc1[4 * q4 + 1] = fmaf(f1[u], z.y, acc1[4 * q4 + 1]);
+                        acc1[4 * q4 + 2] = fmaf(f1[u], z.z, acc1[4 * q4 + 2]);
+                        acc1[4 * q4 + 3] = fmaf(f1[u], z.w, acc1[4 * q4 + 3]);
                     }
                 }
             }
         }
     }
-    if (i >= N) return;
-    const double di = dinv[i];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) {
-        const float u = (float)((double)acc[q] * di);
-        if (q < m) U[i * m + q] = u;
-        // Y = Dtil^{-1} U of the rounded U, 32 columns (zero beyond m), for the
-        // Rayleigh-Ritz T1 pass
-        if (Y) Y[i * 32 + q] = (q < m) ? (float)((double)u * di) : 0.f;
+    for (int r = 0; r < 2; ++r) {
+        const int64_t i = r ? i1 : i0;
+        if (i >= N) continue;
+        const double di = dinv[i];
+#pragma unroll
+        for (int qq = 0; qq < 16; ++qq) {
+            const int q = 16 * h + qq;
+            const float u = (float)((double)(r ? acc1[qq] : acc0[qq]) * di);
+            if (q < m) U[i * m + q] = u;
+            // Y = Dtil^{-1} U of the rounded U, 32 columns (zero beyond m), for the
+            // Rayleigh-Ritz T1 pass
+            if (Y) Y[i * 32 + q] = (q < m) ? (float)((double)u * di) : 0.f;
+        }
     }
 }
 
