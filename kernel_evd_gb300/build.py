@@ -3,8 +3,9 @@
 ``python -m kernel_evd_gb300.build`` compiles every ``csrc/*.cu`` translation
 unit in parallel with nvcc (one ``-gencode``, ``-lineinfo``) and links
 ``kernel_evd_gb300/lib/libkevd.so`` against cuBLAS and cuSOLVER; the host KS generator
-(``csrc/host/ksgen.c``) is compiled with gcc into ``lib/libksgen.so``.  The drivers
-(``csrc/drivers/*.cpp``) are linked against it into ``kernel_evd_gb300/bin``.
+(``csrc/host/ksgen.c``) is compiled with gcc into ``lib/libksgen.so`` and the HDF5
+dataset layer (``csrc/host/h5file.c``) into ``lib/libkevdh5.so``.  The drivers
+(``csrc/drivers/*.cpp``) are linked against both into ``kernel_evd_gb300/bin``.
 """
 from __future__ import annotations
 
@@ -21,6 +22,8 @@ LIBDIR = os.path.join(HERE, "lib")
 BINDIR = os.path.join(HERE, "bin")
 LIB = os.path.join(LIBDIR, "libkevd.so")
 KSGEN = os.path.join(LIBDIR, "libksgen.so")
+H5LIB = os.path.join(LIBDIR, "libkevdh5.so")
+INCLUDE = os.path.join(HERE, "..", "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -42,6 +45,15 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+def build_h5() -> str:
+    """The HDF5 dataset layer alone (host C, no CUDA)."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    cc = shutil.which("gcc") or shutil.which("cc")
+    _run([cc, "-O2", "-std=c11", "-Wall", "-fPIC", "-shared", "-I", INCLUDE, "-o", H5LIB,
+          os.path.join(CSRC, "host", "h5file.c"), "-lm"])
+    return H5LIB
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
@@ -61,6 +73,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     cc = shutil.which("gcc") or shutil.which("cc")
     _run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-o", KSGEN,
           os.path.join(CSRC, "host", "ksgen.c"), "-lm"])
+    build_h5()
     drivers = os.path.join(CSRC, "drivers")
     if os.path.isdir(drivers):
         os.makedirs(BINDIR, exist_ok=True)
@@ -68,7 +81,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             if f.endswith(".cpp"):
                 exe = os.path.join(BINDIR, f[:-4])
                 _run([nvcc, *ARCH, "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"),
-                      os.path.join(drivers, f), "-o", exe, "-L", LIBDIR, "-lkevd",
+                      os.path.join(drivers, f), "-o", exe, "-L", LIBDIR, "-lkevd", "-lkevdh5",
                       "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/../lib"])
     if verbose:
         for l in logs:

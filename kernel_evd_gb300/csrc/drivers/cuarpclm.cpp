@@ -40,12 +40,12 @@ int main() {
     const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ, Nrounds = NROUNDS;
     const size_t N = Ndata - Nq + 1, NM = N * M, rmax = Nrounds * BLK;
     char fname[256], linv_file[256], spiv_file[256];
-    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.bin", Ndata, M, Lfact);
-    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
-    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
+    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.h5", Ndata, M, Lfact);
+    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
+    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
     printf("Data file: %s\nData set: u\n", fname);
     printf("Block size: %d  Devices: 1  Rows/device: %zu  Cols/device: %zu\n\n", BLK, NM, rmax);
-    std::vector<float> u = read_array<float>(fname, Ndata * M);
+    std::vector<float> u = h5_read<float>(fname, "/u", Ndata * M);
 
     kevd_ctx* ctx = nullptr;
     if (kevd_ctx_create(0, &ctx) != KEVD_OK) {
@@ -78,9 +78,9 @@ int main() {
     std::vector<double> linv(Nr * Nr);
     DRV_KEVD(ctx, kevd_linv_from_factor(ctx, F, PRECISION, (int64_t)rmax, spiv.data(), (int64_t)Nr, linv.data(),
                                         nullptr));
-    write_array(linv_file, linv.data(), linv.size());
+    h5_write_one(linv_file, "/linv", linv.data(), linv.size());
     std::vector<uint64_t> spiv_u(spiv.begin(), spiv.begin() + Nr);
-    write_array(spiv_file, spiv_u.data(), spiv_u.size());
+    h5_write_one(spiv_file, "/spiv", spiv_u.data(), spiv_u.size());
 
     printf("\nAccepted rank: %zu in %zu rounds\n", Nr, Nrounds);
     printf("# round accepted cumrank relerr\n");

@@ -25,9 +25,9 @@ int main() {
     const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ;
     const size_t N = Ndata - Nq + 1, NM = N * M;
     char fname[256];
-    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.bin", Ndata, M, Lfact);
+    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.h5", Ndata, M, Lfact);
     printf("Data file: %s\nData set: u\n", fname);
-    std::vector<float> u = read_array<float>(fname, Ndata * M);
+    std::vector<float> u = h5_read<float>(fname, "/u", Ndata * M);
 
     // the 36 candidate bandwidths: 1e-3 .. 9, nine per decade (float, as in the reference)
     std::vector<double> bw;

@@ -44,17 +44,21 @@ int main() {
     const time_t t0 = time(nullptr);
     const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ, Nrounds = NROUNDS, k_out = KOUT;
     const size_t N = Ndata - Nq + 1, NM = N * M;
-    char fname[256], linv_file[256], spiv_file[256], lam_file[256], u_file[256];
-    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.bin", Ndata, M, Lfact);
-    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
-    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.bin", N, M, BLK, Nrounds, Lfact);
-    snprintf(lam_file, sizeof(lam_file), "data/evd_%zu_%zu_%zu_%zu_%zu_lam.bin", N, M, Nq, k_out, Lfact);
-    snprintf(u_file, sizeof(u_file), "data/evd_%zu_%zu_%zu_%zu_%zu_U.bin", N, M, Nq, k_out, Lfact);
+    char fname[256], linv_file[256], spiv_file[256], out_file[256];
+    snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.h5", Ndata, M, Lfact);
+    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
+    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
+    snprintf(out_file, sizeof(out_file), "data/evd_%zu_%zu_%zu_%zu_%zu.h5", N, M, Nq, k_out, Lfact);
+    DRV_H5(kevd_h5_create(out_file));
     printf("Data file: %s\nData set: u\n", fname);
-    std::vector<float> u = read_array<float>(fname, Ndata * M);
-    const size_t Nr = array_length<uint64_t>(spiv_file);
-    std::vector<uint64_t> spiv_u = read_array<uint64_t>(spiv_file, Nr);
-    std::vector<double> linv = read_array<double>(linv_file, Nr * Nr);
+    std::vector<float> u = h5_read<float>(fname, "/u", Ndata * M);
+    const size_t Nr = h5_count(spiv_file, "/spiv");
+    if (h5_count(linv_file, "/linv") != Nr * Nr) {
+        fprintf(stderr, "%s: /linv is not %zu x %zu\n", linv_file, Nr, Nr);
+        return 1;
+    }
+    std::vector<uint64_t> spiv_u = h5_read<uint64_t>(spiv_file, "/spiv", Nr);
+    std::vector<double> linv = h5_read<double>(linv_file, "/linv", Nr * Nr);
     std::vector<int64_t> spiv(spiv_u.begin(), spiv_u.end());
     printf("Rank: %zu  k_out: %zu\n", Nr, k_out);
 
@@ -79,8 +83,8 @@ int main() {
                                         lam.data(), U_dev, &info, nullptr, nullptr));
     std::vector<float> U(NM * k_out);
     DRV_CUDA(cudaMemcpy(U.data(), U_dev, U.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    write_array(lam_file, lam.data(), lam.size());
-    write_array(u_file, U.data(), U.size());
+    h5_add(out_file, "/lam", lam.data(), lam.size());
+    h5_add(out_file, "/U", U.data(), U.size());
     printf("trace(A) = %.10e  shift = %.5e\n", info.trace_A, info.shift);
     printf("Leading eigenvalues:");
     for (size_t j = 0; j < (k_out < 8 ? k_out : 8); ++j) printf(" %.10f", lam[Nr - 1 - j]);

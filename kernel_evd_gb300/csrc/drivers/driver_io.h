@@ -1,7 +1,6 @@
-// Shared helpers of the three stage drivers: raw little-endian array files in
-// place of the reference's HDF5 datasets (libhdf5 is not available here), the
-// same path names with ".bin" for ".h5", and CUDA / library checks that exit
-// the way the reference programs do.
+// Shared helpers of the three stage drivers: the reference's HDF5 datasets read and
+// written through libkevdh5 (include/kevd_h5.h; libhdf5 is not needed), and CUDA /
+// library checks that exit the way the reference programs do.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,6 +11,7 @@
 #include <vector>
 
 #include "kevd.h"
+#include "kevd_h5.h"
 
 #define DRV_CUDA(x)                                                                       \
     do {                                                                                  \
@@ -32,42 +32,51 @@
         }                                                                                  \
     } while (0)
 
+// An HDF5 failure ends the program, as the reference's assert on every H5 call does.
+#define DRV_H5(x)                                                   \
+    do {                                                            \
+        if ((x) != KEVD_H5_OK) {                                    \
+            fprintf(stderr, "HDF5: %s\n", kevd_h5_last_error());   \
+            exit(1);                                                \
+        }                                                           \
+    } while (0)
+
 template <typename T>
-std::vector<T> read_array(const char* path, size_t count) {
+constexpr int32_t h5_type();
+template <>
+constexpr int32_t h5_type<float>() { return KEVD_H5_F32; }
+template <>
+constexpr int32_t h5_type<double>() { return KEVD_H5_F64; }
+template <>
+constexpr int32_t h5_type<uint64_t>() { return KEVD_H5_U64; }
+template <>
+constexpr int32_t h5_type<int64_t>() { return KEVD_H5_I64; }
+
+// `count` elements of dataset `dset`, converted to T (ks_bandwidth.cu:51-83 h5read,
+// ks_kevd.cu:134-243 h5read_float / h5read_double / h5read_sizet).
+template <typename T>
+std::vector<T> h5_read(const char* path, const char* dset, size_t count) {
     std::vector<T> v(count);
-    FILE* f = fopen(path, "rb");
-    if (!f) {
-        fprintf(stderr, "cannot open %s\n", path);
-        exit(1);
-    }
-    if (fread(v.data(), sizeof(T), count, f) != count) {
-        fprintf(stderr, "%s: expected %zu values\n", path, count);
-        exit(1);
-    }
-    fclose(f);
+    DRV_H5(kevd_h5_read(path, dset, h5_type<T>(), v.data(), (int64_t)count));
     return v;
 }
 
-// Number of T values in a file.
-template <typename T>
-size_t array_length(const char* path) {
-    FILE* f = fopen(path, "rb");
-    if (!f) {
-        fprintf(stderr, "cannot open %s\n", path);
-        exit(1);
-    }
-    fseek(f, 0, SEEK_END);
-    const long n = ftell(f);
-    fclose(f);
-    return (size_t)n / sizeof(T);
+// Number of elements of a dataset (ks_kevd.cu:113-132 h5_num_elements).
+inline size_t h5_count(const char* path, const char* dset) {
+    int64_t n = 0;
+    DRV_H5(kevd_h5_dataset_info(path, dset, &n, nullptr, nullptr, nullptr));
+    return (size_t)n;
 }
 
+// A new file holding one dataset (ks_arpclm.cu:121-172 h5write_sizet / h5write_double).
 template <typename T>
-void write_array(const char* path, const T* v, size_t count) {
-    FILE* f = fopen(path, "wb");
-    if (!f || fwrite(v, sizeof(T), count, f) != count) {
-        fprintf(stderr, "cannot write %s\n", path);
-        exit(1);
-    }
-    fclose(f);
+void h5_write_one(const char* path, const char* dset, const T* v, size_t count) {
+    DRV_H5(kevd_h5_create(path));
+    DRV_H5(kevd_h5_append(path, dset, h5_type<T>(), v, (int64_t)count));
+}
+
+// One more dataset in an existing file (ks_kevd.cu:247-290 h5add_double / h5add_float).
+template <typename T>
+void h5_add(const char* path, const char* dset, const T* v, size_t count) {
+    DRV_H5(kevd_h5_append(path, dset, h5_type<T>(), v, (int64_t)count));
 }

@@ -1,0 +1,141 @@
+"""ctypes binding of ``libkevdh5.so`` (include/kevd_h5.h): the HDF5 datasets the
+reference's programs exchange ("/u", "/linv", "/spiv", "/lam", "/U"), read and
+written without libhdf5.
+
+``read`` mirrors the reference's ``h5read_*`` helpers (ks_bandwidth.cu:51-83,
+ks_kevd.cu:134-243): the stored elements converted to the requested type.
+``write`` mirrors ``h5write_*`` (ks_arpclm.cu:121-172, one file, one-dimensional
+datasets), ``create`` + ``append`` the empty-file-then-``h5add_*`` pattern of
+ks_kevd.cu:247-290 and :492-503.  The library is built in-tree with the rest
+(``python -m kernel_evd_gb300.build``; ``build.build_h5()`` alone needs only gcc);
+there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.environ.get("KEVD_H5_LIB") or os.path.join(HERE, "lib", "libkevdh5.so")
+
+F32, F64, I32, U32, I64, U64 = 1, 2, 3, 4, 5, 6
+_TYPES = {np.dtype(np.float32): F32, np.dtype(np.float64): F64, np.dtype(np.int32): I32,
+          np.dtype(np.uint32): U32, np.dtype(np.int64): I64, np.dtype(np.uint64): U64}
+_DTYPES = {v: k for k, v in _TYPES.items()}
+
+STATUS = {0: "KEVD_H5_OK", 1: "KEVD_H5_ERR_ARG", 2: "KEVD_H5_ERR_IO", 3: "KEVD_H5_ERR_FORMAT",
+          4: "KEVD_H5_ERR_NOTFOUND", 5: "KEVD_H5_ERR_UNSUPPORTED"}
+
+SIGNATURES = {
+    "kevd_h5_last_error": (C.c_char_p, []),
+    "kevd_h5_dataset_info": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "kevd_h5_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "kevd_h5_list": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int64, C.POINTER(C.c_int32)]),
+    "kevd_h5_create": (C.c_int, [C.c_char_p]),
+    "kevd_h5_append": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "kevd_h5_write": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+}
+
+
+class H5Error(RuntimeError):
+    """A non-zero kevd_h5 status.  ``code`` is the enum value, ``name`` its name."""
+
+    def __init__(self, code: int, msg: str):
+        self.code = int(code)
+        self.name = STATUS.get(self.code, "KEVD_H5_ERR_UNKNOWN")
+        super().__init__(f"{self.name}: {msg}")
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise H5Error(2, f"{LIB_PATH} is not built (python -m kernel_evd_gb300.build)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != 0:
+        raise H5Error(status, lib().kevd_h5_last_error().decode(errors="replace"))
+
+
+def _b(s) -> bytes:
+    return os.fsencode(s)
+
+
+def info(path, name: str) -> dict:
+    """Element count, stored type (a numpy dtype), rank and shape of a dataset."""
+    n, t, r = C.c_int64(), C.c_int32(), C.c_int32()
+    dims = (C.c_int64 * 32)()
+    _check(lib().kevd_h5_dataset_info(_b(path), name.encode(), C.byref(n), C.byref(t), C.byref(r), dims))
+    return {"count": n.value, "dtype": _DTYPES[t.value], "rank": r.value,
+            "shape": tuple(dims[i] for i in range(r.value))}
+
+
+def read(path, name: str, dtype=None, count: int | None = None) -> np.ndarray:
+    """All elements of a dataset, flat, as ``dtype`` (default: the stored type).  With
+    ``count`` given, a dataset of another size is an error (the reference's assert)."""
+    meta = info(path, name)
+    dt = np.dtype(dtype) if dtype is not None else meta["dtype"]
+    if dt not in _TYPES:
+        raise H5Error(1, f"unsupported element type {dt}")
+    n = meta["count"] if count is None else int(count)
+    out = np.empty(n, dtype=dt)
+    _check(lib().kevd_h5_read(_b(path), name.encode(), _TYPES[dt], out.ctypes.data, n))
+    return out
+
+
+def names(path) -> list[str]:
+    """Names in the root group."""
+    cap = 1 << 16
+    while True:
+        buf = C.create_string_buffer(cap)
+        n = C.c_int32()
+        st = lib().kevd_h5_list(_b(path), buf, cap, C.byref(n))
+        if st == 1 and cap < (1 << 26):
+            cap *= 16
+            continue
+        _check(st)
+        return [s.decode() for s in buf.raw.split(b"\0")[: n.value]]
+
+
+def _flat(a) -> np.ndarray:
+    a = np.ascontiguousarray(a).ravel()
+    if a.dtype not in _TYPES:
+        raise H5Error(1, f"unsupported element type {a.dtype}")
+    return a
+
+
+def create(path) -> None:
+    """An empty HDF5 file (truncates)."""
+    _check(lib().kevd_h5_create(_b(path)))
+
+
+def append(path, name: str, a) -> None:
+    """Adds ``a`` (flattened, C order) as the one-dimensional dataset ``name``."""
+    a = _flat(a)
+    _check(lib().kevd_h5_append(_b(path), name.encode(), _TYPES[a.dtype], a.ctypes.data, a.size))
+
+
+def write(path, datasets: dict) -> None:
+    """A new file holding ``{name: array}`` as one-dimensional datasets."""
+    arrs = [(k, _flat(v)) for k, v in datasets.items()]
+    n = len(arrs)
+    nm = (C.c_char_p * max(n, 1))(*[k.encode() for k, _ in arrs])
+    ty = (C.c_int32 * max(n, 1))(*[_TYPES[a.dtype] for _, a in arrs])
+    da = (C.c_void_p * max(n, 1))(*[a.ctypes.data for _, a in arrs])
+    ct = (C.c_int64 * max(n, 1))(*[a.size for _, a in arrs])
+    _check(lib().kevd_h5_write(_b(path), n, nm, ty, da, ct))

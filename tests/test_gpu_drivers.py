@@ -1,10 +1,10 @@
 """The three stage drivers (cuband, cuarpclm, cukevd) run as the reference's
-programs do: no arguments, compile-time configuration, files under ./data (raw
-arrays in place of HDF5 datasets), bw0.out and the round table on stdout.  The
-built drivers (kernel_evd_gb300/bin) carry the reference's own constants; these
-tests compile test-sized copies of the same sources with -D overrides, as a
-user of the reference edits its constants, and check their outputs against the
-FP64 oracle."""
+programs do: no arguments, compile-time configuration, HDF5 files under ./data
+with the reference's names and datasets (/u, /linv, /spiv, /lam, /U), bw0.out
+and the round table on stdout.  The built drivers (kernel_evd_gb300/bin) carry
+the reference's own constants; these tests compile test-sized copies of the
+same sources with -D overrides, as a user of the reference edits its constants,
+and check their outputs against the FP64 oracle."""
 import os
 import shutil
 import subprocess
@@ -12,6 +12,7 @@ import subprocess
 import numpy as np
 import pytest
 
+from kernel_evd_gb300 import h5
 from oracle import calibrate, evd, kernel, ks, rpchol
 
 pytestmark = pytest.mark.gpu
@@ -32,11 +33,14 @@ def bindir(tmp_path_factory):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(os.path.join(LIBDIR, "libkevd.so")) or not os.path.exists(nvcc):
         pytest.skip("libkevd.so or nvcc missing")
+    if not os.path.exists(os.path.join(LIBDIR, "libkevdh5.so")):
+        from kernel_evd_gb300 import build
+        build.build_h5()
     out = tmp_path_factory.mktemp("drivers")
     for prog, defs in DEFS.items():
         cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17",
                "-I", os.path.join(ROOT, "include"), *[f"-D{k}={v}" for k, v in defs.items()],
-               os.path.join(SRC, prog + ".cpp"), "-o", str(out / prog), "-L", LIBDIR, "-lkevd",
+               os.path.join(SRC, prog + ".cpp"), "-o", str(out / prog), "-L", LIBDIR, "-lkevd", "-lkevdh5",
                "-Xlinker", "-rpath", "-Xlinker", LIBDIR]
         r = subprocess.run(cmd, capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
@@ -46,7 +50,7 @@ def bindir(tmp_path_factory):
 def _write_u(d, ndata):
     S = ks.seeded_mode(ndata, M=64, seed=3, warm_time=60.0)       # ndata times x 64 gridpoints
     u = np.ascontiguousarray(S[:, :M].T).astype(np.float32)         # M gridpoints, time fastest
-    u.ravel().tofile(os.path.join(d, "data", f"ks_true_{ndata}_{M}_{LFACT}_u32.bin"))
+    h5.write(os.path.join(d, "data", f"ks_true_{ndata}_{M}_{LFACT}_u32.h5"), {"u": u.ravel()})
     return u.ravel()
 
 
@@ -82,8 +86,9 @@ def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     out = _run(bindir, d, "cuarpclm")
     assert "# round accepted cumrank relerr" in out
     N = ndata - NQ + 1
-    spiv = np.fromfile(os.path.join(d, "data", f"spiv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.bin"), dtype=np.uint64)
-    linv = np.fromfile(os.path.join(d, "data", f"linv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.bin"), dtype=np.float64)
+    spiv = h5.read(os.path.join(d, "data", f"spiv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.h5"), "/spiv")
+    linv = h5.read(os.path.join(d, "data", f"linv_{N}_{M}_b{BLK}_r{NROUNDS}_{LFACT}.h5"), "/linv")
+    assert spiv.dtype == np.uint64 and linv.dtype == np.float64
     X = kernel.hankel_rows(u, ndata, M, NQ).astype(np.float64)
     scale = 1.0 / (NQ * BW)
     ref = rpchol.rpcholesky(X, scale, BLK * NROUNDS, BLK, seed=1234, n_rounds=NROUNDS)
@@ -92,8 +97,11 @@ def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     Li = rpchol.linv_from_F(ref["F"], ref["piv"])
     np.testing.assert_allclose(linv.reshape(r, r, order="F"), Li, rtol=0, atol=1e-8 * np.abs(Li).max())
     out = _run(bindir, d, "cukevd")
-    lam = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_lam.bin"), dtype=np.float64)
-    U = np.fromfile(os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}_U.bin"), dtype=np.float32)
+    out_file = os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}.h5")
+    assert h5.names(out_file) == ["U", "lam"]
+    lam = h5.read(out_file, "/lam")
+    U = h5.read(out_file, "/U")
+    assert lam.dtype == np.float64 and U.dtype == np.float32
     e = evd.evd_from_factor(ref["F"], 16)
     np.testing.assert_allclose(lam[-16:], e["lam"][-16:], rtol=0, atol=1e-9)
     assert U.size == X.shape[0] * 16
