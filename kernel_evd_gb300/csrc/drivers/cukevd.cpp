@@ -7,7 +7,9 @@
 // bw = 0.8, k_out = 256), reading the stage-2 files of the cuarpclm defaults
 // (BLK = 512, 8 rounds); the factor is formed and decomposed in the mixed form
 // (FP32 factor: at rank 4,096 it and its column-major copy take 138 GB);
-// override with -D.
+// override with -D.  -DDUMP_H5=1 also writes the reference's optional dump file
+// (ks_kevd.cu:483-484, :533-542) with its intermediates in its own basis.
+#include <cmath>
 #include <ctime>
 
 #include "driver_io.h"
@@ -39,6 +41,96 @@
 #ifndef PRECISION
 #define PRECISION KEVD_MIXED
 #endif
+#ifndef DUMP_H5
+#define DUMP_H5 0
+#endif
+
+// The reference's dump points (c1, p1, dtil, cq, pq, Atil, A, R, G, qtil, Btil, W,
+// lam, Z, U in the order of ks_kevd.cu:809-2311) from the library's, which live in
+// the basis of the stored factor F = K(:,S) L^{-T} (L^{-1} = linv, lower, r x r
+// column-major): the reference's c1 = K(:,S)^T 1 = L c1_F, p1 = L^{-T} L^{-1} c1 =
+// linv^T c1_F, likewise cq / pq; Atil = L A L^T and Btil = L B L^T; R = chol(A + sI)
+// (upper); G = R L^{-1}; Z = L^{-T} Z_F.  The products with L are forward
+// substitutions with linv; the host work is O(r^3), as the reference's own dump
+// gathers r x r matrices to one rank.  V (the eigenvectors of W) is not kept by the
+// library and is not dumped.
+static void fwd_solve(const std::vector<double>& li, size_t r, double* x, size_t stride) {
+    for (size_t i = 0; i < r; ++i) {
+        double v = x[i * stride];
+        for (size_t j = 0; j < i; ++j) v -= li[i + j * r] * x[j * stride];
+        x[i * stride] = v / li[i + i * r];
+    }
+}
+
+static std::vector<double> linv_t_times(const std::vector<double>& li, size_t r, const double* x) {
+    std::vector<double> y(r, 0.0);
+    for (size_t j = 0; j < r; ++j) {
+        double v = 0.0;
+        for (size_t i = j; i < r; ++i) v += li[i + j * r] * x[i];
+        y[j] = v;
+    }
+    return y;
+}
+
+// L M L^T for a symmetric M (column-major): row-wise then column-wise substitution.
+static std::vector<double> l_sym_lt(const std::vector<double>& li, size_t r, const std::vector<double>& m) {
+    std::vector<double> x(m);
+    for (size_t c = 0; c < r; ++c) fwd_solve(li, r, x.data() + c * r, 1);   // X = L M
+    for (size_t i = 0; i < r; ++i) fwd_solve(li, r, x.data() + i, r);       // rows of X: X L^T
+    return x;
+}
+
+static void write_dump(const char* path, size_t r, size_t nm, size_t k_out, const std::vector<double>& li,
+                       const kevd_evd_dump& d, double shift, const std::vector<double>& lam,
+                       const std::vector<float>& U) {
+    DRV_H5(kevd_h5_create(path));
+    std::vector<double> c1(d.c1, d.c1 + r), cq(d.cq, d.cq + r);
+    const std::vector<double> p1 = linv_t_times(li, r, d.c1), pq = linv_t_times(li, r, d.cq);
+    fwd_solve(li, r, c1.data(), 1);
+    fwd_solve(li, r, cq.data(), 1);
+    const std::vector<double> A(d.A, d.A + r * r), B(d.B, d.B + r * r);
+    std::vector<double> R(r * r, 0.0), G(r * r, 0.0), Z(r * k_out, 0.0);
+    for (size_t j = 0; j < r; ++j) {                        // A + sI = R^T R, R upper
+        double v = A[j + j * r] + shift;
+        for (size_t k = 0; k < j; ++k) v -= R[k + j * r] * R[k + j * r];
+        if (!(v > 0.0)) {
+            fprintf(stderr, "dump: A + sI is not positive definite at %zu\n", j);
+            exit(1);
+        }
+        const double rjj = std::sqrt(v);
+        R[j + j * r] = rjj;
+        for (size_t i = j + 1; i < r; ++i) {
+            double w = A[j + i * r];
+            for (size_t k = 0; k < j; ++k) w -= R[k + j * r] * R[k + i * r];
+            R[j + i * r] = w / rjj;
+        }
+    }
+    for (size_t j = 0; j < r; ++j)                          // G = R L^{-1}
+        for (size_t i = 0; i < r; ++i) {
+            double v = 0.0;
+            for (size_t k = (i > j ? i : j); k < r; ++k) v += R[i + k * r] * li[k + j * r];
+            G[i + j * r] = v;
+        }
+    for (size_t c = 0; c < k_out; ++c) {                    // Z = L^{-T} Z_F
+        const std::vector<double> z = linv_t_times(li, r, d.Z + c * r);
+        for (size_t i = 0; i < r; ++i) Z[i + c * r] = z[i];
+    }
+    h5_add(path, "c1", c1.data(), r);
+    h5_add(path, "p1", p1.data(), r);
+    h5_add(path, "dtil", d.dtil, nm);
+    h5_add(path, "cq", cq.data(), r);
+    h5_add(path, "pq", pq.data(), r);
+    h5_add(path, "Atil", l_sym_lt(li, r, A).data(), r * r);
+    h5_add(path, "A", A.data(), r * r);
+    h5_add(path, "R", R.data(), r * r);
+    h5_add(path, "G", G.data(), r * r);
+    h5_add(path, "qtil", d.qtil, nm);
+    h5_add(path, "Btil", l_sym_lt(li, r, B).data(), r * r);
+    h5_add(path, "W", d.W, r * r);
+    h5_add(path, "lam", lam.data(), r);
+    h5_add(path, "Z", Z.data(), r * k_out);
+    h5_add(path, "U", U.data(), nm * k_out);
+}
 
 int main() {
     const time_t t0 = time(nullptr);
@@ -79,12 +171,32 @@ int main() {
                                         (int64_t)Nr, linv.data(), PRECISION, F, (int64_t)Nr, nullptr));
     std::vector<double> lam(Nr);
     kevd_evd_info info = {};
+    kevd_evd_dump dump = {};
+    std::vector<double> d_c1, d_dtil, d_cq, d_qtil, d_A, d_B, d_W, d_Z;
+    if (DUMP_H5) {
+        d_c1.resize(Nr);
+        d_dtil.resize(NM);
+        d_cq.resize(Nr);
+        d_qtil.resize(NM);
+        d_A.resize(Nr * Nr);
+        d_B.resize(Nr * Nr);
+        d_W.resize(Nr * Nr);
+        d_Z.resize(Nr * k_out);
+        dump = {d_c1.data(), d_dtil.data(), d_cq.data(), d_qtil.data(), d_A.data(), d_B.data(), d_W.data(),
+                d_Z.data()};
+    }
     DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, PRECISION, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
-                                        lam.data(), U_dev, &info, nullptr, nullptr));
+                                        lam.data(), U_dev, &info, DUMP_H5 ? &dump : nullptr, nullptr));
     std::vector<float> U(NM * k_out);
     DRV_CUDA(cudaMemcpy(U.data(), U_dev, U.size() * sizeof(float), cudaMemcpyDeviceToHost));
     h5_add(out_file, "/lam", lam.data(), lam.size());
     h5_add(out_file, "/U", U.data(), U.size());
+    if (DUMP_H5) {
+        char dump_file[256];
+        snprintf(dump_file, sizeof(dump_file), "data/kevd_dump_%zu_%zu_%zu.h5", N, M, Lfact);
+        write_dump(dump_file, Nr, NM, k_out, linv, dump, info.shift, lam, U);
+        printf("Dump: %s\n", dump_file);
+    }
     printf("trace(A) = %.10e  shift = %.5e\n", info.trace_A, info.shift);
     printf("Leading eigenvalues:");
     for (size_t j = 0; j < (k_out < 8 ? k_out : 8); ++j) printf(" %.10f", lam[Nr - 1 - j]);

@@ -25,7 +25,12 @@ DEFS = {"cuband": dict(LFACT=LFACT, MGRID=M, NDATA=600, NQ=NQ),
         "cuarpclm": dict(LFACT=LFACT, MGRID=M, NDATA=2000, NQ=NQ, BLK=BLK, NROUNDS=NROUNDS, BW=BW,
                          PRECISION="KEVD_FP64"),
         "cukevd": dict(LFACT=LFACT, MGRID=M, NDATA=2000, NQ=NQ, BLK=BLK, NROUNDS=NROUNDS, BW=BW, KOUT=16,
-                       PRECISION="KEVD_FP64")}
+                       PRECISION="KEVD_FP64", DUMP_H5=1)}
+# Relative (to the largest magnitude) agreement of the dump points with the
+# reference's own algebra on the same L^{-1} and pivots: R and G carry the
+# conditioning of chol(A + sI), p1 / pq and Z that of L^{-1}.
+DUMP_TOL = dict(c1=1e-11, dtil=1e-11, cq=1e-11, qtil=1e-11, A=1e-10, Atil=1e-10, Btil=1e-10, W=1e-10,
+                lam=1e-10, p1=1e-8, pq=1e-8, R=1e-7, G=1e-6)
 
 
 @pytest.fixture(scope="module")
@@ -105,3 +110,16 @@ def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     e = evd.evd_from_factor(ref["F"], 16)
     np.testing.assert_allclose(lam[-16:], e["lam"][-16:], rtol=0, atol=1e-9)
     assert U.size == X.shape[0] * 16
+    # the optional dump file (ks_kevd.cu:533-542) against the reference's pass algebra
+    dump = os.path.join(d, "data", f"kevd_dump_{N}_{M}_{LFACT}.h5")
+    assert h5.names(dump) == sorted(list(DUMP_TOL) + ["Z", "U"])
+    g = evd.evd_from_linv(X, scale, linv.reshape(r, r, order="F"), spiv.astype(np.int64), 16)
+    for k, tol in DUMP_TOL.items():
+        got, want = h5.read(dump, k), g[k].ravel(order="F")
+        assert got.dtype == np.float64 and got.size == want.size, k
+        assert np.max(np.abs(got - want)) <= tol * np.max(np.abs(want)), k
+    Z = evd.align_signs(h5.read(dump, "Z").reshape(r, 16, order="F"), g["Z"])
+    assert np.max(np.abs(Z - g["Z"])) <= 1e-8 * np.max(np.abs(g["Z"]))
+    np.testing.assert_array_equal(h5.read(dump, "U"), U)
+    Ug = evd.align_signs(U.reshape(-1, 16).astype(np.float64), g["U"])
+    assert np.max(np.abs(Ug - g["U"])) <= 1e-5 * np.max(np.abs(g["U"]))
