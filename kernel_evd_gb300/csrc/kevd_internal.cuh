@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
 #include <cusolverDn.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <cstdio>
@@ -115,16 +116,20 @@ int set_error(kevd_ctx* ctx, int code, const char* fmt, ...);
         if (st_ != KEVD_OK) return st_; \
     } while (0)
 
-// Times the kernels launched on stream s during its lifetime under name.
+// Times the kernels launched on stream s during its lifetime under name, and
+// marks the same span as an NVTX range (for ncu --nvtx filters; a no-op when
+// no tool is attached).
 class ProfScope {
   public:
     ProfScope(kevd_ctx* ctx, const char* name, cudaStream_t s) : ctx_(ctx), name_(name), s_(s) {
+        nvtxRangePushA(name);
         if (ctx_->prof) {
             a_ = take();
             if (a_) cudaEventRecord(a_, s_);
         }
     }
     ~ProfScope() {
+        nvtxRangePop();
         if (!a_) return;
         cudaEvent_t b = take();
         if (!b) return;
