@@ -1,10 +1,12 @@
 // Stage 1 driver (the reference's ./cuband, ks_bandwidth.cu:339-667): delay
 // embedding of u, pair sums over the 36-bandwidth sweep, selection, bw0.out.
 // Compile-time configuration as in the reference (ks_bandwidth.cu:359-365:
-// L = 30 pi, 128 gridpoints, 4,607 snapshots, Nq = 512); override with -D.
+// L = 30 pi, 128 gridpoints, 4,607 snapshots, Nq = 512); override with -D, or at
+// run time with the flags of driver_args.h (none given: the reference's run).
 #include <cmath>
 #include <ctime>
 
+#include "driver_args.h"
 #include "driver_io.h"
 
 #ifndef LFACT
@@ -20,12 +22,26 @@
 #define NQ 512
 #endif
 
-int main() {
+int main(int argc, char** argv) {
     const time_t t0 = time(nullptr);
-    const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ;
+    DriverConfig cfg("cuband", {{"lfact", LFACT, DriverSetting::kInt, "domain length factor in the file name"},
+                                {"mgrid", MGRID, DriverSetting::kInt, "gridpoints per snapshot"},
+                                {"ndata", NDATA, DriverSetting::kInt, "snapshots"},
+                                {"nq", NQ, DriverSetting::kInt, "delay window"}});
+    cfg.parse(argc, argv);
+    const size_t Lfact = cfg.size("lfact"), M = cfg.size("mgrid"), Ndata = cfg.size("ndata"), Nq = cfg.size("nq");
+    if (Nq < 1 || Nq > Ndata || M < 1) {
+        fprintf(stderr, "cuband: need 1 <= nq <= ndata and mgrid >= 1\n");
+        return 2;
+    }
     const size_t N = Ndata - Nq + 1, NM = N * M;
     char fname[256];
     snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.h5", Ndata, M, Lfact);
+    if (cfg.print_only) {
+        cfg.print(stdout);
+        printf("input = %s:/u\noutput = bw0.out\n", fname);
+        return 0;
+    }
     printf("Data file: %s\nData set: u\n", fname);
     std::vector<float> u = h5_read<float>(fname, "/u", Ndata * M);
 

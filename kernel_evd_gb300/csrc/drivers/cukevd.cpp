@@ -7,11 +7,14 @@
 // bw = 0.8, k_out = 256), reading the stage-2 files of the cuarpclm defaults
 // (BLK = 512, 8 rounds); the factor is formed and decomposed in the mixed form
 // (FP32 factor: at rank 4,096 it and its column-major copy take 138 GB);
-// override with -D.  -DDUMP_H5=1 also writes the reference's optional dump file
-// (ks_kevd.cu:483-484, :533-542) with its intermediates in its own basis.
+// override with -D, or at run time with the flags of driver_args.h (none given:
+// the configuration above).  -DDUMP_H5=1 (--dump 1) also writes the reference's
+// optional dump file (ks_kevd.cu:483-484, :533-542) with its intermediates in its
+// own basis.
 #include <cmath>
 #include <ctime>
 
+#include "driver_args.h"
 #include "driver_io.h"
 
 #ifndef LFACT
@@ -132,15 +135,44 @@ static void write_dump(const char* path, size_t r, size_t nm, size_t k_out, cons
     h5_add(path, "U", U.data(), nm * k_out);
 }
 
-int main() {
+int main(int argc, char** argv) {
     const time_t t0 = time(nullptr);
-    const size_t Lfact = LFACT, M = MGRID, Ndata = NDATA, Nq = NQ, Nrounds = NROUNDS, k_out = KOUT;
+    DriverConfig cfg("cukevd", {{"lfact", LFACT, DriverSetting::kInt, "domain length factor in the file names"},
+                                {"mgrid", MGRID, DriverSetting::kInt, "gridpoints per snapshot"},
+                                {"ndata", NDATA, DriverSetting::kInt, "snapshots"},
+                                {"nq", NQ, DriverSetting::kInt, "delay window"},
+                                {"blk", BLK, DriverSetting::kInt, "stage-2 block size (in the file names)"},
+                                {"nrounds", NROUNDS, DriverSetting::kInt, "stage-2 rounds (in the file names)"},
+                                {"bw", BW, DriverSetting::kReal, "bandwidth (scale 1 / (nq bw))"},
+                                {"kout", KOUT, DriverSetting::kInt, "eigenvectors written to /U (1..256)"},
+                                {"precision", PRECISION == KEVD_FP64 ? 0 : 1, DriverSetting::kPrecision,
+                                 "fp64 or mixed (FP32 factor)"},
+                                {"dump", DUMP_H5, DriverSetting::kFlag, "1: also write the dump file"}});
+    cfg.parse(argc, argv);
+    const size_t Lfact = cfg.size("lfact"), M = cfg.size("mgrid"), Ndata = cfg.size("ndata"), Nq = cfg.size("nq"),
+                 Nrounds = cfg.size("nrounds"), k_out = cfg.size("kout");
+    const int blk = cfg.integer("blk");
+    const double bw = cfg.get("bw");
+    const int32_t precision = cfg.get("precision") == 0 ? KEVD_FP64 : KEVD_MIXED;
+    const bool dump_h5 = cfg.get("dump") != 0;
+    if (Nq < 1 || Nq > Ndata || M < 1 || k_out < 1 || !(bw > 0)) {
+        fprintf(stderr, "cukevd: need 1 <= nq <= ndata, mgrid, kout >= 1 and bw > 0\n");
+        return 2;
+    }
     const size_t N = Ndata - Nq + 1, NM = N * M;
-    char fname[256], linv_file[256], spiv_file[256], out_file[256];
+    char fname[256], linv_file[256], spiv_file[256], out_file[256], dump_file[256];
     snprintf(fname, sizeof(fname), "data/ks_true_%zu_%zu_%zu_u32.h5", Ndata, M, Lfact);
-    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
-    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, BLK, Nrounds, Lfact);
+    snprintf(linv_file, sizeof(linv_file), "data/linv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, blk, Nrounds, Lfact);
+    snprintf(spiv_file, sizeof(spiv_file), "data/spiv_%zu_%zu_b%d_r%zu_%zu.h5", N, M, blk, Nrounds, Lfact);
     snprintf(out_file, sizeof(out_file), "data/evd_%zu_%zu_%zu_%zu_%zu.h5", N, M, Nq, k_out, Lfact);
+    snprintf(dump_file, sizeof(dump_file), "data/kevd_dump_%zu_%zu_%zu.h5", N, M, Lfact);
+    if (cfg.print_only) {
+        cfg.print(stdout);
+        printf("input = %s:/u\ninput = %s:/linv\ninput = %s:/spiv\noutput = %s:/lam,/U\n", fname, linv_file,
+               spiv_file, out_file);
+        if (dump_h5) printf("output = %s\n", dump_file);
+        return 0;
+    }
     DRV_H5(kevd_h5_create(out_file));
     printf("Data file: %s\nData set: u\n", fname);
     std::vector<float> u = h5_read<float>(fname, "/u", Ndata * M);
@@ -163,17 +195,17 @@ int main() {
     double* F = nullptr;
     DRV_CUDA(cudaMalloc(&u_dev, u.size() * sizeof(float)));
     DRV_CUDA(cudaMalloc(&X_dev, NM * Nq * sizeof(float)));
-    DRV_CUDA(cudaMalloc(&F, NM * Nr * (PRECISION == KEVD_FP64 ? sizeof(double) : sizeof(float))));
+    DRV_CUDA(cudaMalloc(&F, NM * Nr * (precision == KEVD_FP64 ? sizeof(double) : sizeof(float))));
     DRV_CUDA(cudaMalloc(&U_dev, NM * k_out * sizeof(float)));
     DRV_CUDA(cudaMemcpy(u_dev, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice));
     DRV_KEVD(ctx, kevd_hankel_rows(ctx, u_dev, (int64_t)Ndata, (int64_t)M, (int64_t)Nq, X_dev, nullptr));
-    DRV_KEVD(ctx, kevd_factor_from_linv(ctx, X_dev, (int64_t)NM, (int32_t)Nq, 1.0 / ((double)Nq * BW), spiv.data(),
-                                        (int64_t)Nr, linv.data(), PRECISION, F, (int64_t)Nr, nullptr));
+    DRV_KEVD(ctx, kevd_factor_from_linv(ctx, X_dev, (int64_t)NM, (int32_t)Nq, 1.0 / ((double)Nq * bw), spiv.data(),
+                                        (int64_t)Nr, linv.data(), precision, F, (int64_t)Nr, nullptr));
     std::vector<double> lam(Nr);
     kevd_evd_info info = {};
     kevd_evd_dump dump = {};
     std::vector<double> d_c1, d_dtil, d_cq, d_qtil, d_A, d_B, d_W, d_Z;
-    if (DUMP_H5) {
+    if (dump_h5) {
         d_c1.resize(Nr);
         d_dtil.resize(NM);
         d_cq.resize(Nr);
@@ -185,15 +217,13 @@ int main() {
         dump = {d_c1.data(), d_dtil.data(), d_cq.data(), d_qtil.data(), d_A.data(), d_B.data(), d_W.data(),
                 d_Z.data()};
     }
-    DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, PRECISION, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
-                                        lam.data(), U_dev, &info, DUMP_H5 ? &dump : nullptr, nullptr));
+    DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, precision, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
+                                        lam.data(), U_dev, &info, dump_h5 ? &dump : nullptr, nullptr));
     std::vector<float> U(NM * k_out);
     DRV_CUDA(cudaMemcpy(U.data(), U_dev, U.size() * sizeof(float), cudaMemcpyDeviceToHost));
     h5_add(out_file, "/lam", lam.data(), lam.size());
     h5_add(out_file, "/U", U.data(), U.size());
-    if (DUMP_H5) {
-        char dump_file[256];
-        snprintf(dump_file, sizeof(dump_file), "data/kevd_dump_%zu_%zu_%zu.h5", N, M, Lfact);
+    if (dump_h5) {
         write_dump(dump_file, Nr, NM, k_out, linv, dump, info.shift, lam, U);
         printf("Dump: %s\n", dump_file);
     }

@@ -83,6 +83,27 @@ def test_cuband_selects_the_oracle_bandwidth(bindir, tmp_path):
     np.testing.assert_allclose(got[:, 1], logS[1:-1], rtol=1e-4, atol=1e-6)
 
 
+def test_run_time_flags_match_the_compiled_constants(bindir, tmp_path):
+    """The in-tree cuband (the reference's constants) given the test constants as
+    flags writes the same bw0.out, byte for byte, as the copy compiled with them."""
+    exe = os.path.join(ROOT, "kernel_evd_gb300", "bin", "cuband")
+    if not os.path.exists(exe):
+        pytest.skip("in-tree drivers not built")
+    runs = []
+    for how in ("compiled", "flags"):
+        d = str(tmp_path / how)
+        os.makedirs(os.path.join(d, "data"))
+        _write_u(d, 600)
+        if how == "compiled":
+            _run(bindir, d, "cuband")
+        else:
+            flags = [f"--{k.lower()}={v}" for k, v in DEFS["cuband"].items()]
+            r = subprocess.run([exe, *flags], cwd=d, capture_output=True, text=True, timeout=600)
+            assert r.returncode == 0, r.stdout + r.stderr
+        runs.append(open(os.path.join(d, "bw0.out")).read())
+    assert runs[0] == runs[1]
+
+
 def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     d = str(tmp_path)
     os.makedirs(os.path.join(d, "data"))
