@@ -659,11 +659,10 @@ def main():
     Xd = Xh.cuda()
     eps, med, n_cal = calibrate_eps(ctx, Xd, N)
     scale = 1.0 / eps
-    # block size: the autotuner times b in {16, 32, 64} on this data (a 131,072-row
-    # prefix to rank 512); --b 0 runs the step with its choice
+    # block size: the autotuner times b in {16, 32, 64, 128, 256} on this data (a
+    # 131,072-row prefix to rank 512); --b 0 runs the step with its choice
     from kernel_evd_gb300 import autotune
-    tuned = None if args.no_autotune else autotune.tune_block(ctx, Xd, scale, args.k,
-                                                                candidates=(16, 32, 64, 128, 256))
+    tuned = None if args.no_autotune else autotune.tune_block(ctx, Xd, scale, args.k)
     if args.b == 0:
         args.b = int(tuned["block"]) if tuned else 64
     F = torch.empty((N, args.k), dtype=torch.float32, device="cuda")

@@ -72,7 +72,7 @@ def block_key(N: int, d: int, k: int) -> str:
     return f"rpchol/d{d}/n{int(math.log2(max(N, 2)))}/k{(k + 255) // 256}"
 
 
-def tune_block(ctx: api.Context, X: torch.Tensor, scale: float, k: int, candidates=(16, 32, 64),
+def tune_block(ctx: api.Context, X: torch.Tensor, scale: float, k: int, candidates=(16, 32, 64, 128, 256),
                probe_rows: int = 131072, probe_k: int = 512) -> dict:
     """Block size b for a mixed-precision factorisation of X to rank k: each
     candidate factorises the first ``probe_rows`` rows to rank
