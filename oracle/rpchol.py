@@ -130,6 +130,58 @@ def rpcholesky(X, scale: float, k_max: int, b: int, tol: float = 1e-10, seed: in
                 hm=np.array(hm, dtype=np.int64), proposals=props, accpos=accs, d=d)
 
 
+def rpcholesky_linv(X, scale: float, k_max: int, b: int, tol: float = 1e-10, seed: int = 1234,
+                    n_rounds: int | None = None, draw=None, rblk: int = 4096):
+    """The reference's own round algebra, which never stores F (``ks_arpclm.cu:800-1040``),
+    in FP64: ``L^{-1}`` (r x r) and the residual diagonal ``d`` are the whole state.
+
+    * ``P = L^{-1} K(S, S')``, ``H = K(S', S') - P^T P`` (``:807-874``);
+    * accept/reject and ``L_i^{-1}`` as in ``reject_and_factor`` (``:877-880``);
+    * ``M = L^{-T} L^{-1} K(S, S_i) = L^{-T} P[:, accpos]`` (``:895-927``);
+    * per row block R (``rblk`` rows): ``T = K(R, S_i) - K(R, S) M``, ``G = T L_i^{-T}``,
+      ``d(R) = max(d(R) - rowsq(G), 0)`` (``:933-995``, ``:459-478``);
+    * ``L^{-1}`` grows by the block row ``[-L_i^{-1} M^T | L_i^{-1}]`` (``:489-534``,
+      ``:998-1015``).
+
+    Same draws as ``rpcholesky``; returns dict(piv, err, hm, Linv, d)."""
+    X = np.asarray(X)
+    N = X.shape[0]
+    if draw is None:
+        def draw(rnd, stream, n):
+            return philox.uniforms(seed, rnd, stream, n)
+    if n_rounds is None:
+        n_rounds = 1 << 30
+    Linv = np.zeros((k_max, k_max))
+    d = np.ones(N)
+    piv = np.zeros(0, dtype=np.int64)
+    err, hm = [], []
+    rnd = 0
+    while rnd < n_rounds and piv.size < k_max:
+        r = piv.size
+        Sp = propose(d, draw(rnd, 0, b))
+        ua = draw(rnd, 1, b)
+        P = Linv[:r, :r] @ kblock(X, piv, Sp, scale)
+        H = kblock(X, Sp, Sp, scale) - P.T @ P
+        accpos, _, Minv = reject_and_factor(H, ua, tol, k_max - r)
+        nacc = accpos.size
+        if nacc > 0:
+            Si = Sp[accpos]
+            M = Linv[:r, :r].T @ P[:, accpos]
+            for i0 in range(0, N, rblk):
+                rows = np.arange(i0, min(N, i0 + rblk))
+                T = kblock(X, rows, Si, scale) - kblock(X, rows, piv, scale) @ M
+                G = T @ Minv.T
+                d[rows] = np.maximum(d[rows] - np.einsum("ij,ij->i", G, G), 0.0)
+            Linv[r:r + nacc, :r] = -Minv @ M.T
+            Linv[r:r + nacc, r:r + nacc] = np.tril(Minv)
+            piv = np.concatenate([piv, Si])
+        err.append(d.sum() / N)
+        hm.append(nacc)
+        rnd += 1
+    r = piv.size
+    return dict(piv=piv, err=np.array(err), hm=np.array(hm, dtype=np.int64), Linv=Linv[:r, :r], d=d)
+
+
 def linv_from_F(F: np.ndarray, piv: np.ndarray) -> np.ndarray:
     """L^{-1} with L = F(S, :) lower triangular (the reference's /linv, r x r)."""
     import scipy.linalg as sla

@@ -64,6 +64,24 @@ def test_lm_form_matches_factor_form(golden, b):
     np.testing.assert_allclose(np.abs(e2["U"]), np.abs(e1["U"]), rtol=0, atol=1e-11)
 
 
+@pytest.mark.parametrize("b", [1, 16, 64])
+def test_reference_round_algebra_matches_stored_factor(b):
+    """The reference's low-memory rounds (L^{-1} and d only, K(R, S) regenerated per row
+    block) and the stored-factor rounds make the same decisions on the same draws: the
+    same pivots and accept counts, trace errors to 1e-13, and L^{-1} equal to the one
+    recovered from F (measured: 3e-15 and 5e-14)."""
+    X = ks.seeded_mode(1500, warm_time=50.0)
+    sc = 1.0 / 30.0
+    f = rpchol.rpcholesky(X, sc, 160, b, seed=11)
+    g = rpchol.rpcholesky_linv(X, sc, 160, b, seed=11, rblk=512)
+    np.testing.assert_array_equal(g["piv"], f["piv"])
+    np.testing.assert_array_equal(g["hm"], f["hm"])
+    np.testing.assert_allclose(g["err"], f["err"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(g["d"], f["d"], rtol=0, atol=1e-13)
+    Li = rpchol.linv_from_F(f["F"], f["piv"])
+    np.testing.assert_allclose(g["Linv"], Li, rtol=0, atol=1e-12 * np.abs(Li).max())
+
+
 def test_rpchol_trace_error_matches_factor():
     X = ks.seeded_mode(600, warm_time=50.0)
     sc = 1.0 / 30.0
