@@ -47,6 +47,9 @@
 #ifndef DUMP_H5
 #define DUMP_H5 0
 #endif
+#ifndef MEM_CHECK
+#define MEM_CHECK 0
+#endif
 
 // The reference's dump points (c1, p1, dtil, cq, pq, Atil, A, R, G, qtil, Btil, W,
 // lam, Z, U in the order of ks_kevd.cu:809-2311) from the library's, which live in
@@ -147,14 +150,16 @@ int main(int argc, char** argv) {
                                 {"kout", KOUT, DriverSetting::kInt, "eigenvectors written to /U (1..256)"},
                                 {"precision", PRECISION == KEVD_FP64 ? 0 : 1, DriverSetting::kPrecision,
                                  "fp64 or mixed (FP32 factor)"},
-                                {"dump", DUMP_H5, DriverSetting::kFlag, "1: also write the dump file"}});
+                                {"dump", DUMP_H5, DriverSetting::kFlag, "1: also write the dump file"},
+                                {"memcheck", MEM_CHECK, DriverSetting::kFlag,
+                                 "1: print device memory in use at labelled points"}});
     cfg.parse(argc, argv);
     const size_t Lfact = cfg.size("lfact"), M = cfg.size("mgrid"), Ndata = cfg.size("ndata"), Nq = cfg.size("nq"),
                  Nrounds = cfg.size("nrounds"), k_out = cfg.size("kout");
     const int blk = cfg.integer("blk");
     const double bw = cfg.get("bw");
     const int32_t precision = cfg.get("precision") == 0 ? KEVD_FP64 : KEVD_MIXED;
-    const bool dump_h5 = cfg.get("dump") != 0;
+    const bool dump_h5 = cfg.get("dump") != 0, mem_check = cfg.get("memcheck") != 0;
     if (Nq < 1 || Nq > Ndata || M < 1 || k_out < 1 || !(bw > 0)) {
         fprintf(stderr, "cukevd: need 1 <= nq <= ndata, mgrid, kout >= 1 and bw > 0\n");
         return 2;
@@ -198,6 +203,7 @@ int main(int argc, char** argv) {
     DRV_CUDA(cudaMalloc(&F, NM * Nr * (precision == KEVD_FP64 ? sizeof(double) : sizeof(float))));
     DRV_CUDA(cudaMalloc(&U_dev, NM * k_out * sizeof(float)));
     DRV_CUDA(cudaMemcpy(u_dev, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (mem_check) mem_probe("post-init");
     DRV_KEVD(ctx, kevd_hankel_rows(ctx, u_dev, (int64_t)Ndata, (int64_t)M, (int64_t)Nq, X_dev, nullptr));
     DRV_KEVD(ctx, kevd_factor_from_linv(ctx, X_dev, (int64_t)NM, (int32_t)Nq, 1.0 / ((double)Nq * bw), spiv.data(),
                                         (int64_t)Nr, linv.data(), precision, F, (int64_t)Nr, nullptr));
@@ -217,8 +223,10 @@ int main(int argc, char** argv) {
         dump = {d_c1.data(), d_dtil.data(), d_cq.data(), d_qtil.data(), d_A.data(), d_B.data(), d_W.data(),
                 d_Z.data()};
     }
+    if (mem_check) mem_probe("pre-pass1");
     DRV_KEVD(ctx, kevd_bistochastic_evd(ctx, F, precision, (int64_t)NM, (int64_t)Nr, (int64_t)Nr, (int32_t)k_out,
                                         lam.data(), U_dev, &info, dump_h5 ? &dump : nullptr, nullptr));
+    if (mem_check) mem_probe("post-pass4");
     std::vector<float> U(NM * k_out);
     DRV_CUDA(cudaMemcpy(U.data(), U_dev, U.size() * sizeof(float), cudaMemcpyDeviceToHost));
     h5_add(out_file, "/lam", lam.data(), lam.size());

@@ -41,6 +41,18 @@
         }                                                           \
     } while (0)
 
+// Device memory in use at a labelled point, in the reference's format
+// (ks_kevd.cu:98-110 mem_probe; one device, so always rank 0).
+inline void mem_probe(const char* label) {
+    DRV_CUDA(cudaDeviceSynchronize());
+    size_t freeb = 0, totalb = 0;
+    DRV_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    const double gib = 1024.0 * 1024.0 * 1024.0;
+    printf("MEM[%-10s] rank 0: used %.3f GiB  free %.3f GiB\n", label, (double)(totalb - freeb) / gib,
+           (double)freeb / gib);
+    fflush(stdout);
+}
+
 template <typename T>
 constexpr int32_t h5_type();
 template <>

@@ -87,5 +87,5 @@ def test_malformed_json_is_rejected(bindir, tmp_path, text):
 def test_help_lists_every_setting(bindir):
     r = _run(bindir, "cukevd", "--help")
     assert r.returncode == 0
-    for key in ("lfact", "mgrid", "ndata", "nq", "blk", "nrounds", "bw", "kout", "precision", "dump"):
+    for key in ("lfact", "mgrid", "ndata", "nq", "blk", "nrounds", "bw", "kout", "precision", "dump", "memcheck"):
         assert f"--{key}" in r.stdout

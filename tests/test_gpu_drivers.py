@@ -122,7 +122,11 @@ def test_cuarpclm_then_cukevd_match_the_oracle(bindir, tmp_path):
     r = spiv.size
     Li = rpchol.linv_from_F(ref["F"], ref["piv"])
     np.testing.assert_allclose(linv.reshape(r, r, order="F"), Li, rtol=0, atol=1e-8 * np.abs(Li).max())
-    out = _run(bindir, d, "cukevd")
+    run = subprocess.run([os.path.join(bindir, "cukevd"), "--memcheck=1"], cwd=d, capture_output=True, text=True,
+                         timeout=600)
+    assert run.returncode == 0, run.stdout + run.stderr
+    mem = [l for l in run.stdout.split("\n") if l.startswith("MEM[")]
+    assert [l[4:14].strip() for l in mem] == ["post-init", "pre-pass1", "post-pass4"]
     out_file = os.path.join(d, "data", f"evd_{N}_{M}_{NQ}_16_{LFACT}.h5")
     assert h5.names(out_file) == ["U", "lam"]
     lam = h5.read(out_file, "/lam")
