@@ -139,3 +139,92 @@ def write(path, datasets: dict) -> None:
     da = (C.c_void_p * max(n, 1))(*[a.ctypes.data for _, a in arrs])
     ct = (C.c_int64 * max(n, 1))(*[a.size for _, a in arrs])
     _check(lib().kevd_h5_write(_b(path), n, nm, ty, da, ct))
+
+
+# ---- the subset of h5py the reference's Python programs use --------------------
+# ks_datagen.py:91-103, ks_preproc.py:17-32 and ks_reference.py:18-47 open files
+# with ``h5py.File(path, "r" | "w")`` as a context manager, read ``f["u"][:]`` and
+# write ``f.create_dataset(name, shape=(n,), dtype=..., data=...)``.  ``File``
+# gives that surface over this library, and ``h5py_module()`` a module object to
+# place in ``sys.modules["h5py"]`` so those programs run unmodified without h5py,
+# writing files that the stage drivers (and libhdf5) read.
+
+class Dataset:
+    """A dataset of an open ``File``: shape, dtype, and indexing (``d[:]``, ``d[...]``)
+    that reads the stored elements."""
+
+    def __init__(self, path, name: str):
+        self._path, self.name = path, name
+        meta = info(path, name)
+        self.shape, self.dtype, self.size = meta["shape"], meta["dtype"], meta["count"]
+
+    def __len__(self):
+        return self.shape[0] if self.shape else 1
+
+    def __getitem__(self, key):
+        return read(self._path, self.name).reshape(self.shape)[key]
+
+    def __array__(self, dtype=None, copy=None):
+        a = read(self._path, self.name).reshape(self.shape)
+        return a if dtype is None else a.astype(dtype)
+
+
+class File:
+    """``File(path, mode)``: "r" reads, "w" creates (truncating), "a" / "r+" add
+    datasets to an existing file ("a" creates it when missing)."""
+
+    def __init__(self, path, mode: str = "r"):
+        self.filename, self.mode = os.fspath(path), mode
+        if mode == "w" or (mode == "a" and not os.path.exists(self.filename)):
+            create(self.filename)
+        elif mode in ("r", "r+", "a"):
+            names(self.filename)          # fails now if the file is missing or not HDF5
+        else:
+            raise ValueError(f"unsupported mode {mode!r}")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
+
+    def close(self):
+        pass                              # every call opens and closes the file itself
+
+    def keys(self):
+        return names(self.filename)
+
+    def __contains__(self, name):
+        return name.lstrip("/") in names(self.filename)
+
+    def __iter__(self):
+        return iter(self.keys())
+
+    def __getitem__(self, name: str) -> Dataset:
+        return Dataset(self.filename, name)
+
+    def create_dataset(self, name: str, shape=None, dtype=None, data=None) -> Dataset:
+        if self.mode == "r":
+            raise H5Error(1, f"{self.filename} is open read-only")
+        if data is None:
+            if shape is None:
+                raise ValueError("create_dataset needs shape or data")
+            data = np.zeros(shape, dtype=dtype if dtype is not None else np.float32)
+        a = np.asarray(data, dtype=dtype)
+        if shape is not None:
+            shape = (shape,) if np.isscalar(shape) else tuple(shape)
+            a = a.reshape(shape)
+        if a.ndim != 1:
+            raise H5Error(5, "one-dimensional datasets only (as the reference writes them)")
+        append(self.filename, name, a)
+        return Dataset(self.filename, name)
+
+
+def h5py_module():
+    """A module with ``File``, for ``sys.modules["h5py"]``."""
+    import types
+    m = types.ModuleType("h5py")
+    m.File = File
+    m.Dataset = Dataset
+    return m

@@ -10,6 +10,11 @@ h5py (absent here).  This script therefore
   * shrinks the size constants in the program text before executing it
     (``Nequil``/``Nfinal`` of ks_datagen.py, ``Ntrue`` of ks_preproc.py,
     ``N`` of ks_reference.py); the algorithms run unmodified.
+
+``--check-h5`` runs the same three programs again with this repository's HDF5
+layer in place of h5py (``kernel_evd_gb300.h5.h5py_module()``), in a scratch
+directory, writing real HDF5 files, and checks that every dataset read back from
+them equals the committed fixture bit for bit.
 """
 from __future__ import annotations
 
@@ -97,5 +102,40 @@ def main():
     print("wrote ks_reference_small.npz:", {k: v.shape for k, v in out.items()})
 
 
+def check_h5_layer():
+    import tempfile
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from kernel_evd_gb300 import h5
+    sys.modules["h5py"] = h5.h5py_module()
+    g = np.load(os.path.join(HERE, "ks_reference_small.npz"))
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        os.makedirs("data")
+        try:
+            _run("ks_datagen.py", [(r"Nequil = 10000", "Nequil = 40"), (r"Nfinal = 512", "Nfinal = 32")])
+            Ntrue, M = 32 + 64 - 1, 64
+            _run("ks_preproc.py", [(r"Ntrue = 575", f"Ntrue = {Ntrue}")])
+            N = Ntrue - 64 + 1
+            _run("ks_reference.py", [(r"N = 512 ", f"N = {N} ")])
+            f = f"data/ks_true_{Ntrue}_{M}_7"
+            got = {
+                "datagen_u": h5.read(f + ".h5", "/u").reshape((Ntrue, M), order="F"),
+                "datagen_t": h5.read(f + ".h5", "/t"),
+                "datagen_u32": h5.read(f + "_u32.h5", "/u"),
+                "udelay": h5.read(f"data/ks_train_{N * M}_64_7_udelay.h5", "/u").reshape((N * M, 64), order="F"),
+                "ref_eigvals": h5.read(f"data/evd_ref_{N}_{M}_64_7.h5", "/eigvals"),
+                "ref_eigvecs_top16": h5.read(f"data/evd_ref_{N}_{M}_64_7.h5", "/eigvecs").reshape(
+                    (N * M, N * M), order="F")[:, :16],
+            }
+        finally:
+            os.chdir(cwd)
+    bad = [k for k, v in got.items() if v.dtype != g[k].dtype or v.tobytes() != g[k].tobytes()]
+    print("HDF5 round trip of the reference's programs:", "all equal" if not bad else f"differ: {bad}")
+    return not bad
+
+
 if __name__ == "__main__":
+    if "--check-h5" in sys.argv:
+        sys.exit(0 if check_h5_layer() else 1)
     main()

@@ -184,6 +184,36 @@ def test_version2_headers_link_messages_and_continuations(tmp_path):
     assert e.value.name == "KEVD_H5_ERR_UNSUPPORTED"
 
 
+def test_h5py_subset_in_the_reference_call_pattern(tmp_path):
+    """The calls of ks_datagen.py:91-103 and ks_preproc.py:17-32 (h5py.File as a context
+    manager, create_dataset(name, shape, dtype, data), f["u"][:]) on the golden
+    fixture's arrays, through ``h5.h5py_module()``: what is read equals what was written."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ks_reference_small.npz"))
+    h5py = h5.h5py_module()
+    usave = g["datagen_u"]
+    Ntrue, M = usave.shape
+    p = tmp_path / "ks_true.h5"
+    with h5py.File(p, "w") as f:
+        f.create_dataset("u", shape=(Ntrue * M,), dtype=np.float32, data=usave.astype(np.float32).flatten(order="F"))
+        f.create_dataset("t", shape=(Ntrue,), dtype=np.float64, data=g["datagen_t"])
+    with h5py.File(p, "r") as f:
+        assert sorted(f.keys()) == ["t", "u"] and "u" in f and "/t" in f
+        utrue = f["u"][:].reshape((Ntrue, M), order="F")
+        assert f["u"].shape == (Ntrue * M,) and f["u"].dtype == np.float32 and len(f["t"]) == Ntrue
+        assert np.asarray(f["t"]).tobytes() == g["datagen_t"].tobytes()
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("x", data=np.zeros(3))
+    assert utrue.tobytes() == usave.astype(np.float32).tobytes()
+    assert h5.read(p, "/u").tobytes() == g["datagen_u32"].tobytes()     # what the drivers read
+    with h5py.File(p, "a") as f:
+        f.create_dataset("extra", data=np.arange(4))
+    assert h5.names(p) == ["extra", "t", "u"]
+    with pytest.raises(h5.H5Error):
+        h5py.File(p, "w").create_dataset("m", data=np.zeros((2, 2)))
+    with pytest.raises(h5.H5Error):
+        h5py.File(tmp_path / "none.h5", "r")
+
+
 def test_corrupt_files_are_errors_not_crashes(tmp_path):
     """Truncated or byte-flipped files end in a status, never in a crash (run in a
     child process so that a crash fails this test instead of the session)."""
