@@ -317,7 +317,7 @@ static int obj_read(h5file* h, uint64_t addr, h5obj* o) {
     h5span* conts = (h5span*)malloc(kMaxChunks * sizeof(h5span));
     if (!conts) return fail(KEVD_H5_ERR_IO, "out of host memory");
     int nconts = 0, s = KEVD_H5_OK, v2 = 0, track = 0;
-    uint8_t pre[40];
+    uint8_t pre[40] = {0};
     uint8_t* chunk = NULL;
     s = rd(h, addr, pre, 16);
     if (s) goto done;
