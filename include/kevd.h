@@ -310,8 +310,9 @@ int kevd_weighted_gram2(kevd_ctx* ctx, const void* F, int32_t precision,
  * N x k_out float row-major, columns ascending (the last is the leading
  * eigenvector), k_out <= 256 (the reference's k_out, ks_kevd.cu:481); the
  * reference's /lam and /U (ks_kevd.cu:1932-1940, :2301-2308).  In the mixed
- * form the leading k_out <= 32 eigenpairs are refined against F in FP64
- * (Rayleigh-Ritz); beyond 32 they come from the k x k eigensolve. */
+ * form the leading min(k_out, 32) eigenpairs (eigenvalues and U columns) are
+ * refined against F in FP64 (Rayleigh-Ritz); the others come from the k x k
+ * eigensolve. */
 int kevd_bistochastic_evd(kevd_ctx* ctx, const void* F, int32_t precision,
                           int64_t N, int64_t k, int64_t ldF, int32_t k_out,
                           double* lam, float* U, kevd_evd_info* info,

@@ -1139,14 +1139,28 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
                                CUBLAS_DIAG_NON_UNIT, (int)k, k_out, &one, A, (int)k, Z, (int)k));
     // pass 4: U = Dtil^{-1} F Z
     float* Yrr = nullptr;   // Dtil^{-1} U for the Rayleigh-Ritz T1 pass (FP32 factor)
+    float* Urr = nullptr;   // the leading columns the Rayleigh-Ritz refines (U itself for k_out <= 32)
+    const int m_rr = (int)std::min<int64_t>(k_out, 32);
     {
         ProfScope ps(ctx, "ev_u", s);
         if (sizeof(T) == 4 && k_out <= 32) {
             Yrr = arena_get<float>(ctx, "ev.Yrr", (size_t)N * 32, &st);
             if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
             evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z, k_out, dinv, U, Yrr);
-        } else
+            Urr = U;
+        } else {
             ev_u_kernel<T><<<dim3(ceil_div(N, 64), ceil_div(k_out, 64)), 256, 0, s>>>(F, ldF, N, k, Z, k_out, dinv, U);
+            if (sizeof(T) == 4) {
+                // FP32 factor with k_out > 32: the leading 32 columns once more, with
+                // Y, for their refinement (Z's last 32 columns)
+                KEVD_LAUNCH(ctx);
+                Yrr = arena_get<float>(ctx, "ev.Yrr", (size_t)N * 32, &st);
+                Urr = arena_get<float>(ctx, "ev.Urr", (size_t)N * 32, &st);
+                if (st != KEVD_OK) return set_error(ctx, st, "bistochastic_evd: out of device memory");
+                evt_u_kernel<<<ceil_div(N, 256), 256, 0, s>>>(FT, ldT, N, k, Z + (size_t)(k_out - 32) * k, 32, dinv,
+                                                              Urr, Yrr);
+            }
+        }
         KEVD_LAUNCH(ctx);
     }
     if (dump) KEVD_TRY(d2h(ctx, dump->Z, Z, (size_t)k * k_out, s));
@@ -1155,12 +1169,16 @@ static int evd_impl(kevd_ctx* ctx, const T* F, int64_t N, int64_t k, int64_t ldF
     KEVD_CUDA(ctx, cudaMemcpyAsync(hflags, flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (lam_h) KEVD_CUDA(ctx, cudaMemcpyAsync(lam_h, lam, k * sizeof(double), cudaMemcpyDeviceToHost, s));
     KEVD_CUDA(ctx, cudaStreamSynchronize(s));
-    if (sizeof(T) == 4 && hflags[2] == 0 && hflags[3] == 0 && k_out <= 32) {
-        // FP32 factor: refine the leading k_out eigenpairs by Rayleigh-Ritz in FP64
+    if (sizeof(T) == 4 && hflags[2] == 0 && hflags[3] == 0) {
+        // FP32 factor: refine the leading min(k_out, 32) eigenpairs by Rayleigh-Ritz
+        // in FP64; with k_out > 32 the refined columns replace U's last 32
         double top[32];
-        KEVD_TRY(rayleigh_ritz(ctx, FT, ldT, N, k, k_out, U, Yrr, qinv, top, s));
+        KEVD_TRY(rayleigh_ritz(ctx, FT, ldT, N, k, m_rr, Urr, Yrr, qinv, top, s));
+        if (Urr != U)
+            KEVD_CUDA(ctx, cudaMemcpy2DAsync(U + (k_out - 32), (size_t)k_out * sizeof(float), Urr, 32 * sizeof(float),
+                                             32 * sizeof(float), (size_t)N, cudaMemcpyDeviceToDevice, s));
         if (lam_h)
-            for (int j = 0; j < k_out; ++j) lam_h[k - k_out + j] = top[j];
+            for (int j = 0; j < m_rr; ++j) lam_h[k - m_rr + j] = top[j];
     }
     if (info) {
         info->trace_A = htr[0];

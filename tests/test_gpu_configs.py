@@ -69,6 +69,7 @@ def test_c1_plain_fp64_pipeline_against_oracle(ctx, c1_states):
 
 def test_mixed_factorisation_and_evd_against_fp64_on_same_pivots(ctx):
     from kernel_evd_gb300 import api, datagen
+    from oracle import evd
     X = datagen.seeded_states(200_000, L=22.0, M=64, seed=0, warm_time=1000.0, dt=0.25)
     Xd = torch.from_numpy(X).cuda()
     eps = _eps_exact_median(ctx, Xd[:20_000].contiguous())
@@ -81,6 +82,17 @@ def test_mixed_factorisation_and_evd_against_fp64_on_same_pivots(ctx):
     e64 = api.bistochastic_evd(ctx, F64, k_out=top)
     err = np.abs(em.lam[-top:] - e64.lam[-top:])
     assert err.max() <= 1e-8, f"top-{top} eigenvalue error {err.max():.3e} (leading {err[::-1][:4]})"
+    # more eigenvectors than the refinement covers (the reference's k_out = 256 is of
+    # this kind): the leading 32 pairs are refined all the same
+    em64 = api.bistochastic_evd(ctx, m.factor, k_out=64)
+    err64 = np.abs(em64.lam[-top:] - e64.lam[-top:])
+    assert err64.max() <= 1e-8, f"k_out = 64: top-{top} eigenvalue error {err64.max():.3e}"
+    assert abs(em64.lam[-1] - 1.0) <= 1e-8
+    U32, U64 = em.U.cpu().numpy().astype(np.float64), em64.U.cpu().numpy().astype(np.float64)
+    # the refined leading eigenvector (lambda = 1, well separated; the pairs below it
+    # may be nearly degenerate) agrees with the k_out = 32 run's up to sign
+    ang = evd.eigvec_angles(U64[:, -1:], U32[:, -1:])
+    assert ang[0] < 1e-4, ang
     # trace error of the mixed run against the FP64 factor of the same pivots
     t64 = float((X.shape[0] - torch.sum(F64 * F64).item()) / X.shape[0])
     assert abs(m.trace_error - t64) <= 1e-6 + 1e-3 * t64
