@@ -352,15 +352,17 @@ int kevd_factor_from_linv(kevd_ctx* ctx, const float* X, int64_t N, int32_t d, d
     KEVD_CUDA(ctx, cudaMemcpyAsync(idx, piv, r * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     KEVD_CUDA(ctx, cudaMemcpyAsync(Li, Linv, (size_t)r * r * sizeof(double), cudaMemcpyHostToDevice, s));
     KEVD_BLAS(ctx, cublasSetStream(ctx->blas, s));
-    const double one = 1.0, zero = 0.0;
+    const double one = 1.0;
     for (int64_t r0 = 0; r0 < N; r0 += rows) {
         const int64_t nr = std::min(rows, N - r0);
         KEVD_TRY(launch_kernel_block(ctx, X, N, d, scale, nullptr, r0, nr, idx, r, KEVD_FP64, Kp, r, s));
-        // (F panel)^T = Linv * (K panel)^T  in column-major terms
+        // (F panel)^T = Linv * (K panel)^T  in column-major terms; Linv is lower
+        // triangular (its upper part is never read), half the FP64 work of a GEMM
         double* dst = precision == KEVD_FP64 ? (double*)F + r0 * ldF : Fp;
         const int64_t ldd = precision == KEVD_FP64 ? ldF : r;
-        KEVD_BLAS(ctx, cublasDgemm(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)r, (int)nr, (int)r, &one,
-                                   Li, (int)r, Kp, (int)r, &zero, dst, (int)ldd));
+        KEVD_BLAS(ctx, cublasDtrmm(ctx->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                   CUBLAS_DIAG_NON_UNIT, (int)r, (int)nr, &one, Li, (int)r, Kp, (int)r, dst,
+                                   (int)ldd));
         if (precision == KEVD_MIXED) {
             const int grid = (int)std::min<int64_t>((nr * r + 255) / 256, (int64_t)ctx->num_sms * 16);
             cast_d2f_kernel<<<grid, 256, 0, s>>>(Fp, nr, r, r, (float*)F + r0 * ldF, ldF);

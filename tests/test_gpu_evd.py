@@ -84,6 +84,10 @@ def test_factor_from_linv_roundtrip(ctx, fac):
     Xt = torch.from_numpy(X).cuda()
     F = api.factor_from_linv(ctx, Xt, SCALE, r["piv"], Li, precision="fp64").cpu().numpy()
     np.testing.assert_allclose(F, r["F"], rtol=0, atol=1e-8)
+    # L^{-1} is lower triangular: whatever its upper part holds is not read
+    Lg = Li + np.triu(np.random.default_rng(0).standard_normal(Li.shape), 1)
+    Fg = api.factor_from_linv(ctx, Xt, SCALE, r["piv"], Lg, precision="fp64").cpu().numpy()
+    assert Fg.tobytes() == F.tobytes()
     e_lm = evd.evd_from_linv(X.astype(np.float64), SCALE, Li, r["piv"], 8)
     g = api.bistochastic_evd(ctx, torch.from_numpy(F).cuda(), k_out=8)
     np.testing.assert_allclose(g.lam[-8:], e_lm["lam"][-8:], rtol=1e-9)
