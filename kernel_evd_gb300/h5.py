@@ -228,3 +228,35 @@ def h5py_module():
     m.File = File
     m.Dataset = Dataset
     return m
+
+
+def _main(argv=None) -> int:
+    """``python -m kernel_evd_gb300.h5 FILE [DATASET]``: the root group's datasets
+    with their element type and shape (like ``h5ls``), or one dataset's first values."""
+    import argparse
+    ap = argparse.ArgumentParser(prog="python -m kernel_evd_gb300.h5")
+    ap.add_argument("file")
+    ap.add_argument("dataset", nargs="?")
+    ap.add_argument("-n", type=int, default=8, help="values shown with a dataset name")
+    a = ap.parse_args(argv)
+    try:
+        if a.dataset:
+            meta = info(a.file, a.dataset)
+            v = read(a.file, a.dataset)
+            print(f"{a.dataset}: {meta['dtype']} {meta['shape']}")
+            print(" ".join(repr(x.item()) for x in v[: a.n]) + (" ..." if v.size > a.n else ""))
+        else:
+            for name in names(a.file):
+                try:
+                    meta = info(a.file, name)
+                    print(f"{name:24s} {str(meta['dtype']):8s} {meta['shape']}")
+                except H5Error as e:
+                    print(f"{name:24s} ({e.name})")
+    except H5Error as e:
+        print(f"{a.file}: {e}")
+        return 1
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

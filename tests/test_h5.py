@@ -214,6 +214,19 @@ def test_h5py_subset_in_the_reference_call_pattern(tmp_path):
         h5py.File(tmp_path / "none.h5", "r")
 
 
+def test_listing_tool(tmp_path):
+    p = tmp_path / "l.h5"
+    h5.write(p, {"lam": np.array([0.25, 0.5, 1.0]), "spiv": np.arange(5, dtype=np.uint64)})
+    run = lambda *a: subprocess.run([sys.executable, "-m", "kernel_evd_gb300.h5", *a], cwd=ROOT,
+                                    capture_output=True, text=True, timeout=60)
+    r = run(str(p))
+    assert r.returncode == 0 and r.stdout.split() == ["lam", "float64", "(3,)", "spiv", "uint64", "(5,)"]
+    r = run(str(p), "/lam", "-n", "2")
+    assert r.returncode == 0 and r.stdout.split("\n")[1] == "0.25 0.5 ..."
+    r = run(str(tmp_path / "missing.h5"))
+    assert r.returncode == 1 and "KEVD_H5_ERR_IO" in r.stdout
+
+
 def test_corrupt_files_are_errors_not_crashes(tmp_path):
     """Truncated or byte-flipped files end in a status, never in a crash (run in a
     child process so that a crash fails this test instead of the session)."""
