@@ -34,6 +34,8 @@
  *
  * Entry points return KEVD_H5_OK or an error code; kevd_h5_last_error() describes the
  * last failure on the calling thread.  No function keeps a file open between calls.
+ * Reads of one file may run concurrently; an append must not overlap any other call on
+ * the same file (as with libhdf5 without its thread-safe build).
  */
 #ifndef KEVD_H5_H
 #define KEVD_H5_H
