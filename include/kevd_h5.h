@@ -23,8 +23,9 @@
  *          integers of either byte order;
  *   write: superblock version 0 with 8-byte offsets and lengths, a symbol-table root
  *          group, one-dimensional contiguous datasets of float32, float64, int32,
- *          uint32, int64, uint64 (little-endian): the layout libhdf5 writes with its
- *          default ("earliest") format settings, which every HDF5 reader accepts.
+ *          uint32, int64, uint64 (little-endian): the structures libhdf5 writes with its
+ *          default ("earliest") format settings (compared with a libhdf5-written file;
+ *          no libhdf5 was at hand to read these files back).
  *
  * Chunked or filtered (compressed) datasets, dense (fractal-heap) groups, committed
  * datatypes, external storage and virtual datasets are reported as
