@@ -227,6 +227,42 @@ def test_listing_tool(tmp_path):
     assert r.returncode == 1 and "KEVD_H5_ERR_IO" in r.stdout
 
 
+def test_reader_paths_the_writer_does_not_make(tmp_path):
+    """Big-endian elements, 1- and 2-byte integers, a scalar and a 2-D dataspace, compact
+    storage and a dataset inside a group, in a file built here from the specification."""
+    f64 = np.linspace(-2.0, 3.0, 12).reshape(3, 4)
+    i16 = np.array([-300, -1, 0, 1, 32767], dtype=np.int16)
+    u8 = np.array([0, 7, 255], dtype=np.uint8)
+    f32 = np.array([1.5, -2.25, 3.0e-8], dtype=np.float32)
+    p = tmp_path / "paths.h5"
+    p.write_bytes(_v2_file({"be2d": (f64, {"be": True}),
+                            "i16be": (i16, {"be": True}),
+                            "u8": u8,
+                            "scalar": (np.array([0.75], dtype=np.float32), {"shape": ()}),
+                            "compact": (np.arange(5, dtype=np.int32), {"compact": True}),
+                            "f32be": (f32, {"be": True})},
+                           group=("grp", {"x": np.array([4.0, 5.0])})))
+    assert h5.names(p) == ["be2d", "i16be", "u8", "scalar", "compact", "f32be", "grp"]
+    meta = h5.info(p, "be2d")
+    assert meta["shape"] == (3, 4) and meta["dtype"] == np.float64
+    assert h5.read(p, "be2d").tobytes() == f64.ravel().tobytes()
+    assert h5.info(p, "i16be")["dtype"] == np.int32
+    np.testing.assert_array_equal(h5.read(p, "i16be"), i16.astype(np.int32))
+    assert h5.info(p, "u8")["dtype"] == np.uint32
+    np.testing.assert_array_equal(h5.read(p, "u8", np.float64), u8.astype(np.float64))
+    meta = h5.info(p, "scalar")
+    assert meta["rank"] == 0 and meta["count"] == 1 and h5.read(p, "scalar")[0] == np.float32(0.75)
+    np.testing.assert_array_equal(h5.read(p, "compact"), np.arange(5, dtype=np.int32))
+    np.testing.assert_array_equal(h5.read(p, "/f32be", np.float64), f32.astype(np.float64))
+    np.testing.assert_array_equal(h5.read(p, "/grp/x"), [4.0, 5.0])
+    with pytest.raises(h5.H5Error) as e:
+        h5.read(p, "/grp")
+    assert e.value.name == "KEVD_H5_ERR_ARG"
+    with pytest.raises(h5.H5Error) as e:
+        h5.read(p, "/grp/y")
+    assert e.value.name == "KEVD_H5_ERR_NOTFOUND"
+
+
 def test_corrupt_files_are_errors_not_crashes(tmp_path):
     """Truncated or byte-flipped files end in a status, never in a crash (run in a
     child process so that a crash fails this test instead of the session)."""
@@ -377,48 +413,80 @@ def _check_dataset(b, oh, eof):
 
 # ----------------------------------------------------------------- a version-2 file
 
-def _v2_file(datasets):
+def _v2_file(datasets, group=None):
     """Superblock v2, root object header v2 whose link messages sit half in the first
     chunk and half in a continuation block, dataset headers v2 with dataspace v2,
-    layout v4 contiguous.  Checksums are left zero (the reader does not verify them)."""
+    layout v4.  ``datasets``: name -> array, or name -> (array, options) with options
+    ``be`` (big-endian elements), ``shape`` (() for a scalar dataspace) and ``compact``
+    (the elements inside the layout message).  ``group``: (name, datasets) of one
+    subgroup linked from the root.  Checksums are left zero (the reader does not
+    verify them)."""
     out = bytearray(48)                                          # superblock v2: 12 + 4 * 8 + 4
-    data_at, headers = {}, {}
-    for k, a in datasets.items():
-        out += bytes((-len(out)) % 16)
-        data_at[k] = len(out)
-        out += a.tobytes()
 
     def ohdr(msgs):
         body = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in msgs)
         return b"OHDR" + bytes([2, 0x02]) + struct.pack("<I", len(body)) + body + bytes(4)
 
-    for k, a in datasets.items():
-        space = bytes([2, 1, 0, 1]) + struct.pack("<Q", a.size)
-        if a.dtype.kind == "f":
-            dt = bytes([0x11, 0x20, 63, 0]) + struct.pack("<IHHBBBBI", 8, 0, 64, 52, 11, 0, 52, 1023)
-        else:
-            dt = bytes([0x10, 0x08, 0, 0]) + struct.pack("<IHH", a.itemsize, 0, 8 * a.itemsize)
-        layout = bytes([4, 1]) + struct.pack("<QQ", data_at[k], a.nbytes)
-        out += bytes((-len(out)) % 8)
-        headers[k] = len(out)
-        out += ohdr([(0x01, space), (0x03, dt), (0x08, layout)])
-
     def link(name, addr):
         nm = name.encode()
         return bytes([1, 0]) + bytes([len(nm)]) + nm + struct.pack("<Q", addr)
 
-    keys = list(datasets)
+    def put_dataset(a, be=False, shape=None, compact=False):
+        a = np.asarray(a)
+        raw = a.astype(a.dtype.newbyteorder(">" if be else "<")).tobytes()
+        shape = a.shape if shape is None else shape
+        if shape == ():
+            space = bytes([2, 0, 0, 0])
+        else:
+            space = bytes([2, len(shape), 0, 1]) + b"".join(struct.pack("<Q", n) for n in shape)
+        order = 1 if be else 0
+        if a.dtype.kind == "f":
+            if a.itemsize == 8:
+                dt = bytes([0x11, 0x20 | order, 63, 0]) + struct.pack("<IHHBBBBI", 8, 0, 64, 52, 11, 0, 52, 1023)
+            else:
+                dt = bytes([0x11, 0x20 | order, 31, 0]) + struct.pack("<IHHBBBBI", 4, 0, 32, 23, 8, 0, 23, 127)
+        else:
+            sign = 0x08 if a.dtype.kind == "i" else 0
+            dt = bytes([0x10, sign | order, 0, 0]) + struct.pack("<IHH", a.itemsize, 0, 8 * a.itemsize)
+        if compact:
+            layout = bytes([4, 0]) + struct.pack("<H", len(raw)) + raw
+        else:
+            out.extend(bytes((-len(out)) % 16))
+            at = len(out)
+            out.extend(raw)
+            layout = bytes([4, 1]) + struct.pack("<QQ", at, len(raw))
+        out.extend(bytes((-len(out)) % 8))
+        addr = len(out)
+        out.extend(ohdr([(0x01, space), (0x03, dt), (0x08, layout)]))
+        return addr
+
+    def put_all(ds):
+        addrs = {}
+        for k, v in ds.items():
+            a, opt = v if isinstance(v, tuple) else (v, {})
+            addrs[k] = put_dataset(a, **opt)
+        return addrs
+
+    headers = put_all(datasets)
+    if group is not None:
+        gname, gds = group
+        ga = put_all(gds)
+        linfo = bytes([0, 0]) + struct.pack("<QQ", 2 ** 64 - 1, 2 ** 64 - 1)
+        out.extend(bytes((-len(out)) % 8))
+        headers[gname] = len(out)
+        out.extend(ohdr([(0x02, linfo)] + [(0x06, link(k, a)) for k, a in ga.items()]))
+    keys = list(headers)
     cont_links = [(0x06, link(k, headers[k])) for k in keys[1:]]
     cont_body = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in cont_links)
-    out += bytes((-len(out)) % 8)
+    out.extend(bytes((-len(out)) % 8))
     cont_at = len(out)
-    out += b"OCHK" + cont_body + bytes(4)
+    out.extend(b"OCHK" + cont_body + bytes(4))
     linfo = bytes([0, 0]) + struct.pack("<QQ", 2 ** 64 - 1, 2 ** 64 - 1)
     root_msgs = [(0x02, linfo), (0x06, link(keys[0], headers[keys[0]])),
                  (0x10, struct.pack("<QQ", cont_at, 8 + len(cont_body)))]
-    out += bytes((-len(out)) % 8)
+    out.extend(bytes((-len(out)) % 8))
     root_at = len(out)
-    out += ohdr(root_msgs)
+    out.extend(ohdr(root_msgs))
     sb = b"\x89HDF\r\n\x1a\n" + bytes([2, 8, 8, 0]) + struct.pack("<QQQQ", 0, 2 ** 64 - 1, len(out), root_at)
     out[:48] = sb + bytes(4)
     return bytes(out)
