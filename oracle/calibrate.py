@@ -10,7 +10,11 @@ Restates ``ks_bandwidth.cu``:
 * the post-processing on rank 0 (``ks_bandwidth.cu:612-656``):
   ``logS = log(2 T/NM + 1)``, the centred slope, the first arg-max over
   ``i in [0, Nbw-3)``, ``eopt = bw[idmax+1]``, ``mdim = 2 slope[idmax]``;
-* the ``bw0.out`` text layout (``ks_bandwidth.cu:645-655``).
+* the ``bw0.out`` text layout (``ks_bandwidth.cu:645-655``);
+* the flat index of the strict lower triangle that the reference's batches walk
+  (``tri_count`` / ``tri_ind``, ``ks_bandwidth.cu:104-136``: column-major order, the
+  column from a square-root solve in FP64 corrected by integer comparisons), and the
+  pair sums taken in that order (``pair_sums_flat``).
 
 It also provides the log-spaced sweep around the median squared distance used
 by the dense-state workloads (41 or 64 values in ``2^-10 .. 2^10 x median``).
@@ -50,6 +54,49 @@ def pair_sums(X: np.ndarray, scales: np.ndarray, block: int = 2048) -> np.ndarra
         ii = np.arange(r0, r1)[:, None]
         ll = np.arange(r1)[None, :]
         D = D[ii > ll]
+        for j, s in enumerate(scales):
+            T[j] += np.exp(-s * D).sum()
+    return T
+
+
+def tri_count(k, N: int):
+    """Entries of the strict lower triangle of an N x N matrix in the columns before k
+    (exact integers)."""
+    k = np.asarray(k, dtype=np.int64)
+    return k * (2 * N - 1 - k) // 2
+
+
+def tri_ind(p, N: int):
+    """(row, col) of flat indices p of the strict lower triangle, column-major: the
+    column is the largest k with tri_count(k) <= p, from the root of the quadratic in
+    FP64, truncated, then moved down or up until the integer comparisons hold."""
+    p = np.asarray(p, dtype=np.int64)
+    a = 2.0 * N - 1.0
+    disc = a * a - 8.0 * p.astype(np.float64)
+    k = np.trunc((a - np.sqrt(np.maximum(disc, 0.0))) / 2.0).astype(np.int64)
+    k = np.maximum(k, 0)
+    down = (k > 0) & (tri_count(k, N) > p)
+    while down.any():
+        k[down] -= 1
+        down = (k > 0) & (tri_count(k, N) > p)
+    up = tri_count(k + 1, N) <= p
+    while up.any():
+        k[up] += 1
+        up = tri_count(k + 1, N) <= p
+    return k + 1 + p - tri_count(k, N), k
+
+
+def pair_sums_flat(X: np.ndarray, scales: np.ndarray, batch: int = 1 << 16) -> np.ndarray:
+    """``pair_sums`` with the pairs visited in batches of the flat index, as the
+    reference's distance batches are (``ks_bandwidth.cu:537-577``)."""
+    X = np.asarray(X, dtype=np.float64)
+    scales = np.asarray(scales, dtype=np.float64)
+    N = X.shape[0]
+    total = N * (N - 1) // 2
+    T = np.zeros(scales.size, dtype=np.float64)
+    for p0 in range(0, total, batch):
+        i, l = tri_ind(np.arange(p0, min(total, p0 + batch)), N)
+        D = ((X[i] - X[l]) ** 2).sum(axis=1)
         for j, s in enumerate(scales):
             T[j] += np.exp(-s * D).sum()
     return T

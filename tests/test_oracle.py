@@ -120,6 +120,38 @@ def test_calibration_selection_reference_sweep():
     assert len(txt.strip().split("\n")) == (bw.size - 2) + 3
 
 
+@pytest.mark.parametrize("N", [2, 3, 7, 64, 1001])
+def test_flat_triangle_index_is_a_bijection(N):
+    """tri_ind maps 0 .. N(N-1)/2 - 1 onto the strict lower triangle, column by column."""
+    total = N * (N - 1) // 2
+    row, col = calibrate.tri_ind(np.arange(total), N)
+    want_col, want_row = np.nonzero(np.tril(np.ones((N, N), dtype=bool), -1).T)
+    np.testing.assert_array_equal(col, want_col)
+    np.testing.assert_array_equal(row, want_row)
+
+
+def test_flat_triangle_index_at_column_boundaries_of_large_matrices():
+    """Where the square root rounds the wrong way: the first and last index of columns
+    of the reference's calibration size (NM = 524,288) and of N = 4,194,304 agree with
+    exact integer arithmetic."""
+    rng = np.random.default_rng(3)
+    for N in (524_288, 4_194_304):
+        k = np.concatenate([np.arange(0, 64), N - 2 - np.arange(64), rng.integers(0, N - 1, 4000)])
+        first = calibrate.tri_count(k, N)
+        last = calibrate.tri_count(k + 1, N) - 1
+        for p, want_col, want_row in ((first, k, k + 1), (last, k, np.full_like(k, N - 1))):
+            row, col = calibrate.tri_ind(p, N)
+            np.testing.assert_array_equal(col, want_col)
+            np.testing.assert_array_equal(row, want_row)
+
+
+def test_pair_sums_in_flat_order_match_blocked():
+    X = ks.seeded_mode(700, warm_time=20.0)
+    scales = 1.0 / np.array([0.5, 5.0, 50.0])
+    np.testing.assert_allclose(calibrate.pair_sums_flat(X, scales, batch=10_000), calibrate.pair_sums(X, scales),
+                               rtol=1e-12)
+
+
 def test_pair_sums_bruteforce():
     rng = np.random.default_rng(0)
     X = rng.standard_normal((37, 5))
